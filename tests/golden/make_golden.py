@@ -1,0 +1,276 @@
+"""Generate the golden fixtures by running the reference DFTpy here.
+
+Run from the repository root:  ``python tests/golden/make_golden.py [name ...]``
+
+It imports the reference from its source tree through the two shims in
+``_shims/`` (see ``refenv.py``) and writes small ``.npz`` files next to this
+script.  The GPU tests and the CPU oracle tests read only those ``.npz``
+files; the reference tree is not needed to run them.
+
+Fixtures
+--------
+fde.npz      the reference's own test density ``Al_fde_rho.pp`` (2 Al,
+             36x36x72) with each functional's energy, potential samples and
+             potential checksums, Ewald terms and forces (reference tests
+             ``test_functional.py:24-34``, ``test_ewald.py:33-54``).
+al4.npz      32^3, 4 Al: full TN optimisation (TFVW+LDA+Hartree+analytic PP,
+             PME), converged density, energies, forces, evaluation counts.
+al256.npz    128^3, 256 Al, WT: full TN optimisation; scalars and a density
+             sample (the full field is 16 MB).
+dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
+             (``LineSearchDcsrch2``) on analytic 1-D functions.
+"""
+import os
+import sys
+import time
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(ROOT))
+
+import refenv  # noqa: E402
+
+refenv.load()
+
+from dftpy.field import DirectField  # noqa: E402
+from dftpy.formats import io  # noqa: E402
+from dftpy.functional import Functional, TotalFunctional  # noqa: E402
+from dftpy.functional.pseudo import LocalPseudo  # noqa: E402
+from dftpy.functional.pseudo.abstract_pseudo import BasePseudo  # noqa: E402
+from dftpy.grid import DirectGrid  # noqa: E402
+from dftpy.ions import Ions  # noqa: E402
+from dftpy.ewald import ewald  # noqa: E402
+from dftpy.optimization import Optimization  # noqa: E402
+from dftpy.time_data import TimeData  # noqa: E402
+from dftpy.math_utils import LineSearchDcsrch2  # noqa: E402
+
+from dftpy_gb300 import systems  # noqa: E402
+
+NSAMPLE = 2000
+
+
+class AnalyticPP(BasePseudo):
+    """BasePseudo holding the analytic v(G) table (``direct=False``)."""
+
+    def __init__(self, Z, rc):
+        super().__init__(fname=None, direct=False)
+        self._zval = float(Z)
+        self.r, self.v = systems.analytic_pp_table(Z, rc)
+
+
+def pp_list(symbols):
+    return {s: AnalyticPP(*systems.SPECIES[s]) for s in sorted(set(symbols))}
+
+
+def sample_index(n, seed=123):
+    return np.sort(np.random.default_rng(seed).choice(n, size=min(NSAMPLE, n), replace=False))
+
+
+def checksums(v):
+    v = np.asarray(v, dtype=np.float64).ravel()
+    return np.array([v.sum(), (v * v).sum(), np.abs(v).max(), v.min(), v.max()])
+
+
+def ref_ions(st):
+    return Ions(symbols=list(st.symbols), positions=st.positions.copy(), cell=st.lattice.copy(), units="au")
+
+
+class CountingEvaluator:
+    """Wrap a TotalFunctional and count its evaluations by kind."""
+
+    def __init__(self, func):
+        self.func = func
+        self.n_ev = 0
+        self.n_v = 0
+        self.energies = []
+
+    def __call__(self, rho, calcType={"E", "V"}, **kw):
+        out = self.func(rho, calcType=calcType, **kw)
+        if "E" in calcType:
+            self.n_ev += 1
+            self.energies.append(float(out.energy))
+        else:
+            self.n_v += 1
+        return out
+
+
+def component_outputs(rho, funcs):
+    res = {}
+    for name, f in funcs.items():
+        out = f(rho, calcType={"E", "V"})
+        res[name] = (float(out.energy), np.asarray(out.potential))
+    return res
+
+
+def gen_fde():
+    ions, rho, _ = io.read_all(refenv.REF_DATA / "Al_fde_rho.pp")
+    grid = rho.grid
+    idx = sample_index(rho.size)
+    out = {"rho": np.asarray(rho), "lattice": grid.lattice.copy(), "nr": np.array(grid.nrR),
+           "positions": ions.positions.copy(), "charges": ions.charges.copy(), "sample_idx": idx}
+    funcs = {
+        "TF": Functional(type="KEDF", name="TF"),
+        "VW": Functional(type="KEDF", name="VW"),
+        "WTNL": Functional(type="KEDF", name="WT-NL"),
+        "KEDF_WT": Functional(type="KEDF", name="WT"),
+        "KEDF_TFVW": Functional(type="KEDF", name="TFVW"),
+        "LDA": Functional(type="XC", name="LDA"),
+        "HARTREE": Functional(type="HARTREE"),
+    }
+    t0 = time.time()
+    for name, (e, v) in component_outputs(rho, funcs).items():
+        out["E_" + name] = e
+        out["Vs_" + name] = v.ravel()[idx]
+        out["Vc_" + name] = checksums(v)
+    # LMGP (reference test_functional.py:29-34): first call builds the MGP table
+    for interp in ("linear", "hermite"):
+        f = Functional(type="KEDF", name="LMGP", interp=interp)
+        o = f(rho, calcType={"E", "V"})
+        out["E_LMGP_" + interp] = float(o.energy)
+        out["Vs_LMGP_" + interp] = np.asarray(o.potential).ravel()[idx]
+        out["Vc_LMGP_" + interp] = checksums(o.potential)
+    # analytic local PP on these ions (PME and exact structure factor)
+    al = {"Al": AnalyticPP(*systems.SPECIES["Al"])}
+    for pme in (True, False):
+        tag = "PME" if pme else "EXACT"
+        ps = LocalPseudo(grid=grid, ions=ions, PP_list=al, PME=pme)
+        o = ps(rho)
+        out["E_PP_" + tag] = float(o.energy)
+        out["Vs_PP_" + tag] = np.asarray(o.potential).ravel()[idx]
+        out["Vc_PP_" + tag] = checksums(o.potential)
+        out["F_PP_" + tag] = ps.forces(rho)
+    # Ewald (reference test_ewald.py:33-54 values are re-asserted by the tests)
+    ew = ewald(rho=rho, ions=ions, verbose=False)
+    ewp = ewald(rho=rho, ions=ions, verbose=False, PME=True)
+    out["EW_corr"] = ew.Energy_corr()
+    out["EW_real"] = ew.Energy_real()
+    out["EW_rec"] = ew.Energy_rec()
+    out["EW_real_pme"] = ewp.Energy_real_fast2()
+    out["EW_rec_pme"] = ewp.Energy_rec_PME()
+    out["EW_energy"] = ew.energy
+    out["EW_energy_pme"] = ewp.energy
+    out["EW_forces"] = ew.forces
+    out["EW_forces_pme"] = ewp.forces
+    out["EW_eta"] = ew.eta
+    # FFT convention: rho.fft() (x dV), sampled on the half spectrum
+    rg = np.asarray(rho.fft())
+    gidx = sample_index(rg.size, seed=7)
+    out["FFT_idx"] = gidx
+    out["FFT_s"] = rg.ravel()[gidx]
+    print("fde: %.1f s" % (time.time() - t0))
+    np.savez_compressed(HERE / "fde.npz", **out)
+
+
+def build_total(st, kedf, pme=True, **kedf_kw):
+    grid = DirectGrid(lattice=st.lattice.copy(), nr=st.nr, full=False)
+    ions = ref_ions(st)
+    pseudo = LocalPseudo(grid=grid, ions=ions, PP_list=pp_list(st.symbols), PME=pme)
+    funcs = dict(KineticEnergyFunctional=Functional(type="KEDF", name=kedf, **kedf_kw),
+                 XCFunctional=Functional(type="XC", name="LDA"),
+                 HARTREE=Functional(type="HARTREE"), PSEUDO=pseudo)
+    return grid, ions, pseudo, TotalFunctional(**funcs), funcs
+
+
+def run_tn(st, kedf, econv, full_rho=True, **kedf_kw):
+    grid, ions, pseudo, total, funcs = build_total(st, kedf, **kedf_kw)
+    rho0 = DirectField(grid=grid)
+    rho0[:] = ions.get_ncharges() / ions.cell.volume
+    t0 = time.time()
+    pseudo.local_PP()
+    e_ii = total.ewald.energy
+    t_setup = time.time() - t0
+    ev = CountingEvaluator(total)
+    opt = Optimization(EnergyEvaluator=ev, optimization_method="TN",
+                       optimization_options={"econv": econv, "maxfun": 50, "maxiter": 100})
+    TimeData.reset()
+    t0 = time.time()
+    rho = opt.optimize_rho(guess_rho=rho0)
+    t_opt = time.time() - t0
+    n_fft = TimeData.number.get("FFT", 0)
+    n_ifft = TimeData.number.get("InvFFT", 0)
+    e_final = float(total.Energy(rho))
+    out = {"lattice": st.lattice, "positions": st.positions, "nr": np.array(st.nr),
+           "symbols": np.array(st.symbols), "econv": econv, "E_final": e_final,
+           "E_history": np.array(ev.energies), "n_ev": ev.n_ev, "n_v": ev.n_v,
+           "converged": opt.converged, "n_fft": n_fft, "n_ifft": n_ifft,
+           "t_opt": t_opt, "t_setup": t_setup, "E_ewald": float(e_ii),
+           "mu": float(opt.mu)}
+    idx = sample_index(rho.size)
+    out["sample_idx"] = idx
+    out["rho_s"] = np.asarray(rho).ravel()[idx]
+    out["rho_c"] = checksums(rho)
+    if full_rho:
+        out["rho"] = np.asarray(rho)
+    comps = {"KEDF": funcs["KineticEnergyFunctional"], "XC": funcs["XCFunctional"],
+             "HARTREE": funcs["HARTREE"], "PSEUDO": funcs["PSEUDO"]}
+    for name, (e, v) in component_outputs(rho, comps).items():
+        out["E_" + name] = e
+        out["Vs_" + name] = v.ravel()[idx]
+        out["Vc_" + name] = checksums(v)
+    out["vloc_s"] = np.asarray(pseudo.vreal).ravel()[idx]
+    out["vloc_c"] = checksums(pseudo.vreal)
+    out["forces"] = total.get_forces(rho, ions=ions)
+    out["forces_pp"] = pseudo.forces(rho)
+    out["forces_ii"] = total.ewald.forces
+    # one evaluation at the uniform start density, for per-evaluation checks
+    o = total(rho0, calcType={"E", "V"})
+    out["E_uniform"] = float(o.energy)
+    out["V_uniform_s"] = np.asarray(o.potential).ravel()[idx]
+    print("%s: E=%.10f  evals E+V %d, V %d, FFT %d+%d, %.1f s" % (
+        st.name, e_final, ev.n_ev, ev.n_v, n_fft, n_ifft, t_opt))
+    return out
+
+
+def gen_al4():
+    st = systems.config_al4(seed=0)
+    out = run_tn(st, "TFVW", econv=1e-7)
+    np.savez_compressed(HERE / "al4.npz", **out)
+
+
+def gen_al256():
+    st = systems.config_al256(seed=0)
+    out = run_tn(st, "WT", econv=1e-7, full_rho=False)
+    np.savez_compressed(HERE / "al256.npz", **out)
+
+
+def gen_dcsrch():
+    """Trial-step sequences of the reference line search on 1-D test functions."""
+    cases = {
+        # (phi(a), phi'(a)) pairs, a in [0, pi]
+        "quad": lambda a: ((a - 0.7) ** 2, 2.0 * (a - 0.7)),
+        "cos": lambda a: (-np.cos(a - 0.3) + 0.01 * a ** 4, np.sin(a - 0.3) + 0.04 * a ** 3),
+        "steep": lambda a: (np.exp(-3.0 * a) + 3.0 * a * a, -3.0 * np.exp(-3.0 * a) + 6.0 * a),
+        "flat": lambda a: (-a / (1.0 + 40.0 * a * a), -(1.0 - 40.0 * a * a) / (1.0 + 40.0 * a * a) ** 2),
+        "mt1": lambda a: (-a / (a * a + 2.0), (a * a - 2.0) / (a * a + 2.0) ** 2),
+    }
+    out = {}
+    for name, fn in cases.items():
+        for a0 in (0.1, 1e-3, 1.5):
+            trials = []
+
+            def f(a, fn=fn, trials=trials):
+                trials.append(float(a))
+                v, g = fn(a)
+                return [float(v), float(g)]
+            f0 = fn(0.0)
+            theta, _, _, task, nls, _ = LineSearchDcsrch2(
+                f, alpha0=a0, func0=[float(f0[0]), float(f0[1])], c1=1e-4, c2=0.2,
+                amax=np.pi, amin=0.0, xtol=1e-12, maxiter=30)
+            key = "%s_%g" % (name, a0)
+            out[key + "_trials"] = np.array(trials)
+            out[key + "_theta"] = np.nan if theta is None else float(theta)
+            out[key + "_task"] = task.decode() if isinstance(task, bytes) else str(task)
+    np.savez_compressed(HERE / "dcsrch.npz", **out)
+    print("dcsrch: %d cases" % len(cases))
+
+
+GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch}
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(GENERATORS)
+    for n in names:
+        GENERATORS[n]()

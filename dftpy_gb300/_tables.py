@@ -1,0 +1,101 @@
+"""Small 1-D set-up tables built on the host (sizes ~1e4 at most).
+
+Grid-sized work never happens here; these are the per-species / per-axis
+tables the device kernels interpolate from.
+"""
+import numpy as np
+
+
+def spline_notaknot(x, y):
+    """Cubic spline through (x, y) with not-a-knot ends.
+
+    ``scipy.interpolate.splrep(x, y, k=3, s=0)`` (FITPACK) builds exactly this
+    interpolant (interior knots at x[2..m-3]); here it is computed directly:
+    second derivatives from a tridiagonal system (the two not-a-knot rows
+    reduced with their neighbours), solved by the Thomas algorithm.
+    Returns (x, c) with c[i] = (a, b, c, d) of a + b u + c u^2 + d u^3 on
+    [x[i], x[i+1]], u = t - x[i].
+    """
+    x = np.asarray(x, float)
+    y = np.asarray(y, float)
+    n = x.size
+    if n < 4:
+        raise ValueError("spline needs >= 4 points")
+    h = np.diff(x)
+    delta = np.diff(y) / h
+    lo = np.zeros(n)
+    di = np.zeros(n)
+    up = np.zeros(n)
+    r = np.zeros(n)
+    lo[1:n - 1] = h[:-1]
+    di[1:n - 1] = 2.0 * (h[:-1] + h[1:])
+    up[1:n - 1] = h[1:]
+    r[1:n - 1] = 6.0 * (delta[1:] - delta[:-1])
+    f = h[0] / h[1]
+    di[0] = h[1] - f * h[0]
+    up[0] = -(h[0] + h[1]) - f * 2.0 * (h[0] + h[1])
+    r[0] = -f * r[1]
+    f = h[n - 2] / h[n - 3]
+    di[n - 1] = h[n - 3] - f * h[n - 2]
+    lo[n - 1] = -(h[n - 3] + h[n - 2]) - f * 2.0 * (h[n - 3] + h[n - 2])
+    r[n - 1] = -f * r[n - 2]
+    # Thomas algorithm
+    cp = np.zeros(n)
+    dp = np.zeros(n)
+    cp[0] = up[0] / di[0]
+    dp[0] = r[0] / di[0]
+    for i in range(1, n):
+        m = di[i] - lo[i] * cp[i - 1]
+        cp[i] = up[i] / m if i < n - 1 else 0.0
+        dp[i] = (r[i] - lo[i] * dp[i - 1]) / m
+    M = np.zeros(n)
+    M[-1] = dp[-1]
+    for i in range(n - 2, -1, -1):
+        M[i] = dp[i] - cp[i] * M[i + 1]
+    a = y[:-1]
+    b = delta - h * (2.0 * M[:-1] + M[1:]) / 6.0
+    c = M[:-1] / 2.0
+    d = (M[1:] - M[:-1]) / (6.0 * h)
+    return x, np.ascontiguousarray(np.stack([a, b, c, d], axis=1))
+
+
+def quartic_coefficients(vp):
+    """Coefficients of ``quartic_interpolation`` through (v2, v1, v0, v1, v2)
+    (``math_utils.py:457-467``): value = q4[0] + dx (q4[1] + dx (...)) / 24."""
+    f = [vp[2], vp[1], vp[0], vp[1], vp[2]]
+    t0 = f[2]
+    t1 = 2.0 * f[0] - 16.0 * f[1] + 16.0 * f[3] - 2.0 * f[4]
+    t2 = -f[0] + 16.0 * f[1] - 30.0 * f[2] + 16.0 * f[3] - f[4]
+    t3 = -2.0 * f[0] + 4.0 * f[1] - 4.0 * f[3] + 2.0 * f[4]
+    t4 = f[0] - 4.0 * f[1] + 6.0 * f[2] - 4.0 * f[3] + f[4]
+    return [t0, t1, t2, t3, t4]
+
+
+def bspline_mn(x, order, size=None):
+    """Cardinal B-spline values M_n(x + k), k = 0..order-1, at index 1..order
+    (recursion of ``CBspline.calc_Mn``, ``ewald.py:63-80``)."""
+    Mn = np.zeros((order if size is None else size) + 1)
+    Mn[1] = x
+    Mn[2] = 1.0 - x
+    for i in range(3, order + 1):
+        for j in range(0, i):
+            n = i - j
+            Mn[n] = ((x + n - 1) * Mn[n] + (j + 1 - x) * Mn[n - 1]) / (i - 1)
+    return Mn
+
+
+def pme_bm(nr, order=10):
+    """PME b(m) factors of the three axes concatenated: axis 0 (n0), axis 1
+    (n1), axis 2 (n2//2+1) (``CBspline._calc_bm``, ``ewald.py:82-98``)."""
+    Mn = bspline_mn(1.0, order)
+    out = []
+    lens = (nr[0], nr[1], nr[2] // 2 + 1)
+    for i in range(3):
+        m = np.arange(lens[i])
+        q = 2.0 * np.pi * m / nr[i]
+        num = np.exp(-1j * (order - 1.0) * q)
+        den = np.zeros_like(num)
+        for k in range(1, order):
+            den += Mn[k] * np.exp(-1j * k * q)
+        out.append(num / den)
+    return np.concatenate(out).astype(np.complex128)

@@ -1,0 +1,248 @@
+// C ABI entry points: plans, FFTs, the fused functional evaluation.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "plan.h"
+
+static thread_local char g_err[1024] = "";
+
+int gb_set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+size_t gb_elem(const gbofdft_plan* p) { return p->prec == GBOFDFT_F64 ? 8 : 4; }
+
+static void factorize(int n, AxisPlan& ax) {
+  ax.n = n;
+  ax.nst = 0;
+  int m = n;
+  const int pref[] = {8, 4, 2, 3, 5};
+  for (int r : pref)
+    while (m % r == 0 && ax.nst < GB_MAX_STAGES) { ax.radix[ax.nst++] = r; m /= r; }
+  for (int pr = 7; m > 1 && ax.nst < GB_MAX_STAGES; pr += 2)
+    while (m % pr == 0) { ax.radix[ax.nst++] = pr; m /= pr; }
+}
+
+static void det_inv(const double* L, double* inv, double* det) {
+  const double a = L[0], b = L[1], c = L[2], d = L[3], e = L[4], f = L[5], g = L[6], h = L[7], i = L[8];
+  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  *det = a * A + b * B + c * C;
+  const double id = 1.0 / *det;
+  inv[0] = A * id; inv[1] = -(b * i - c * h) * id; inv[2] = (b * f - c * e) * id;
+  inv[3] = B * id; inv[4] = (a * i - c * g) * id;  inv[5] = -(a * f - c * d) * id;
+  inv[6] = C * id; inv[7] = -(a * h - b * g) * id; inv[8] = (a * e - b * d) * id;
+}
+
+extern "C" {
+
+int gbofdft_version(void) { return GBOFDFT_ABI_VERSION; }
+
+int gbofdft_last_error(char* buf, size_t len) {
+  size_t n = strlen(g_err);
+  if (buf && len) {
+    size_t m = n < len - 1 ? n : len - 1;
+    memcpy(buf, g_err, m);
+    buf[m] = 0;
+  }
+  return (int)n;
+}
+
+int gbofdft_plan_destroy(gbofdft_plan* p) {
+  if (!p) return GBOFDFT_OK;
+  for (int a = 0; a < 3; ++a)
+    if (p->tw[a]) cudaFree(p->tw[a]);
+  if (p->spec) cudaFree(p->spec);
+  if (p->partials) cudaFree(p->partials);
+  if (p->scratch) cudaFree(p->scratch);
+  delete p;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision, int full, gbofdft_plan** out) {
+  GB_REQUIRE(nr && lattice && out, "plan_create: null argument");
+  GB_REQUIRE(precision == GBOFDFT_F32 || precision == GBOFDFT_F64, "plan_create: bad precision %d", precision);
+  for (int a = 0; a < 3; ++a)
+    GB_REQUIRE(nr[a] >= 1 && nr[a] <= GB_MAX_N, "plan_create: nr[%d]=%d outside [1, %d]", a, nr[a], GB_MAX_N);
+  *out = nullptr;
+  gbofdft_plan* p = new (std::nothrow) gbofdft_plan;
+  if (!p) return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: host allocation failed");
+  memset(p, 0, sizeof(*p));
+  for (int a = 0; a < 3; ++a) p->n[a] = nr[a];
+  p->n2h = nr[2] / 2 + 1;
+  p->ld2 = p->n2h;
+  p->full = full ? 1 : 0;
+  p->prec = precision;
+  cudaGetDevice(&p->device);
+  memcpy(p->lattice, lattice, sizeof(double) * 9);
+  double inv[9], det;
+  det_inv(lattice, inv, &det);
+  if (!(fabs(det) > 0.0)) {
+    delete p;
+    return gb_set_error(GBOFDFT_ERR_ARG, "plan_create: singular lattice");
+  }
+  const double twopi = 6.283185307179586476925286766559;
+  // bg = 2 pi inv(L)^T, rows are reciprocal vectors
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) p->bg[r * 3 + c] = twopi * inv[c * 3 + r];
+  p->volume = fabs(det);
+  p->N = (int64_t)nr[0] * nr[1] * nr[2];
+  p->NG = (int64_t)nr[0] * nr[1] * p->n2h;
+  p->NGld = (int64_t)nr[0] * nr[1] * p->ld2;
+  p->dV = p->volume / (double)p->N;
+  const size_t cs = 2 * gb_elem(p);
+  for (int a = 0; a < 3; ++a) {
+    factorize(nr[a], p->ax[a]);
+    std::vector<double> t(2 * (size_t)nr[a]);
+    for (int m = 0; m < nr[a]; ++m) {
+      // exp(-2 pi i m / n); reduce by symmetry to keep the angle small
+      const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)nr[a];
+      t[2 * m] = (double)cosl(ang);
+      t[2 * m + 1] = (double)sinl(ang);
+    }
+    cudaError_t e = cudaMalloc(&p->tw[a], cs * nr[a]);
+    if (e != cudaSuccess) { gbofdft_plan_destroy(p); return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: %s", cudaGetErrorString(e)); }
+    if (precision == GBOFDFT_F64) {
+      e = cudaMemcpy(p->tw[a], t.data(), cs * nr[a], cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> tf(t.begin(), t.end());
+      e = cudaMemcpy(p->tw[a], tf.data(), cs * nr[a], cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) { gbofdft_plan_destroy(p); return gb_set_error(GBOFDFT_ERR_CUDA, "plan_create: %s", cudaGetErrorString(e)); }
+  }
+  // column tile: keep (n + 2 n tb) complex elements within ~96 KB
+  for (int a = 0; a < 3; ++a) {
+    const int n = nr[a];
+    int tb = (int)((96 * 1024 / cs - n) / (2 * (size_t)n));
+    if (tb > 16) tb = 16;
+    if (tb < 1) tb = 1;
+    p->tb[a] = tb;
+  }
+  p->pairs = 2;
+  const size_t rows_sm = cs * ((size_t)nr[2] + 2 * (size_t)GB_MAX_FIELDS * p->pairs * nr[2]);
+  if (rows_sm > 200 * 1024 || cs * ((size_t)nr[0] * (1 + 2 * p->tb[0])) > 220 * 1024 ||
+      cs * ((size_t)nr[1] * (1 + 2 * p->tb[1])) > 220 * 1024) {
+    gbofdft_plan_destroy(p);
+    return gb_set_error(GBOFDFT_ERR_UNSUPPORTED, "plan_create: grid %dx%dx%d too large for the line passes",
+                        nr[0], nr[1], nr[2]);
+  }
+  cudaError_t e = cudaMalloc(&p->spec, cs * (size_t)GB_MAX_FIELDS * p->NGld);
+  const int64_t nrows = (int64_t)nr[0] * nr[1];
+  p->max_partials = (nrows + 2 * p->pairs - 1) / (2 * p->pairs) + 1;
+  if (e == cudaSuccess) e = cudaMalloc(&p->partials, sizeof(double) * GB_NE * p->max_partials);
+  if (e == cudaSuccess) e = cudaMalloc(&p->scratch, sizeof(double) * 4096);
+  if (e != cudaSuccess) {
+    gbofdft_plan_destroy(p);
+    return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: workspace: %s", cudaGetErrorString(e));
+  }
+  memcpy(p->gi.bg, p->bg, sizeof(p->bg));
+  p->gi.n0 = nr[0]; p->gi.n1 = nr[1]; p->gi.n2 = nr[2]; p->gi.n2h = p->n2h; p->gi.ld2 = p->ld2;
+  p->gi.full = p->full;
+  *out = p;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_plan_sizes(const gbofdft_plan* p, int64_t out[4]) {
+  GB_REQUIRE(p && out, "plan_sizes: null argument");
+  out[0] = p->N;
+  out[1] = p->NG;
+  out[2] = p->n2h;
+  out[3] = (int64_t)(2 * gb_elem(p) * (GB_MAX_FIELDS * p->NGld + p->n[0] + p->n[1] + p->n[2])) +
+           (int64_t)sizeof(double) * (GB_NE * p->max_partials + 4096);
+  return GBOFDFT_OK;
+}
+
+int gbofdft_fft_r2c(gbofdft_plan* p, const void* in, void* out, void* stream) {
+  GB_REQUIRE(p && in && out, "fft_r2c: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int op = OP_RHO;
+  int rc = gb_rows_fwd(p, in, out, 0, p->n2h, 1, &op, 1.0, p->dV, st);
+  if (!rc) rc = gb_cols(p, out, 0, p->n2h, 1, 1, -1, 1.0, st);
+  if (!rc) rc = gb_cols(p, out, 0, p->n2h, 1, 0, -1, 1.0, st);
+  return rc;
+}
+
+int gbofdft_fft_c2r(gbofdft_plan* p, const void* in, void* out, void* stream) {
+  GB_REQUIRE(p && in && out, "fft_c2r: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cs = 2 * gb_elem(p);
+  GB_CUDA(cudaMemcpy2DAsync(p->spec, cs * p->ld2, in, cs * p->n2h, cs * p->n2h, (size_t)p->n[0] * p->n[1],
+                            cudaMemcpyDeviceToDevice, st));
+  int rc = gb_cols(p, p->spec, 0, p->ld2, 1, 0, 1, 1.0, st);
+  if (!rc) rc = gb_cols(p, p->spec, 0, p->ld2, 1, 1, 1, 1.0, st);
+  if (!rc) rc = gb_rows_inv_store(p, p->spec, 0, p->ld2, 1, out, 0, 1.0 / ((double)p->N * p->dV), st);
+  return rc;
+}
+
+int gbofdft_convolve(gbofdft_plan* p, const void* in, void* out, int kernel, const void* karr, double coef,
+                     void* stream) {
+  GB_REQUIRE(p && in && out, "convolve: null argument");
+  GB_REQUIRE(kernel >= GBOFDFT_KER_NONE && kernel <= GBOFDFT_KER_ARRAY, "convolve: bad kernel %d", kernel);
+  GB_REQUIRE(kernel != GBOFDFT_KER_ARRAY || karr, "convolve: kernel array missing");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int op = OP_RHO;
+  KerDesc kd;
+  memset(&kd, 0, sizeof(kd));
+  kd.type[0] = kernel;
+  kd.arr[0] = karr;
+  kd.coef[0] = coef;
+  int rc = gb_rows_fwd(p, in, p->spec, 0, p->ld2, 1, &op, 1.0, 1.0, st);
+  if (!rc) rc = gb_cols(p, p->spec, 0, p->ld2, 1, 1, -1, 1.0, st);
+  if (!rc) rc = gb_cols_conv(p, p->spec, 0, p->ld2, 1, kd, 1.0 / (double)p->N, st);
+  if (!rc) rc = gb_cols(p, p->spec, 0, p->ld2, 1, 1, 1, 1.0, st);
+  if (!rc) rc = gb_rows_inv_store(p, p->spec, 0, p->ld2, 1, out, 0, 1.0, st);
+  return rc;
+}
+
+int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
+                 int calc, void* stream) {
+  GB_REQUIRE(p && rho && f && pot, "eval: null argument");
+  GB_REQUIRE(!(calc & GBOFDFT_CALC_E) || energies, "eval: energies buffer required with CALC_E");
+  GB_REQUIRE(!f->wt || f->wt_kernel, "eval: WT enabled without a kernel table");
+  GB_REQUIRE(!f->wt || fabs(f->wt_alpha - f->wt_beta) < 1e-9,
+             "eval: fused WT path requires alpha == beta (got %g, %g)", f->wt_alpha, f->wt_beta);
+  GB_REQUIRE(f->xc == 0 || f->xc == 1, "eval: unsupported xc %d", f->xc);
+  cudaStream_t st = (cudaStream_t)stream;
+  EvalDesc ev;
+  memset(&ev, 0, sizeof(ev));
+  KerDesc kd;
+  memset(&kd, 0, sizeof(kd));
+  int ops[GB_MAX_FIELDS];
+  int nf = 0;
+  ev.tf = f->tf; ev.tf_x = f->tf_x;
+  ev.vw = f->vw; ev.vw_y = f->vw_y;
+  ev.wt = f->wt; ev.wt_alpha = f->wt_alpha; ev.wt_beta = f->wt_beta;
+  ev.xc = f->xc; ev.hartree = f->hartree; ev.pp = f->vloc != nullptr; ev.e_ion = f->e_ion;
+  if (f->hartree) { ev.slot_h = nf; ops[nf] = OP_RHO; kd.type[nf] = KER_HARTREE; kd.coef[nf] = 1.0; ++nf; }
+  if (f->vw) { ev.slot_vw = nf; ops[nf] = OP_SQRT; kd.type[nf] = KER_G2; kd.coef[nf] = 1.0; ++nf; }
+  if (f->wt) {
+    ev.slot_wt = nf; ops[nf] = OP_POWB; kd.type[nf] = KER_ARRAY; kd.arr[nf] = f->wt_kernel; kd.coef[nf] = 1.0;
+    ++nf;
+  }
+  const int64_t fs = p->NGld;
+  int rc = 0;
+  if (nf > 0) {
+    rc = gb_rows_fwd(p, rho, p->spec, fs, p->ld2, nf, ops, f->wt_beta, 1.0, st);
+    if (!rc) rc = gb_cols(p, p->spec, fs, p->ld2, nf, 1, -1, 1.0, st);
+    if (!rc) rc = gb_cols_conv(p, p->spec, fs, p->ld2, nf, kd, 1.0 / (double)p->N, st);
+    if (!rc) rc = gb_cols(p, p->spec, fs, p->ld2, nf, 1, 1, 1.0, st);
+  }
+  if (!rc)
+    rc = gb_rows_inv_eval(p, p->spec, fs, nf, ev, rho, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
+  return rc;
+}
+
+int gbofdft_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out, void* stream) {
+  GB_REQUIRE(p && out, "wt_kernel: null argument");
+  return gb_build_wt_kernel(p, rho0, x, alpha, beta, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

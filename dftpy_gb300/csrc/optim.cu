@@ -1,0 +1,486 @@
+// Truncated-Newton direct density optimisation on the device.
+//
+// Host control flow mirrors dftpy's Optimization.optimize_rho with method
+// "TN" (src/dftpy/optimization/optimization.py:91-147 get_direction_TN,
+// :204-225 OrthogonalNormalization, :227-279 ValueAndDerivative,
+// :281-520 optimize_rho, :522-535 check_converge) and the More-Thuente line
+// search of LineSearchDcsrch2 (math_utils.py:76-106).  Every field-sized
+// operation is a fused elementwise kernel whose dot products finish in the
+// same launch (the last CTA to arrive sums the per-CTA partials in a fixed
+// order with compensated FP64 arithmetic), so results are deterministic.
+// Scalars cross to the host once per evaluation (one small D2H copy).
+#include <math.h>
+#include <string.h>
+
+#include "dcsrch.h"
+#include "plan.h"
+
+namespace {
+
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
+constexpr int kRedThreads = 256;
+constexpr int kMaxVals = 4;
+
+// scalar slots in the workspace scalar array
+enum {
+  S_A = 0, S_B = 1, S_C = 2, S_D = 3,   // generic reduction outputs
+  S_PAP = 4, S_R1 = 8,                  // TN inner loop
+  S_EN = 16,                            // energies (GB_NE)
+  S_COUNT = 64
+};
+
+struct Ws {
+  void* f[14];
+  double* partials;  // kRedBlocks * kMaxVals
+  double* sc;        // S_COUNT
+  unsigned* counter;
+};
+
+enum { F_PHI = 0, F_RHO, F_POT, F_RES0, F_P, F_CGR, F_CGP, F_AP, F_DIR, F_BEST, F_PHI1, F_POT1, F_TMP, F_NF };
+
+template <int NV>
+__device__ __forceinline__ void reduce_finalize(KSum (&acc)[NV], double* partials, double* out, unsigned* counter) {
+  __shared__ double red[kRedThreads / 32][NV];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double v = warp_sum(acc[k].value());
+    if (lane == 0) red[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < kRedThreads / 32; ++w) s += red[w][k];
+      partials[blockIdx.x * NV + k] = s;
+    }
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    KSum s;
+    s.init();
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s.add(__ldcg(partials + b * NV + k));
+    double v = warp_sum(s.value());
+    if (lane == 0) red[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      KSum s;
+      s.init();
+      for (int w = 0; w < kRedThreads / 32; ++w) s.add(red[w][k]);
+      out[k] = s.value();
+    }
+    *counter = 0u;
+  }
+}
+
+// f(i, double* contributions[NV]) for i in [0, n)
+template <int NV, typename F>
+__global__ void __launch_bounds__(kRedThreads) k_map_reduce(int64_t n, F f, double* partials, double* out,
+                                                           unsigned* counter) {
+  KSum acc[NV > 0 ? NV : 1];
+#pragma unroll
+  for (int k = 0; k < (NV > 0 ? NV : 1); ++k) acc[k].init();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double c[NV > 0 ? NV : 1];
+    f(i, c);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k].add(c[k]);
+  }
+  if constexpr (NV > 0) reduce_finalize<NV>(acc, partials, out, counter);
+}
+
+template <int NV, typename F>
+int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st) {
+  int nb = (int)((n + kRedThreads * 4 - 1) / (kRedThreads * 4));
+  if (nb > kRedBlocks) nb = kRedBlocks;
+  if (nb < 1) nb = 1;
+  k_map_reduce<NV><<<nb, kRedThreads, 0, st>>>(n, f, w.partials, w.sc + slot, w.counter);
+  GB_CHECK_LAUNCH();
+  return 0;
+}
+
+}  // namespace
+
+struct TnState {
+  gbofdft_plan* p;
+  const gbofdft_functional* fn;
+  Ws w;
+  cudaStream_t st;
+  double host[S_COUNT];
+  int n_ev, n_v;
+};
+
+static int ts_sync(TnState& s) {
+  GB_CUDA(cudaMemcpyAsync(s.host, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
+  GB_CUDA(cudaStreamSynchronize(s.st));
+  return 0;
+}
+
+static int ts_eval(TnState& s, const void* rho, void* pot, bool want_e) {
+  if (want_e) ++s.n_ev; else ++s.n_v;
+  return gbofdft_eval(s.p, rho, s.fn, pot, want_e ? s.w.sc + S_EN : nullptr,
+                      GBOFDFT_CALC_V | (want_e ? GBOFDFT_CALC_E : 0), s.st);
+}
+
+template <typename T>
+static T* F(TnState& s, int i) { return reinterpret_cast<T*>(s.w.f[i]); }
+
+template <typename T>
+static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft_tn_result* res) {
+  const int64_t N = s.p->N;
+  const double dV = s.p->dV;
+  cudaStream_t st = s.st;
+  const Ws& w = s.w;
+  int rc;
+  T* rio = reinterpret_cast<T*>(rho_io);
+  // ---- initial phi (optimization.py:305-316) --------------------------------
+  {
+    T* phi = F<T>(s, F_PHI);
+    rc = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+      const T r = rio[i];
+      const T ph = r > (T)0 ? sqrt(r) : (sizeof(T) == 8 ? (T)1e-300 : (T)1e-30);
+      phi[i] = ph;
+      c[0] = (double)r;
+      c[1] = (double)ph * (double)ph;
+    }, S_A, st);
+    if (rc) return rc;
+    if ((rc = ts_sync(s))) return rc;
+    const T fac = (T)sqrt(s.host[S_A] / s.host[S_B]);
+    T* rho = F<T>(s, F_RHO);
+    rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+      const T ph = phi[i] * fac;
+      phi[i] = ph;
+      rho[i] = ph * ph;
+    }, S_A, st);
+    if (rc) return rc;
+  }
+  if ((rc = ts_eval(s, F<T>(s, F_RHO), F<T>(s, F_POT), true))) return rc;
+  // mu and residual
+  auto mu_residual = [&](double& mu, double& energy, double& resN) -> int {
+    T* phi = F<T>(s, F_PHI);
+    T* pot = F<T>(s, F_POT);
+    T* rho = F<T>(s, F_RHO);
+    int r = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+      const T ph = phi[i];
+      const T rr = ph * ph;
+      rho[i] = rr;
+      c[0] = (double)pot[i] * (double)rr;
+      c[1] = (double)rr;
+    }, S_A, st);
+    if (r) return r;
+    if ((r = ts_sync(s))) return r;
+    energy = s.host[S_EN + GB_E_TOTAL];
+    mu = (s.host[S_A] * dV) / (s.host[S_B] * dV);
+    const T muT = (T)mu;
+    T* res0 = F<T>(s, F_RES0);
+    r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+      const T v = (pot[i] - muT) * phi[i];
+      res0[i] = v;
+      c[0] = (double)v * (double)v;
+    }, S_C, st);
+    resN = 0.0;
+    return r;
+  };
+  double mu, energy, resN;
+  if ((rc = mu_residual(mu, energy, resN))) return rc;
+  const int hist_cap = res->history_cap;
+  int nh = 0;
+  double ehist_last[64];
+  int nhist = 0;
+  auto push_hist = [&](double e) {
+    if (res->history && nh < hist_cap) res->history[nh++] = e;
+    if (nhist < 64) ehist_last[nhist++] = e;
+    else { memmove(ehist_last, ehist_last + 1, sizeof(double) * 63); ehist_last[63] = e; }
+  };
+  push_hist(energy);
+  double theta = 0.1;
+  int converged = 1;
+  int it;
+  // eps > 0: fixed step (the reference's 1e-9); eps < 0: |eps| relative to
+  // ||phi|| / ||residual|| of each TN direction (single precision needs a step
+  // the perturbation phi + eps p can resolve); eps == 0: 1e-9
+  const double eps_fixed = o.eps > 0 ? o.eps : 1e-9;
+  const double eps_rel = o.eps < 0 ? -o.eps : 0.0;
+  for (it = 1; it < o.maxiter; ++it) {
+    // ---- TN direction (optimization.py:91-147) -----------------------------
+    {
+      T* res0 = F<T>(s, F_RES0);
+      T* cgr = F<T>(s, F_CGR);
+      T* cgp = F<T>(s, F_CGP);
+      T* dir = F<T>(s, F_DIR);
+      T* phic = F<T>(s, F_PHI);
+      rc = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+        const T r = -res0[i];
+        cgr[i] = r;
+        cgp[i] = r;
+        dir[i] = (T)0;
+        c[0] = (double)r * (double)r;
+        c[1] = (double)phic[i] * (double)phic[i];
+      }, S_A, st);
+      if (rc) return rc;
+      if ((rc = ts_sync(s))) return rc;
+      double r0Norm = s.host[S_A];
+      const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
+      const double rConv = r0Norm * 0.1;
+      double rmin = 1e10;          // min(rLists) with rLists = [1e10]
+      double prev_min = 1e10;
+      bool use_best = false;
+      bool have_best = false;      // Best starts as the zero direction
+      int j;
+      double beta = 0.0;
+      for (j = 0; j < o.maxfun; ++j) {
+        T* phi = F<T>(s, F_PHI);
+        T* phi1 = F<T>(s, F_PHI1);
+        T* rho1 = F<T>(s, F_TMP);
+        const T eT = (T)epsi, bT = (T)beta;
+        const bool first = (j == 0);
+        rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+          T pv = cgp[i];
+          if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
+          const T p1 = phi[i] + eT * pv;
+          phi1[i] = p1;
+          rho1[i] = p1 * p1;
+        }, S_A, st);
+        if (rc) return rc;
+        T* pot1 = F<T>(s, F_POT1);
+        if ((rc = ts_eval(s, rho1, pot1, false))) return rc;
+        T* ap = F<T>(s, F_AP);
+        const T muT = (T)mu;
+        const T inv_e = (T)(1.0 / epsi);
+        rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+          const T a = ((pot1[i] - muT) * phi1[i] - res0[i]) * inv_e;
+          ap[i] = a;
+          c[0] = (double)cgp[i] * (double)a;
+        }, S_PAP, st);
+        if (rc) return rc;
+        const double* scd = w.sc;
+        const double r0c = r0Norm;
+        rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+          const double pap = scd[S_PAP];
+          if (pap < 0.0) { c[0] = 0.0; return; }
+          const T alpha = (T)(r0c / pap);
+          dir[i] += alpha * cgp[i];
+          const T r = cgr[i] - alpha * ap[i];
+          cgr[i] = r;
+          c[0] = (double)r * (double)r;
+        }, S_R1, st);
+        if (rc) return rc;
+        if ((rc = ts_sync(s))) return rc;
+        const double pAp = s.host[S_PAP];
+        if (pAp < 0.0) {
+          if (j == 0) {
+            // direction = r0Norm / pAp * p
+            const T sc = (T)(r0Norm / pAp);
+            rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { dir[i] = sc * cgp[i]; }, S_A, st);
+            if (rc) return rc;
+          }
+          break;
+        }
+        const double r1Norm = s.host[S_R1];
+        if (r1Norm < rmin) {
+          GB_CUDA(cudaMemcpyAsync(F<T>(s, F_BEST), dir, sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
+          have_best = true;
+        }
+        prev_min = rmin;
+        if (r1Norm < rmin) rmin = r1Norm;
+        if (r1Norm < rConv) break;
+        if (r1Norm > 1000.0 * prev_min) { use_best = true; break; }
+        if (j > 10 && fabs(r0Norm - r1Norm) < 0.1 * r0Norm) { use_best = true; break; }
+        beta = r1Norm / r0Norm;
+        r0Norm = r1Norm;
+      }
+      // Best aliases the direction itself until the first improvement copies it
+      if (use_best && have_best)
+        GB_CUDA(cudaMemcpyAsync(dir, F<T>(s, F_BEST), sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
+      GB_CUDA(cudaMemcpyAsync(F<T>(s, F_P), dir, sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
+    }
+    // ---- OrthogonalNormalization (optimization.py:204-225) -----------------
+    double theta0 = 0.0, d0 = 0.0;
+    auto orthonormalize = [&]() -> int {
+      T* phi = F<T>(s, F_PHI);
+      T* p = F<T>(s, F_P);
+      T* pot = F<T>(s, F_POT);
+      int r = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+        c[0] = (double)phi[i] * (double)phi[i];
+        c[1] = (double)p[i] * (double)phi[i];
+      }, S_A, st);
+      if (r) return r;
+      if ((r = ts_sync(s))) return r;
+      const double Ne = s.host[S_A] * dV;
+      const T fac = (T)(s.host[S_B] * dV / Ne);
+      r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+        const T v = p[i] - fac * phi[i];
+        p[i] = v;
+        c[0] = (double)v * (double)v;
+      }, S_C, st);
+      if (r) return r;
+      if ((r = ts_sync(s))) return r;
+      const double pNorm = s.host[S_C] * dV;
+      theta0 = sqrt(pNorm / Ne);
+      const T sc = (T)sqrt(Ne / pNorm);
+      r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+        const T v = p[i] * sc;
+        p[i] = v;
+        c[0] = (double)pot[i] * (double)phi[i] * (double)v;
+      }, S_D, st);
+      if (r) return r;
+      if ((r = ts_sync(s))) return r;
+      d0 = s.host[S_D];
+      return 0;
+    };
+    if ((rc = orthonormalize())) return rc;
+    if (d0 * 2.0 > 0.0) {  // "Change to steepest descent" (optimization.py:371-380)
+      T* p = F<T>(s, F_P);
+      T* res0 = F<T>(s, F_RES0);
+      rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { p[i] = -res0[i]; }, S_A, st);
+      if (rc) return rc;
+      if ((rc = orthonormalize())) return rc;
+    }
+    theta = fmin(theta0, theta);
+    // ---- line search over the rotation angle (ValueAndDerivative) ----------
+    Dcsrch ls;
+    dcs_init(ls, o.c1, o.c2, o.xtol, 0.0, 3.14159265358979323846);
+    int task = DCS_START;
+    double stp = theta, fval = energy, gval = 2.0 * d0 * dV;
+    bool accepted = false;
+    int nls;
+    for (nls = 0; nls < o.maxls; ++nls) {
+      task = dcs_step(ls, stp, fval, gval, task);
+      if (task != DCS_FG) break;
+      T* phi = F<T>(s, F_PHI);
+      T* p = F<T>(s, F_P);
+      T* phi1 = F<T>(s, F_PHI1);
+      T* rho1 = F<T>(s, F_TMP);
+      const T ct = (T)cos(stp), sn = (T)sin(stp);
+      rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+        const T v = phi[i] * ct + p[i] * sn;
+        phi1[i] = v;
+        rho1[i] = v * v;
+      }, S_A, st);
+      if (rc) return rc;
+      T* pot1 = F<T>(s, F_POT1);
+      if ((rc = ts_eval(s, rho1, pot1, true))) return rc;
+      rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+        const T p2 = p[i] * ct - phi[i] * sn;
+        c[0] = (double)pot1[i] * (double)phi1[i] * (double)p2;
+      }, S_A, st);
+      if (rc) return rc;
+      if ((rc = ts_sync(s))) return rc;
+      fval = s.host[S_EN + GB_E_TOTAL];
+      gval = 2.0 * s.host[S_A] * dV;
+      accepted = true;
+    }
+    if (nls >= o.maxls || task == DCS_WARN || task == DCS_ERROR || !accepted) {
+      converged = 1;  // line search failed (optimization.py:440-444)
+      break;
+    }
+    theta = stp;
+    // accept: phi <- newphi, pot <- newpot (swap buffers)
+    void* t0 = s.w.f[F_PHI]; s.w.f[F_PHI] = s.w.f[F_PHI1]; s.w.f[F_PHI1] = t0;
+    void* t1 = s.w.f[F_POT]; s.w.f[F_POT] = s.w.f[F_POT1]; s.w.f[F_POT1] = t1;
+    if ((rc = mu_residual(mu, energy, resN))) return rc;
+    push_hist(energy);
+    // check_converge (optimization.py:522-535)
+    if (nhist - 1 >= o.ncheck) {
+      bool ok = true;
+      for (int i = 0; i < o.ncheck; ++i)
+        if (fabs(ehist_last[nhist - 2 - i] - ehist_last[nhist - 1]) > o.econv) { ok = false; break; }
+      if (ok) { converged = 0; break; }
+    }
+  }
+  if (it >= o.maxiter) converged = 2;
+  // final density = phi^2
+  {
+    T* phi = F<T>(s, F_PHI);
+    rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { rio[i] = phi[i] * phi[i]; }, S_A, st);
+    if (rc) return rc;
+    if ((rc = ts_sync(s))) return rc;
+  }
+  res->energy = energy;
+  res->mu = mu;
+  res->converged = converged;
+  res->n_iter = it;
+  res->n_eval_ev = s.n_ev;
+  res->n_eval_v = s.n_v;
+  res->n_history = nh;
+  for (int k = 0; k < GBOFDFT_NE; ++k) res->energies[k] = s.host[S_EN + k];
+  return 0;
+}
+
+extern "C" {
+
+int gbofdft_tn_workspace_bytes(const gbofdft_plan* p, int64_t* bytes) {
+  GB_REQUIRE(p && bytes, "tn_workspace_bytes: null argument");
+  const size_t fb = ((gb_elem(p) * (size_t)p->N + 255) / 256) * 256;
+  *bytes = (int64_t)(fb * F_NF + sizeof(double) * (kRedBlocks * kMaxVals + S_COUNT) + 256);
+  return GBOFDFT_OK;
+}
+
+int gbofdft_tn_options_default(gbofdft_tn_options* o) {
+  GB_REQUIRE(o, "tn_options_default: null argument");
+  // defaults of Optimization (optimization.py:64-77)
+  o->econv = 1.0e-5;
+  o->maxfun = 50;
+  o->maxiter = 200;
+  o->maxls = 30;
+  o->c1 = 1e-4;
+  o->c2 = 0.2;
+  o->xtol = 1e-12;
+  o->ncheck = 2;
+  o->eps = 0.0;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_optimize_tn(gbofdft_plan* p, const gbofdft_functional* f, void* rho_io, const gbofdft_tn_options* o,
+                        void* workspace, int64_t workspace_bytes, gbofdft_tn_result* res, void* stream) {
+  GB_REQUIRE(p && f && rho_io && o && workspace && res, "optimize_tn: null argument");
+  int64_t need = 0;
+  gbofdft_tn_workspace_bytes(p, &need);
+  GB_REQUIRE(workspace_bytes >= need, "optimize_tn: workspace %lld bytes < %lld", (long long)workspace_bytes,
+             (long long)need);
+  GB_REQUIRE(o->maxiter >= 1 && o->maxfun >= 1 && o->maxls >= 1 && o->ncheck >= 1 && o->ncheck < 60,
+             "optimize_tn: bad options");
+  GB_REQUIRE(((uintptr_t)workspace & 255) == 0, "optimize_tn: workspace must be 256-byte aligned");
+  TnState s;
+  memset(&s, 0, sizeof(s));
+  s.p = p;
+  s.fn = f;
+  s.st = (cudaStream_t)stream;
+  const size_t fb = ((gb_elem(p) * (size_t)p->N + 255) / 256) * 256;
+  char* base = reinterpret_cast<char*>(workspace);
+  for (int i = 0; i < F_NF; ++i) s.w.f[i] = base + fb * i;
+  s.w.partials = reinterpret_cast<double*>(base + fb * F_NF);
+  s.w.sc = s.w.partials + kRedBlocks * kMaxVals;
+  s.w.counter = reinterpret_cast<unsigned*>(s.w.sc + S_COUNT);
+  GB_CUDA(cudaMemsetAsync(s.w.sc, 0, sizeof(double) * S_COUNT + 256, s.st));
+  memset(res->energies, 0, sizeof(res->energies));
+  return p->prec == GBOFDFT_F64 ? tn_run<double>(s, rho_io, *o, res) : tn_run<float>(s, rho_io, *o, res);
+}
+
+int gbofdft_dcsrch(double* state, int64_t state_len, double* stp, double f, double g, int task) {
+  // Host-side line-search step, exposed for tests and for callers that run
+  // their own loops.  state holds the Dcsrch struct (>= 24 doubles); on
+  // DCS_START it is initialised from state[0..4] = ftol, gtol, xtol, stpmin,
+  // stpmax.  Returns the new task code (DCS_* values).
+  GB_REQUIRE(state && stp && state_len * (int64_t)sizeof(double) >= (int64_t)sizeof(Dcsrch),
+             "dcsrch: state buffer too small");
+  Dcsrch s;
+  memcpy(&s, state, sizeof(Dcsrch));
+  if (task == DCS_START) dcs_init(s, state[0], state[1], state[2], state[3], state[4]);
+  const int t = dcs_step(s, *stp, f, g, task);
+  memcpy(state, &s, sizeof(Dcsrch));
+  return t;
+}
+
+}  // extern "C"

@@ -1,0 +1,646 @@
+// FFT passes over a 3D grid with the OF-DFT pointwise work fused in.
+//
+// Data layout (C order): real fields T[n0][n1][n2]; spectra are the half
+// spectrum cpx<T>[n0][n1][ld2] (the first n2h = n2/2+1 columns are valid).
+//
+//   rows forward   real rows -> axis-2 R2C; two real rows ride in one complex
+//                  line (z = a + i b), separated after the transform.  The
+//                  prologue derives up to GB_MAX_FIELDS fields from one read
+//                  of the input (rho, sqrt(rho), rho^beta).
+//   cols           axis-1 or axis-0 C2C on tiles of tb adjacent columns
+//                  (coalesced along the contiguous axis).
+//   cols conv      axis-0 forward, multiply by a reciprocal-space kernel,
+//                  axis-0 inverse, in one pass (no spectrum round trip).
+//   rows inverse   axis-2 C2R (irfftn semantics: imaginary parts of the DC
+//                  and Nyquist columns are ignored), two rows per line; the
+//                  epilogue either stores or assembles the OF-DFT potential
+//                  and the energy densities (compensated FP64 partial sums).
+#include <math.h>
+#include "fft_core.cuh"
+#include "plan.h"
+
+using namespace gbfft;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kZero = 1e-30;                       // dftpy ZERO
+
+template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
+
+template <typename T>
+__device__ __forceinline__ void load_twiddles(cpx<T>* dst, const cpx<T>* src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+// rho^beta; beta == 5/6 uses sqrt(rho) * cbrt(rho)
+template <typename T> __device__ __forceinline__ T pow_beta(T x, double beta) {
+  if (fabs(beta - 5.0 / 6.0) < 1e-15) return sqrt(x) * cbrt(x);
+  return pow(x, (T)beta);
+}
+
+template <typename T>
+__device__ __forceinline__ T prologue(int op, T rho, double beta) {
+  if (op == OP_SQRT) {
+    T r = rho > (T)0 ? rho : (T)kZero;
+    return sqrt(r);
+  }
+  if (op == OP_POWB) {
+    T r = rho < (T)kZero ? (T)kZero : rho;
+    return pow_beta<T>(r, beta);
+  }
+  return rho;
+}
+
+// ---------------------------------------------------------------------------
+// rows forward (R2C along axis 2)
+// ---------------------------------------------------------------------------
+struct RowsFwdArgs {
+  const void* in;
+  void* out;
+  int64_t fstride;
+  int nrows, n2, n2h, ld2, nf, pairs;
+  int op[GB_MAX_FIELDS];
+  double beta, scale;
+  AxisPlan ax;
+  const void* tw;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_fwd(RowsFwdArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n2 = a.n2, P = a.pairs, nf = a.nf;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  const int nl = nf * P;
+  cpx<T>* A = tw + n2;
+  cpx<T>* B = A + (size_t)nl * n2;
+  load_twiddles<T>(tw, reinterpret_cast<const cpx<T>*>(a.tw), n2);
+  const T* in = reinterpret_cast<const T*>(a.in);
+  const int64_t base = (int64_t)blockIdx.x * 2 * P;
+  T* Af = reinterpret_cast<T*>(A);
+  for (int idx = threadIdx.x; idx < 2 * P * n2; idx += blockDim.x) {
+    const int rr = idx / n2, j = idx - rr * n2;
+    const int64_t R = base + rr;
+    const bool ok = R < a.nrows;
+    const T x = ok ? ld(in + R * n2 + j) : (T)0;
+    for (int f = 0; f < nf; ++f) {
+      const T v = ok ? prologue<T>(a.op[f], x, a.beta) : (T)0;
+      Af[2 * ((size_t)(f * P + (rr >> 1)) * n2 + j) + (rr & 1)] = v;
+    }
+  }
+  __syncthreads();
+  cpx<T>* res = lines_fft<-1, T, true>(A, B, tw, a.ax, nl, n2, 1);
+  const int n2h = a.n2h;
+  const T half = (T)0.5 * (T)a.scale;
+  cpx<T>* out = reinterpret_cast<cpx<T>*>(a.out);
+  for (int idx = threadIdx.x; idx < nl * n2h; idx += blockDim.x) {
+    const int line = idx / n2h, k = idx - line * n2h;
+    const int f = line / P, pp = line - f * P;
+    const cpx<T> Z = res[(size_t)line * n2 + k];
+    const cpx<T> Zc = res[(size_t)line * n2 + (k == 0 ? 0 : n2 - k)];
+    const int64_t ra = base + 2 * pp, rb = ra + 1;
+    if (ra >= a.nrows) continue;
+    cpx<T>* o = out + f * a.fstride;
+    o[ra * a.ld2 + k] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
+    if (rb < a.nrows) o[rb * a.ld2 + k] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
+  }
+}
+
+// ---------------------------------------------------------------------------
+// rows inverse (C2R along axis 2) with store or OF-DFT epilogue
+// ---------------------------------------------------------------------------
+struct RowsInvArgs {
+  const void* in;
+  int64_t fstride;
+  int nrows, n2, n2h, ld2, nf, pairs;
+  AxisPlan ax;
+  const void* tw;
+  // store epilogue
+  void* out;
+  int64_t ostride;
+  double scale;
+  // evaluation epilogue
+  EvalDesc ev;
+  const void* rho;
+  const void* vloc;
+  void* pot;
+  double* partials;
+  int calc_e;
+};
+
+template <typename T>
+__device__ __forceinline__ cpx<T>* rows_inv_core(const RowsInvArgs& a, cpx<T>* tw, cpx<T>* A, cpx<T>* B,
+                                                  int64_t base) {
+  const int n2 = a.n2, n2h = a.n2h, P = a.pairs, nl = a.nf * P;
+  load_twiddles<T>(tw, reinterpret_cast<const cpx<T>*>(a.tw), n2);
+  const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
+  for (int idx = threadIdx.x; idx < nl * n2h; idx += blockDim.x) {
+    const int line = idx / n2h, k = idx - line * n2h;
+    const int f = line / P, pp = line - f * P;
+    const int64_t ra = base + 2 * pp, rb = ra + 1;
+    cpx<T> va = {(T)0, (T)0}, vb = {(T)0, (T)0};
+    const cpx<T>* src = in + f * a.fstride;
+    if (ra < a.nrows) va = src[ra * a.ld2 + k];
+    if (rb < a.nrows) vb = src[rb * a.ld2 + k];
+    const bool edge = (k == 0) || (2 * k == n2);
+    if (edge) { va.y = (T)0; vb.y = (T)0; }
+    cpx<T>* L = A + (size_t)line * n2;
+    L[k] = cpx<T>{va.x - vb.y, va.y + vb.x};
+    if (k > 0 && 2 * k < n2) L[n2 - k] = cpx<T>{va.x + vb.y, vb.x - va.y};
+  }
+  __syncthreads();
+  return lines_fft<1, T, true>(A, B, tw, a.ax, nl, n2, 1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_inv_store(RowsInvArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n2 = a.n2, P = a.pairs, nl = a.nf * P;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + n2;
+  cpx<T>* B = A + (size_t)nl * n2;
+  const int64_t base = (int64_t)blockIdx.x * 2 * P;
+  cpx<T>* res = rows_inv_core<T>(a, tw, A, B, base);
+  T* out = reinterpret_cast<T*>(a.out);
+  const T s = (T)a.scale;
+  for (int idx = threadIdx.x; idx < 2 * P * n2; idx += blockDim.x) {
+    const int rr = idx / n2, j = idx - rr * n2;
+    const int64_t R = base + rr;
+    if (R >= a.nrows) continue;
+    for (int f = 0; f < a.nf; ++f) {
+      const cpx<T> z = res[(size_t)(f * P + (rr >> 1)) * n2 + j];
+      out[f * a.ostride + R * n2 + j] = ((rr & 1) ? z.y : z.x) * s;
+    }
+  }
+}
+
+// Perdew-Zunger 1981 LDA (unpolarised): energy density per particle and
+// potential; rho^(1/3) clamped at 1e-30 as in the reference.
+template <typename T>
+__device__ __forceinline__ void pz_lda(T rho, T& eps, T& pot, bool want_e) {
+  const T a = (T)0.0311, b = (T)-0.048, c = (T)0.0020, d = (T)-0.0116;
+  const T g = (T)-0.1423, b1 = (T)1.0529, b2 = (T)0.3334;
+  T rc = cbrt(rho);
+  if (rc < (T)kZero) rc = (T)kZero;
+  const T rs = (T)0.62035049089940001667 / rc;          // (3/(4 pi))^(1/3)
+  const T cx = (T)0.98474502184269654115;                // (3/pi)^(1/3)
+  pot = -cx * rc;
+  eps = (T)(-0.75) * cx * rc;
+  if (rs < (T)1) {
+    const T lr = log(rs);
+    pot += lr * (a + (T)(2.0 / 3.0) * c * rs) + b - (T)(1.0 / 3.0) * a + (T)(1.0 / 3.0) * ((T)2 * d - c) * rs;
+    if (want_e) eps += a * lr + b + c * rs * lr + d * rs;
+  } else {
+    const T sq = sqrt(rs);
+    const T den = (T)1 + b1 * sq + b2 * rs;
+    pot += (g + ((T)(7.0 / 6.0) * g * b1) * sq + ((T)(4.0 / 3.0) * g * b2 * rs)) / (den * den);
+    if (want_e) eps += g / den;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_inv_eval(RowsInvArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n2 = a.n2, P = a.pairs, nl = a.nf * P;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + n2;
+  cpx<T>* B = A + (size_t)nl * n2;
+  const int64_t base = (int64_t)blockIdx.x * 2 * P;
+  cpx<T>* res = rows_inv_core<T>(a, tw, A, B, base);
+  const EvalDesc& ev = a.ev;
+  const T* rhop = reinterpret_cast<const T*>(a.rho);
+  const T* vlocp = reinterpret_cast<const T*>(a.vloc);
+  T* potp = reinterpret_cast<T*>(a.pot);
+  const bool want_e = a.calc_e != 0;
+  const T ctf = (T)2.87123400018819181594;             // (3/10)(3 pi^2)^(2/3)
+  const T alpha = (T)ev.wt_alpha;
+  KSum es[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) es[c].init();
+  for (int idx = threadIdx.x; idx < 2 * P * n2; idx += blockDim.x) {
+    const int rr = idx / n2, j = idx - rr * n2;
+    const int64_t R = base + rr;
+    if (R >= a.nrows) continue;
+    const int pp = rr >> 1;
+    const bool odd = rr & 1;
+    const int64_t gidx = R * n2 + j;
+    const T rho = ld(rhop + gidx);
+    T pot = (T)0;
+    if (ev.tf) {
+      const T cr = cbrt(rho * rho);
+      pot += (T)(5.0 / 3.0) * ctf * cr * (T)ev.tf_x;
+      if (want_e) {
+        T r5 = rho * rho;
+        r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho;
+        es[0].add((double)(cbrt(r5) * ctf) * ev.tf_x);
+      }
+    }
+    if (ev.vw) {
+      const cpx<T> z = res[(size_t)(ev.slot_vw * P + pp) * n2 + j];
+      const T w = odd ? z.y : z.x;
+      T rm = rho > (T)0 ? rho : (T)kZero;
+      T sq = sqrt(rm);
+      if (fabs(sq) < (T)kZero) sq = (T)kZero;
+      const T v = (T)0.5 * w / sq;
+      pot += v * (T)ev.vw_y;
+      if (want_e && rho > (T)0) es[1].add((double)(rho * v) * ev.vw_y);
+    }
+    if (ev.wt) {
+      const cpx<T> z = res[(size_t)(ev.slot_wt * P + pp) * n2 + j];
+      const T kc = odd ? z.y : z.x;
+      const T rc = rho < (T)kZero ? (T)kZero : rho;
+      const T rb = pow_beta<T>(rc, ev.wt_beta);
+      const T v = (T)2 * alpha * (rb / rc) * kc;
+      pot += v;
+      if (want_e) es[2].add((double)(v * rho / ((T)2 * alpha)));
+    }
+    if (ev.xc) {
+      T eps, vx;
+      pz_lda<T>(rho, eps, vx, want_e);
+      pot += vx;
+      if (want_e) es[3].add((double)(eps * rho));
+    }
+    if (ev.hartree) {
+      const cpx<T> z = res[(size_t)(ev.slot_h * P + pp) * n2 + j];
+      const T vh = odd ? z.y : z.x;
+      pot += vh;
+      if (want_e) es[4].add(0.5 * (double)vh * (double)rho);
+    }
+    if (ev.pp) {
+      const T vl = ld(vlocp + gidx);
+      pot += vl;
+      if (want_e) es[5].add((double)vl * (double)rho);
+    }
+    potp[gidx] = pot;
+  }
+  if (!want_e) return;
+  __shared__ double red[8][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    double v = warp_sum(es[c].value());
+    if (lane == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double s = 0.0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) s += red[w][threadIdx.x];
+    a.partials[(int64_t)blockIdx.x * GB_NE + threadIdx.x] = s;
+  }
+}
+
+// Sum per-CTA partials in a fixed order; slot GB_E_TOTAL gets the sum of
+// the components (times dV) plus the constant ion-ion term.
+__global__ void __launch_bounds__(256) k_energy_final(const double* __restrict__ partials, int64_t nblk,
+                                                      double dV, double e_ion, double* __restrict__ e) {
+  __shared__ double red[8][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = 0; c < 6; ++c) {
+    KSum s;
+    s.init();
+    for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) s.add(partials[b * GB_NE + c]);
+    double v = warp_sum(s.value());
+    if (lane == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int c = 0; c < 6; ++c) {
+      KSum s;
+      s.init();
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s.add(red[w][c]);
+      e[c] = s.value() * dV;
+      tot += e[c];
+    }
+    e[GB_E_EXTRA] = 0.0;
+    e[GB_E_TOTAL] = tot + e_ion;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reciprocal-space kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int ffreq(int i, int n) { return (i <= (n - 1) / 2) ? i : i - n; }
+
+template <typename T>
+__device__ __forceinline__ T gg_of(const GInfo& g, int m0, int m1, int m2) {
+  const T gx = (T)m0 * (T)g.bg[0] + (T)m1 * (T)g.bg[3] + (T)m2 * (T)g.bg[6];
+  const T gy = (T)m0 * (T)g.bg[1] + (T)m1 * (T)g.bg[4] + (T)m2 * (T)g.bg[7];
+  const T gz = (T)m0 * (T)g.bg[2] + (T)m1 * (T)g.bg[5] + (T)m2 * (T)g.bg[8];
+  return gx * gx + gy * gy + gz * gz;
+}
+
+// Evaluate a kernel K(|G|) at half-spectrum index (i0, i1, k2) in the
+// reference's convention: with full grids every axis uses fftfreq, and where
+// an index sits on a Nyquist plane the value is averaged with the one at
+// the conjugate partner (-i0, -i1, -k2) -- the real part of the inverse
+// transform sees exactly that average.  Half grids only average inside the
+// k2 = 0 and k2 = n2/2 planes, which are the ones irfftn symmetrises.
+template <typename T, typename F>
+__device__ __forceinline__ T sym_kernel(const GInfo& g, int i0, int i1, int k2, F kv) {
+  const int m0 = ffreq(i0, g.n0), m1 = ffreq(i1, g.n1);
+  const int m2 = g.full ? ffreq(k2, g.n2) : k2;
+  T k = kv(gg_of<T>(g, m0, m1, m2));
+  const bool nyq = ((g.n0 & 1) == 0 && 2 * i0 == g.n0) || ((g.n1 & 1) == 0 && 2 * i1 == g.n1) ||
+                   (g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2);
+  const bool plane = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
+  if (nyq && plane) {
+    const int p0 = ffreq((g.n0 - i0) % g.n0, g.n0), p1 = ffreq((g.n1 - i1) % g.n1, g.n1);
+    const int p2 = g.full ? ffreq((g.n2 - k2) % g.n2, g.n2) : k2;
+    k = (k + kv(gg_of<T>(g, p0, p1, p2))) * (T)0.5;
+  }
+  return k;
+}
+
+template <typename T>
+__device__ __forceinline__ T kernel_value(const GInfo& g, int type, const void* arr, int i0, int i1, int k2) {
+  if (type == KER_HARTREE)
+    return sym_kernel<T>(g, i0, i1, k2, [](T gg) { return gg > (T)0 ? (T)(4.0 * kPi) / gg : (T)0; });
+  if (type == KER_G2) return sym_kernel<T>(g, i0, i1, k2, [](T gg) { return gg; });
+  if (type == KER_ARRAY)
+    return ld(reinterpret_cast<const T*>(arr) + ((int64_t)i0 * g.n1 + i1) * g.n2h + k2);
+  return (T)1;
+}
+
+// ---------------------------------------------------------------------------
+// column passes
+// ---------------------------------------------------------------------------
+struct ColsArgs {
+  void* data;
+  int64_t fstride;
+  int n;           // transform length
+  int64_t stride;  // complex elements between consecutive line elements
+  int64_t ostride; // complex elements between outer groups (blockIdx.y)
+  int ncols, tb;
+  AxisPlan ax;
+  const void* tw;
+  double scale;
+  // convolution (axis 0 only)
+  GInfo gi;
+  KerDesc kd;
+};
+
+template <typename T>
+__device__ __forceinline__ void cols_load(const ColsArgs& a, cpx<T>* buf, const cpx<T>* base, int nc) {
+  for (int idx = threadIdx.x; idx < a.n * nc; idx += blockDim.x) {
+    const int j = idx / nc, c = idx - j * nc;
+    buf[j * a.tb + c] = base[(int64_t)j * a.stride + c];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cols_store(const ColsArgs& a, const cpx<T>* buf, cpx<T>* base, int nc, T s) {
+  for (int idx = threadIdx.x; idx < a.n * nc; idx += blockDim.x) {
+    const int j = idx / nc, c = idx - j * nc;
+    base[(int64_t)j * a.stride + c] = c_scale(buf[j * a.tb + c], s);
+  }
+}
+
+template <typename T, int DIR>
+__global__ void __launch_bounds__(256) k_cols(ColsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + a.n;
+  cpx<T>* B = A + (size_t)a.n * a.tb;
+  load_twiddles<T>(tw, reinterpret_cast<const cpx<T>*>(a.tw), a.n);
+  const int c0 = blockIdx.x * a.tb;
+  const int nc = min(a.tb, a.ncols - c0);
+  cpx<T>* base = reinterpret_cast<cpx<T>*>(a.data) + blockIdx.z * a.fstride + blockIdx.y * a.ostride + c0;
+  cols_load<T>(a, A, base, nc);
+  __syncthreads();
+  cpx<T>* res = lines_fft<DIR, T, false>(A, B, tw, a.ax, nc, 1, a.tb);
+  cols_store<T>(a, res, base, nc, (T)a.scale);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cols_conv(ColsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + a.n;
+  cpx<T>* B = A + (size_t)a.n * a.tb;
+  load_twiddles<T>(tw, reinterpret_cast<const cpx<T>*>(a.tw), a.n);
+  const int c0 = blockIdx.x * a.tb;
+  const int nc = min(a.tb, a.ncols - c0);
+  const int f = blockIdx.z, i1 = blockIdx.y;
+  cpx<T>* base = reinterpret_cast<cpx<T>*>(a.data) + f * a.fstride + i1 * a.ostride + c0;
+  cols_load<T>(a, A, base, nc);
+  __syncthreads();
+  cpx<T>* res = lines_fft<-1, T, false>(A, B, tw, a.ax, nc, 1, a.tb);
+  const int type = a.kd.type[f];
+  const T coef = (T)a.kd.coef[f];
+  const void* arr = a.kd.arr[f];
+  for (int idx = threadIdx.x; idx < a.n * nc; idx += blockDim.x) {
+    const int j = idx / nc, c = idx - j * nc;
+    const T kval = kernel_value<T>(a.gi, type, arr, j, i1, c0 + c) * coef;
+    res[j * a.tb + c] = c_scale(res[j * a.tb + c], kval);
+  }
+  __syncthreads();
+  cpx<T>* other = (res == A) ? B : A;
+  res = lines_fft<1, T, false>(res, other, tw, a.ax, nc, 1, a.tb);
+  cols_store<T>(a, res, base, nc, (T)1);
+}
+
+// ---------------------------------------------------------------------------
+// Wang-Teter kernel table on the half spectrum (inverse Lindhard function).
+// ---------------------------------------------------------------------------
+__constant__ double c_lind_large[15] = {
+    -0.13714285714285712,    -6.39999999999999875e-2, -3.77825602968460128e-2, -2.51824061652633074e-2,
+    -1.80879839616166146e-2, -1.36715733124818332e-2, -1.07236045520990083e-2, -8.65192783339199453e-3,
+    -7.1372762502456763e-3,  -5.9945117538835746e-3,  -5.10997527675418131e-3, -4.41060829979912465e-3,
+    -3.84763737842981233e-3, -3.38745061493813488e-3, -3.00624946457977689e-3};
+
+__device__ double lindhard_inv(double eta, double lbda, double mu) {
+  if (eta > 3.65) {
+    const double inv = 1.0 / (eta * eta);
+    double s = c_lind_large[14];
+    for (int i = 13; i >= 0; --i) s = c_lind_large[i] + inv * s;
+    return 3.0 * (1.0 - mu) * eta * eta - lbda - 0.6 + inv * s;
+  }
+  if (fabs(eta - 1.0) < 1e-10) return 2.0 - lbda - 3.0 * mu + 20.0 * (eta - 1.0);
+  if (eta < 1e-10) return 1.0 - lbda + eta * eta * (1.0 / 3.0 - 3.0 * mu);
+  return 1.0 / (0.5 + 0.25 * (1.0 - eta * eta) * log((1.0 + eta) / fabs(1.0 - eta)) / eta) -
+         3.0 * mu * eta * eta - lbda;
+}
+
+template <typename T>
+__global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __restrict__ out) {
+  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int k2 = (int)(id % g.n2h);
+    const int64_t r = id / g.n2h;
+    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+    const double v = sym_kernel<double>(g, i0, i1, k2, [&](double gg) {
+      return lindhard_inv(sqrt(gg) / tkf, x, 1.0) * factor;
+    });
+    out[id] = (T)v;
+  }
+}
+
+template <typename T> size_t rows_smem(int n2, int nl) { return sizeof(cpx<T>) * ((size_t)n2 + 2 * (size_t)nl * n2); }
+template <typename T> size_t cols_smem(int n, int tb) { return sizeof(cpx<T>) * ((size_t)n + 2 * (size_t)n * tb); }
+
+template <typename K> int set_smem(K kern, size_t bytes) {
+  if (bytes > 48 * 1024) GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename T>
+static int rows_fwd_t(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf,
+                      const int* ops, double beta, double scale, cudaStream_t st) {
+  RowsFwdArgs a;
+  a.in = in; a.out = spec; a.fstride = fstride;
+  a.nrows = p->n[0] * p->n[1]; a.n2 = p->n[2]; a.n2h = p->n2h; a.ld2 = ld2; a.nf = nf;
+  a.pairs = p->pairs;
+  for (int f = 0; f < GB_MAX_FIELDS; ++f) a.op[f] = f < nf ? ops[f] : OP_RHO;
+  a.beta = beta; a.scale = scale; a.ax = p->ax[2]; a.tw = p->tw[2];
+  const size_t sm = rows_smem<T>(a.n2, nf * a.pairs);
+  if (set_smem(k_rows_fwd<T>, sm)) return GBOFDFT_ERR_CUDA;
+  const int nblk = (a.nrows + 2 * a.pairs - 1) / (2 * a.pairs);
+  k_rows_fwd<T><<<nblk, 256, sm, st>>>(a);
+  GB_CHECK_LAUNCH();
+  return 0;
+}
+
+int gb_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf, const int* ops,
+                double beta, double scale, cudaStream_t st) {
+  return p->prec == GBOFDFT_F64 ? rows_fwd_t<double>(p, in, spec, fstride, ld2, nf, ops, beta, scale, st)
+                                : rows_fwd_t<float>(p, in, spec, fstride, ld2, nf, ops, beta, scale, st);
+}
+
+template <typename T>
+static RowsInvArgs rows_inv_args(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf) {
+  RowsInvArgs a;
+  memset(&a, 0, sizeof(a));
+  a.in = spec; a.fstride = fstride;
+  a.nrows = p->n[0] * p->n[1]; a.n2 = p->n[2]; a.n2h = p->n2h; a.ld2 = ld2; a.nf = nf;
+  a.pairs = p->pairs; a.ax = p->ax[2]; a.tw = p->tw[2];
+  return a;
+}
+
+template <typename T>
+static int rows_inv_store_t(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out,
+                            int64_t ostride, double scale, cudaStream_t st) {
+  RowsInvArgs a = rows_inv_args<T>(p, spec, fstride, ld2, nf);
+  a.out = out; a.ostride = ostride; a.scale = scale;
+  const size_t sm = rows_smem<T>(a.n2, nf * a.pairs);
+  if (set_smem(k_rows_inv_store<T>, sm)) return GBOFDFT_ERR_CUDA;
+  const int nblk = (a.nrows + 2 * a.pairs - 1) / (2 * a.pairs);
+  k_rows_inv_store<T><<<nblk, 256, sm, st>>>(a);
+  GB_CHECK_LAUNCH();
+  return 0;
+}
+
+int gb_rows_inv_store(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out,
+                      int64_t ostride, double scale, cudaStream_t st) {
+  return p->prec == GBOFDFT_F64 ? rows_inv_store_t<double>(p, spec, fstride, ld2, nf, out, ostride, scale, st)
+                                : rows_inv_store_t<float>(p, spec, fstride, ld2, nf, out, ostride, scale, st);
+}
+
+template <typename T>
+static int rows_inv_eval_t(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, const EvalDesc& ev,
+                           const void* rho, const void* vloc, void* pot, int calc_e, double* energies,
+                           cudaStream_t st) {
+  RowsInvArgs a = rows_inv_args<T>(p, spec, fstride, p->ld2, nf);
+  a.ev = ev; a.rho = rho; a.vloc = vloc; a.pot = pot; a.partials = p->partials; a.calc_e = calc_e;
+  const int P = a.pairs;
+  const size_t sm = rows_smem<T>(a.n2, (nf > 0 ? nf : 1) * P);
+  if (nf == 0) a.nf = 0;
+  if (set_smem(k_rows_inv_eval<T>, sm)) return GBOFDFT_ERR_CUDA;
+  const int64_t nblk = (a.nrows + 2 * P - 1) / (2 * P);
+  if (nblk > p->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
+  k_rows_inv_eval<T><<<(unsigned)nblk, 256, sm, st>>>(a);
+  GB_CHECK_LAUNCH();
+  if (calc_e) {
+    k_energy_final<<<1, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies);
+    GB_CHECK_LAUNCH();
+  }
+  return 0;
+}
+
+int gb_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, const EvalDesc& ev,
+                     const void* rho, const void* vloc, void* pot, int calc_e, double* energies, cudaStream_t st) {
+  return p->prec == GBOFDFT_F64
+             ? rows_inv_eval_t<double>(p, spec, fstride, nf, ev, rho, vloc, pot, calc_e, energies, st)
+             : rows_inv_eval_t<float>(p, spec, fstride, nf, ev, rho, vloc, pot, calc_e, energies, st);
+}
+
+template <typename T>
+static ColsArgs cols_args(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int axis, double scale) {
+  ColsArgs a;
+  memset(&a, 0, sizeof(a));
+  a.data = spec; a.fstride = fstride;
+  a.n = p->n[axis];
+  a.stride = axis == 1 ? ld2 : (int64_t)p->n[1] * ld2;
+  a.ostride = axis == 1 ? (int64_t)p->n[1] * ld2 : ld2;
+  a.ncols = p->n2h; a.tb = p->tb[axis];
+  a.ax = p->ax[axis]; a.tw = p->tw[axis]; a.scale = scale;
+  a.gi = p->gi;
+  a.gi.ld2 = ld2;
+  return a;
+}
+
+template <typename T>
+static int cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, int dir, double scale,
+                  cudaStream_t st) {
+  ColsArgs a = cols_args<T>(p, spec, fstride, ld2, axis, scale);
+  const size_t sm = cols_smem<T>(a.n, a.tb);
+  dim3 grid((a.ncols + a.tb - 1) / a.tb, p->n[axis == 1 ? 0 : 1], nf);
+  if (dir < 0) {
+    if (set_smem(k_cols<T, -1>, sm)) return GBOFDFT_ERR_CUDA;
+    k_cols<T, -1><<<grid, 256, sm, st>>>(a);
+  } else {
+    if (set_smem(k_cols<T, 1>, sm)) return GBOFDFT_ERR_CUDA;
+    k_cols<T, 1><<<grid, 256, sm, st>>>(a);
+  }
+  GB_CHECK_LAUNCH();
+  return 0;
+}
+
+int gb_cols(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, int dir, double scale,
+            cudaStream_t st) {
+  return p->prec == GBOFDFT_F64 ? cols_t<double>(p, spec, fstride, ld2, nf, axis, dir, scale, st)
+                                : cols_t<float>(p, spec, fstride, ld2, nf, axis, dir, scale, st);
+}
+
+template <typename T>
+static int cols_conv_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, const KerDesc& kd,
+                       double scale, cudaStream_t st) {
+  ColsArgs a = cols_args<T>(p, spec, fstride, ld2, 0, 1.0);
+  a.kd = kd;
+  for (int f = 0; f < nf; ++f) a.kd.coef[f] = kd.coef[f] * scale;
+  const size_t sm = cols_smem<T>(a.n, a.tb);
+  if (set_smem(k_cols_conv<T>, sm)) return GBOFDFT_ERR_CUDA;
+  dim3 grid((a.ncols + a.tb - 1) / a.tb, p->n[1], nf);
+  k_cols_conv<T><<<grid, 256, sm, st>>>(a);
+  GB_CHECK_LAUNCH();
+  return 0;
+}
+
+int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, const KerDesc& kd, double scale,
+                 cudaStream_t st) {
+  return p->prec == GBOFDFT_F64 ? cols_conv_t<double>(p, spec, fstride, ld2, nf, kd, scale, st)
+                                : cols_conv_t<float>(p, spec, fstride, ld2, nf, kd, scale, st);
+}
+
+int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,
+                       cudaStream_t st) {
+  GB_REQUIRE(rho0 > 0.0, "wt kernel: rho0 must be positive (got %g)", rho0);
+  const double tkf = 2.0 * cbrt(3.0 * rho0 * kPi * kPi);
+  const double ctf = 0.3 * pow(3.0 * kPi * kPi, 2.0 / 3.0);
+  const double factor = 5.0 / (9.0 * alpha * beta * pow(rho0, alpha + beta - 5.0 / 3.0)) * ctf;
+  const int64_t total = p->NG;
+  const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
+  if (p->prec == GBOFDFT_F64)
+    k_wt_kernel<double><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<double*>(out));
+  else
+    k_wt_kernel<float><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<float*>(out));
+  GB_CHECK_LAUNCH();
+  return 0;
+}

@@ -1,0 +1,66 @@
+// Host-side plan: grid geometry, FFT schedules, device tables and workspaces.
+#pragma once
+#include "common.cuh"
+
+struct GInfo {           // reciprocal-space geometry passed to kernels by value
+  double bg[9];          // reciprocal lattice vectors, rows (2 pi inv(L)^T)
+  int n0, n1, n2, n2h, ld2;
+  int full;              // 1: full-grid G convention (fftfreq on every axis)
+};
+
+struct gbofdft_plan {
+  int n[3];
+  int n2h;               // n2 / 2 + 1
+  int ld2;               // row pitch of internal spectra (complex elements)
+  int full;
+  int prec;              // GBOFDFT_F32 / GBOFDFT_F64
+  int device;
+  double lattice[9];
+  double bg[9];
+  double volume, dV;
+  int64_t N;             // n0 n1 n2
+  int64_t NG;            // n0 n1 n2h (API spectrum size)
+  int64_t NGld;          // n0 n1 ld2 (internal spectrum size)
+  AxisPlan ax[3];
+  void* tw[3];           // device twiddle tables, complex<prec>[n_axis]
+  void* spec;            // GB_MAX_FIELDS internal spectra
+  double* partials;      // per-CTA energy partial sums
+  int64_t max_partials;  // rows of GB_NE doubles
+  double* scratch;       // small device scratch (reductions), 4096 doubles
+  int tb[3];             // column tile width per axis
+  int pairs;             // row pairs per CTA in the row passes
+  GInfo gi;
+};
+
+size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
+
+// ---- pass launchers (passes.cu) -------------------------------------------
+enum { OP_RHO = 0, OP_SQRT = 1, OP_POWB = 2 };           // forward prologues
+enum { KER_NONE = 0, KER_HARTREE = 1, KER_G2 = 2, KER_ARRAY = 3 };
+
+struct EvalDesc {
+  int tf, vw, wt, xc, hartree, pp;
+  int slot_h, slot_vw, slot_wt;   // field slot of each convolution output
+  double tf_x, vw_y, wt_alpha, wt_beta;
+  double e_ion;
+};
+
+struct KerDesc {
+  int type[GB_MAX_FIELDS];
+  const void* arr[GB_MAX_FIELDS];
+  double coef[GB_MAX_FIELDS];
+};
+
+int gb_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf,
+                const int* ops, double beta, double scale, cudaStream_t st);
+int gb_rows_inv_store(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf,
+                      void* out, int64_t ostride, double scale, cudaStream_t st);
+int gb_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, const EvalDesc& ev,
+                     const void* rho, const void* vloc, void* pot, int calc_e, double* energies,
+                     cudaStream_t st);
+int gb_cols(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, int dir,
+            double scale, cudaStream_t st);
+int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, const KerDesc& kd,
+                 double scale, cudaStream_t st);
+int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,
+                       cudaStream_t st);

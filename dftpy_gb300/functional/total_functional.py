@@ -1,0 +1,102 @@
+"""Sum of functionals (``functional/total_functional.py``).
+
+When every member is one of this package's functionals (KEDF, XC, HARTREE,
+PSEUDO), ``compute`` issues ONE fused device evaluation (``gbofdft_eval``):
+one read of rho, shared transform passes, one write of the total potential.
+Any other AbstractFunctional falls back to summing the members' outputs.
+"""
+from .. import _lib
+from .kedf import KEDF
+from .output import AbstractFunctional, FunctionalOutput
+from .pseudo import LocalPseudo
+from .xc_hartree import XC, Hartree
+from ._eval import Spec, evaluate
+
+_FUSABLE = (KEDF, XC, Hartree, LocalPseudo)
+
+
+class TotalFunctional(AbstractFunctional):
+    def __init__(self, ewald=None, **kwargs):
+        self.funcDict = {k: v for k, v in kwargs.items() if v is not None}
+        self.UpdateNameType()
+        self._ewald = ewald
+
+    def __repr__(self):
+        return self.funcDict.__repr__()
+
+    def __getitem__(self, key):
+        return self.funcDict[key]
+
+    def __setitem__(self, key, value):
+        self.funcDict.update({key: value})
+        self.UpdateNameType()
+
+    def UpdateNameType(self):
+        """``total_functional.py:67-76``: members must be AbstractFunctional."""
+        self.name = ""
+        self.type = ""
+        for key, f in self.funcDict.items():
+            if not isinstance(f, AbstractFunctional):
+                raise TypeError("{} must be AbstractFunctional".format(key))
+            setattr(self, key, f)
+            self.name += getattr(f, "name") + " "
+            self.type += getattr(f, "type") + " "
+
+    def UpdateFunctional(self, keysToRemove=[], newFuncDict={}):
+        for key in keysToRemove:
+            self.funcDict.pop(key, None)
+        self.funcDict.update(newFuncDict)
+        self.UpdateNameType()
+
+    def Subset(self, keys):
+        return TotalFunctional(**{k: self.funcDict[k] for k in keys})
+
+    @property
+    def ewald(self):
+        if self._ewald is not None:
+            return self._ewald
+        for f in self.funcDict.values():
+            if getattr(f, "type", None) == "PSEUDO":
+                return f.get_ewald()
+        return None
+
+    def fusable(self):
+        return all(isinstance(f, _FUSABLE) for f in self.funcDict.values())
+
+    def spec(self, rho):
+        """Merged component description of all members (fused path)."""
+        sp = Spec()
+        for f in self.funcDict.values():
+            sp = sp.merge(f.spec(rho))
+        ew = self.ewald
+        sp.e_ion = float(ew.energy) if ew is not None else 0.0
+        return sp
+
+    def compute(self, rho, calcType={"E", "V"}, **kwargs):
+        return self.get_energy_potential(rho, calcType=calcType, **kwargs)
+
+    def Energy(self, rho, **kwargs):
+        return self.compute(rho, calcType={"E"}).energy
+
+    def get_energy_potential(self, rho, calcType={"E", "V"}, split=False, **kwargs):
+        if self.fusable() and not split:
+            en, pot = evaluate(rho, self.spec(rho), set(calcType) | {"V"})
+            out = FunctionalOutput(name="TOTAL", energy=0.0 if en is None else float(en[_lib.E_TOTAL]))
+            if "V" in calcType:
+                out.potential = pot
+            if en is not None:
+                self.last_energies = en
+            return out
+        parts = {"TOTAL": FunctionalOutput(name="TOTAL", energy=0.0)}
+        for key, func in self.funcDict.items():
+            res = func(rho, calcType=calcType, **kwargs)
+            if split:
+                parts[getattr(func, "type", key)] = res
+            parts["TOTAL"] = parts["TOTAL"] + res
+        ew = self.ewald
+        if ew is not None:
+            r = FunctionalOutput(name="II", energy=ew.energy)
+            if split:
+                parts["II"] = r
+            parts["TOTAL"] = parts["TOTAL"] + r
+        return parts if split else parts["TOTAL"]

@@ -1,0 +1,164 @@
+"""Direct density optimisation (``dftpy/optimization/optimization.py``).
+
+``Optimization(optimization_method="TN", optimization_options=..., EnergyEvaluator=total)``
+runs the truncated-Newton solver of the reference on the GPU
+(``gbofdft_optimize_tn``): the whole loop -- inner CG with finite-difference
+Hessian products, orthogonal rotation, More-Thuente line search, energy
+convergence test -- is native code with device-resident fields.
+
+Added option ``precision``: "fp64" (default for float64 densities, the
+reference's arithmetic), "fp32", or "mixed" (FP32 fields and transforms until
+the FP32 energy stops resolving progress, then FP64 iterations from that
+density to the requested ``econv``).  Reductions are FP64 in every mode.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .field import DirectField
+from .functional.output import FunctionalOutput
+from .functional.total_functional import TotalFunctional
+
+DEFAULTS = {
+    "maxcor": 6,
+    "ftol": 1.0e-7,
+    "xtol": 1.0e-12,
+    "maxfun": 50,
+    "maxiter": 200,
+    "maxls": 30,
+    "econv": 1.0e-5,
+    "c1": 1e-4,
+    "c2": 0.2,
+    "algorithm": "EMM",
+    "vector": "Orthogonalization",
+    "ncheck": 2,
+    "precision": None,
+    "eps": None,
+    "fp32_econv": None,
+    "fp32_eps": -1.0e-3,
+}
+
+
+class Optimization:
+    def __init__(self, optimization_method="CG-HS", optimization_options=None, EnergyEvaluator=None,
+                 guess_rho=None):
+        self.rho = guess_rho
+        self.optimization_options = dict(optimization_options or {})
+        for k, v in DEFAULTS.items():
+            self.optimization_options.setdefault(k, v)
+        if EnergyEvaluator is None:
+            raise AttributeError("Must provide an energy evaluator")
+        self.EnergyEvaluator = EnergyEvaluator
+        self.optimization_method = optimization_method
+        self.converged = None
+        self.mu = None
+        self.energy = None
+        self.history = []
+        self.stats = {}
+        self._functional = None
+
+    # ------------------------------------------------------------------------
+    def _check(self):
+        if self.optimization_method != "TN":
+            raise NotImplementedError("optimization_method %r: this build implements the truncated-Newton "
+                                      "path (method 'TN')" % self.optimization_method)
+        o = self.optimization_options
+        if o["algorithm"] != "EMM" or o["vector"] != "Orthogonalization":
+            raise NotImplementedError("only algorithm='EMM' with vector='Orthogonalization' is implemented")
+        ev = self.EnergyEvaluator
+        if not (isinstance(ev, TotalFunctional) and ev.fusable()):
+            raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
+                                      "functionals (KEDF, XC, HARTREE, PSEUDO)")
+
+    def _run(self, rho, econv, eps, maxiter):
+        o = self.optimization_options
+        grid = rho.grid
+        plan = grid.plan(rho.dtype)
+        L = _lib.load()
+        opts = _lib.TnOptions()
+        _lib.check(L.gbofdft_tn_options_default(ctypes.byref(opts)))
+        opts.econv = float(econv)
+        opts.maxfun = int(o["maxfun"])
+        opts.maxiter = int(maxiter)
+        opts.maxls = int(o["maxls"])
+        opts.c1, opts.c2, opts.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
+        opts.ncheck = int(o["ncheck"])
+        opts.eps = float(eps)
+        spec = self.EnergyEvaluator.spec(rho)
+        f = spec.ctypes()
+        nb = ctypes.c_int64()
+        _lib.check(L.gbofdft_tn_workspace_bytes(plan.handle, ctypes.byref(nb)))
+        ws = _workspace(grid, rho.dtype, int(nb.value))
+        r = rho.as_subclass(torch.Tensor).contiguous().clone()
+        res = _lib.TnResult()
+        hist = (ctypes.c_double * 4096)()
+        res.history = hist
+        res.history_cap = 4096
+        _lib.check(L.gbofdft_optimize_tn(plan.handle, ctypes.byref(f), _lib.ptr(r), ctypes.byref(opts),
+                                         _lib.aligned_ptr(ws, 256), int(nb.value), ctypes.byref(res),
+                                         _lib.stream_ptr()), "optimize_tn")
+        out = dict(energy=res.energy, mu=res.mu, converged=res.converged, n_iter=res.n_iter,
+                   n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, energies=list(res.energies),
+                   history=[hist[i] for i in range(res.n_history)])
+        return DirectField(grid, data=r), out
+
+    def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):
+        """``optimization.py:281-520`` (method TN)."""
+        if guess_rho is None and self.rho is None:
+            raise AttributeError("Must provide a guess density")
+        if guess_rho is not None:
+            self.rho = guess_rho
+        if guess_phi is not None or lphi:
+            raise NotImplementedError("guess_phi / lphi are not part of this path")
+        self._check()
+        o = self.optimization_options
+        rho = self.rho
+        if not isinstance(rho, DirectField):
+            raise TypeError("guess_rho must be a DirectField")
+        prec = o["precision"] or ("fp64" if rho.dtype == torch.float64 else "fp32")
+        self.stats = {"stages": []}
+        if prec in ("fp64", "fp32"):
+            dt = torch.float64 if prec == "fp64" else torch.float32
+            eps = o["eps"] if o["eps"] is not None else (1e-9 if dt == torch.float64 else o["fp32_eps"])
+            r, out = self._run(rho.to(dt) if rho.dtype != dt else rho, o["econv"], eps, o["maxiter"])
+            self.stats["stages"].append(dict(precision=prec, **out))
+        elif prec == "mixed":
+            e32 = o["fp32_econv"] if o["fp32_econv"] is not None else o["econv"]
+            r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"])
+            self.stats["stages"].append(dict(precision="fp32", **out32))
+            eps = o["eps"] if o["eps"] is not None else 1e-9
+            r, out = self._run(r32.to(torch.float64), o["econv"], eps, o["maxiter"])
+            self.stats["stages"].append(dict(precision="fp64", **out))
+        else:
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed', got %r" % (prec,))
+        self.converged = out["converged"]
+        self.mu = out["mu"]
+        self.energy = out["energy"]
+        self.history = out["history"]
+        self.rho = r
+        self._functional = None
+        return r
+
+    @property
+    def functional(self):
+        if self._functional is None and self.rho is not None:
+            self._functional = self.EnergyEvaluator(self.rho, calcType={"E", "V"})
+        return self._functional
+
+    def __call__(self, guess_rho=None, calcType={"E", "V"}, guess_phi=None, lphi=False):
+        return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)
+
+
+_WS = {}
+
+
+def _workspace(grid, dtype, nbytes):
+    """Per-(grid, dtype) device workspace for the optimiser (allocated once)."""
+    key = (id(grid), dtype)
+    t = _WS.get(key)
+    if t is None or t.numel() * 8 < nbytes + 512:
+        t = torch.empty(nbytes // 8 + 64, dtype=torch.float64, device="cuda")
+        _WS[key] = t
+    return t

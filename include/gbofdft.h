@@ -1,0 +1,237 @@
+/*
+ * gbofdft: GB300-native orbital-free DFT energy/potential evaluation and
+ * direct density optimisation -- the C ABI.
+ *
+ * Every entry point returns an int status (GBOFDFT_OK = 0, otherwise a
+ * gbofdft_status code; gbofdft_last_error() gives the message).  All device
+ * pointers are caller-owned; a plan owns only its tables and workspaces, so
+ * entry points never allocate.  Work is ordered on the given CUDA stream
+ * (``stream`` is a cudaStream_t, NULL = legacy default stream) and nothing
+ * synchronises unless the entry point says so.  A plan holds per-plan
+ * workspaces: do not use one plan on two streams at the same time.
+ *
+ * Precision: GBOFDFT_F64 plans take double / complex-double buffers,
+ * GBOFDFT_F32 plans float / complex-float.  Energies are always double.
+ *
+ * Layouts (C order): real field [n0][n1][n2]; spectrum (half) complex
+ * [n0][n1][n2/2+1], interleaved re/im.  Forward transforms carry the grid
+ * volume element dV, inverse ones 1/dV (dftpy's field.py convention).
+ */
+#ifndef GBOFDFT_H
+#define GBOFDFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBOFDFT_ABI_VERSION 1
+
+enum gbofdft_status {
+  GBOFDFT_OK = 0,
+  GBOFDFT_ERR_ARG = 1,         /* bad argument (python: ValueError / TypeError) */
+  GBOFDFT_ERR_CUDA = 2,        /* CUDA runtime error */
+  GBOFDFT_ERR_UNSUPPORTED = 3, /* size or option not supported */
+  GBOFDFT_ERR_ALLOC = 4,       /* plan workspace allocation failed */
+  GBOFDFT_ERR_NUMERIC = 5,     /* non-finite or invalid numerical state */
+  GBOFDFT_ERR_STATE = 6        /* inconsistent plan / buffer state */
+};
+
+enum gbofdft_precision { GBOFDFT_F32 = 0, GBOFDFT_F64 = 1 };
+
+enum gbofdft_calc { GBOFDFT_CALC_E = 1, GBOFDFT_CALC_V = 2 };
+
+/* energies[] slots written by gbofdft_eval (Hartree atomic units) */
+enum gbofdft_energy_slot {
+  GBOFDFT_E_TF = 0,
+  GBOFDFT_E_VW = 1,
+  GBOFDFT_E_NL = 2,
+  GBOFDFT_E_XC = 3,
+  GBOFDFT_E_HARTREE = 4,
+  GBOFDFT_E_PSEUDO = 5,
+  GBOFDFT_E_EXTRA = 6,
+  GBOFDFT_E_TOTAL = 7,
+  GBOFDFT_NE = 8
+};
+
+typedef struct gbofdft_plan gbofdft_plan;
+
+/* ABI version of the loaded library. */
+int gbofdft_version(void);
+
+/* Copy the last error message (thread-local) into buf; returns its length. */
+int gbofdft_last_error(char* buf, size_t len);
+
+/*
+ * Grid plan.  Replaces dftpy DirectGrid / ReciprocalGrid set-up
+ * (src/dftpy/grid.py:302-330 DirectGrid.__init__, :384-415 get_reciprocal).
+ * lattice: 3x3 row-major, rows are lattice vectors (Bohr).  full = 1 selects
+ * the reference's full-grid G convention (DirectGrid(full=True)).
+ */
+int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision, int full,
+                        gbofdft_plan** out);
+int gbofdft_plan_destroy(gbofdft_plan* plan);
+
+/* out[0] = N real points, out[1] = half-spectrum size, out[2] = n2/2+1,
+ * out[3] = device workspace bytes held by the plan. */
+int gbofdft_plan_sizes(const gbofdft_plan* plan, int64_t out[4]);
+
+/* Forward 3D R2C, times dV.  Replaces DirectField.fft (src/dftpy/field.py:373-390). */
+int gbofdft_fft_r2c(gbofdft_plan* plan, const void* in, void* out, void* stream);
+
+/* Inverse 3D C2R, divided by dV, irfftn semantics; ``in`` is not modified.
+ * Replaces ReciprocalField.ifft(force_real=True) (src/dftpy/field.py:739-764). */
+int gbofdft_fft_c2r(gbofdft_plan* plan, const void* in, void* out, void* stream);
+
+/* Reciprocal-space kernels for gbofdft_convolve */
+enum gbofdft_kernel { GBOFDFT_KER_NONE = 0, GBOFDFT_KER_HARTREE = 1, GBOFDFT_KER_G2 = 2, GBOFDFT_KER_ARRAY = 3 };
+
+/*
+ * out = ifft(fft(in) * coef * K(G)) in one pipeline (real in, real out).
+ * K = 4 pi / G^2 (G=0 -> 0), G^2, or a real half-spectrum array.
+ * Replaces the fft -> multiply -> ifft pattern of hartree.py:34-38,
+ * vw.py:45-49 and wt.py:21.
+ */
+int gbofdft_convolve(gbofdft_plan* plan, const void* in, void* out, int kernel, const void* kernel_array,
+                     double coef, void* stream);
+
+/* Functional composition for gbofdft_eval (TotalFunctional of
+ * KEDF(TF/vW/WT) + XC(LDA) + HARTREE + PSEUDO). */
+typedef struct gbofdft_functional {
+  int tf;                /* Thomas-Fermi, kedf/tf.py:66-80 */
+  double tf_x;
+  int vw;                /* von Weizsaecker, kedf/vw.py:115-131 */
+  double vw_y;
+  int wt;                /* Wang-Teter nonlocal, kedf/wt.py:109-132 */
+  double wt_alpha, wt_beta;
+  const void* wt_kernel; /* real half spectrum from gbofdft_wt_kernel */
+  int xc;                /* 1 = Perdew-Zunger LDA, xc/semilocal_xc.py:253-290 */
+  int hartree;           /* hartree.py:24-45 */
+  const void* vloc;      /* real field (local pseudopotential) or NULL, pseudo/__init__.py:219-234 */
+  double e_ion;          /* constant ion-ion energy added to the total */
+} gbofdft_functional;
+
+/*
+ * Energy and potential of the composed functional at rho.
+ * Replaces TotalFunctional.compute (src/dftpy/functional/total_functional.py:107-146).
+ * calc: GBOFDFT_CALC_E | GBOFDFT_CALC_V.  pot (real field) is always written;
+ * with CALC_E, energies_dev (device, GBOFDFT_NE doubles) receives the
+ * component energies and the total (ion-ion term included).
+ */
+int gbofdft_eval(gbofdft_plan* plan, const void* rho, const gbofdft_functional* f, void* pot,
+                 double* energies_dev, int calc, void* stream);
+
+/*
+ * Wang-Teter kernel on the half spectrum for mean density rho0.
+ * Replaces get_ke_kernel_wt / WTKernel (kedf/wt.py:58-73, kedf/kernel.py:325-334).
+ */
+int gbofdft_wt_kernel(gbofdft_plan* plan, double rho0, double x, double alpha, double beta, void* kernel_out,
+                      void* stream);
+
+/* ---- set-up: local pseudopotential and ion-ion energy --------------------- */
+
+#define GBOFDFT_MAX_SPECIES 16
+
+/* One species' v(|G|) table, evaluated as dftpy's LocalPseudo.calc_vlines
+ * (functional/pseudo/__init__.py:350-375): cubic spline pieces on knots x[0..m-1]
+ * (c: (m-1) x 4 coefficients of a + b u + c u^2 + d u^3, u = q - x[i]) for
+ * gmin <= q < gmax, quartic q4[0..4] in q/dp (divided by 24 for the
+ * non-constant part, math_utils.py:457-467) below gmin, 0 from gmax on.
+ * x and c are device pointers. */
+typedef struct gbofdft_vtable {
+  const double* x;
+  const double* c;
+  int m;
+  double q4[5];
+  double dp, gmin, gmax;
+} gbofdft_vtable;
+
+/* Device workspace bytes for gbofdft_vloc / gbofdft_ewald with nat atoms. */
+int gbofdft_setup_workspace_bytes(const gbofdft_plan* plan, int nat, int64_t* bytes);
+
+/*
+ * Local pseudopotential v_loc on the half spectrum (vloc_recip, complex) and,
+ * if vloc_real != NULL, in real space.  spos_dev: fractional positions
+ * (nat x 3, in [0,1)), species_dev: species index per atom.  pme != 0 uses
+ * order-`order` cardinal B-spline structure factors with bm_dev = the b(m)
+ * factors of the three axes concatenated (n0 + n1 + n2/2+1 complex doubles);
+ * pme == 0 the exact structure factor.
+ * Replaces LocalPseudo.local_PP / _PP_Reciprocal(_PME)
+ * (src/dftpy/functional/pseudo/__init__.py:237-246, 377-404).
+ */
+int gbofdft_vloc(gbofdft_plan* plan, int nspec, const gbofdft_vtable* tables, int nat, const double* spos_dev,
+                 const int* species_dev, int pme, int order, const double* bm_dev, void* work, int64_t work_bytes,
+                 void* vloc_recip, void* vloc_real, void* stream);
+
+/*
+ * Ewald sums of the ions: out_dev[0] = real-space part, out_dev[1] =
+ * reciprocal part (PME or exact).  The host adds the constant correction
+ * and chooses eta, rmax and the lattice images (nimg x 3 Cartesian offsets).
+ * Replaces ewald.Energy_real(_fast2), Energy_rec(_PME) (src/dftpy/ewald.py:281-466,
+ * 786-808).
+ */
+int gbofdft_ewald(gbofdft_plan* plan, int nat, const double* pos_dev, const double* spos_dev,
+                  const double* charges_dev, double eta, double rmax, const double* images_dev, int nimg, int pme,
+                  int order, const double* bm_dev, void* work, int64_t work_bytes, double* out_dev, void* stream);
+
+/* ---- direct density optimisation (truncated Newton) ---------------------- */
+
+/* Options of Optimization(optimization_method="TN") (optimization.py:64-77). */
+typedef struct gbofdft_tn_options {
+  double econv;  /* stop when the last ncheck energy changes are <= econv (Ha) */
+  int maxfun;    /* inner CG iterations per TN direction */
+  int maxiter;   /* outer iterations */
+  int maxls;     /* line-search evaluations per outer iteration */
+  double c1, c2, xtol; /* More-Thuente parameters */
+  int ncheck;
+  double eps;    /* finite-difference step of the Hessian product: > 0 fixed
+                    (the reference uses 1e-9), < 0 relative: |eps| ||phi|| / ||r0||
+                    per TN direction (single precision), 0 -> 1e-9 */
+} gbofdft_tn_options;
+
+typedef struct gbofdft_tn_result {
+  double energy;          /* total energy at the final density (Ha) */
+  double mu;              /* chemical potential (Ha) */
+  int converged;          /* 0 converged, 1 line search failed, 2 maxiter */
+  int n_iter;
+  int n_eval_ev;          /* energy+potential evaluations */
+  int n_eval_v;           /* potential-only evaluations */
+  double energies[GBOFDFT_NE];
+  double* history;        /* optional host array receiving the energy history */
+  int history_cap;
+  int n_history;
+} gbofdft_tn_result;
+
+int gbofdft_tn_options_default(gbofdft_tn_options* opts);
+
+/* Bytes of device workspace gbofdft_optimize_tn needs for this plan. */
+int gbofdft_tn_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
+
+/*
+ * Minimise the composed functional over rho (fixed electron number) by
+ * truncated Newton in phi = sqrt(rho) with the orthogonal rotation line
+ * search.  rho_io: initial density in, optimised density out.  workspace:
+ * caller-owned device buffer (256-byte aligned) of gbofdft_tn_workspace_bytes.
+ * Synchronises the stream (the control flow needs the scalars).
+ * Replaces Optimization.optimize_rho with method "TN"
+ * (src/dftpy/optimization/optimization.py:281-520).
+ */
+int gbofdft_optimize_tn(gbofdft_plan* plan, const gbofdft_functional* f, void* rho_io,
+                        const gbofdft_tn_options* opts, void* workspace, int64_t workspace_bytes,
+                        gbofdft_tn_result* result, void* stream);
+
+/*
+ * One call of the More-Thuente line-search state machine (host only).
+ * Replaces minpack2.dcsrch as driven by LineSearchDcsrch2
+ * (src/dftpy/math_utils.py:76-106).  task codes: 0 START, 1 FG (evaluate f,g
+ * at *stp), 2 CONVERGENCE, 3 WARNING, 4 ERROR.  On START, state[0..4] hold
+ * ftol, gtol, xtol, stpmin, stpmax; state needs >= 24 doubles.
+ */
+int gbofdft_dcsrch(double* state, int64_t state_len, double* stp, double f, double g, int task);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBOFDFT_H */

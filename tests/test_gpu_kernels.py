@@ -1,0 +1,227 @@
+"""GPU kernels through the C ABI against the oracle (numpy FP64).
+
+Tolerances: FP64 results within 1e-11 of the oracle relative to the field's
+max magnitude (FFT round-off); FP32 results within 2e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import ofdft as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from dftpy_gb300 import _lib
+    _lib.require_cuda()
+    return _lib
+
+
+def _dt(prec):
+    torch = _torch()
+    return torch.float64 if prec == 1 else torch.float32
+
+
+def _cdt(prec):
+    torch = _torch()
+    return torch.complex128 if prec == 1 else torch.complex64
+
+
+SIZES = [(32, 32, 32), (36, 36, 72), (51, 51, 51), (8, 12, 10), (96, 128, 160), (30, 30, 30), (7, 9, 11),
+         (2, 4, 6)]
+
+
+def _lattice(nr, skew=False):
+    L = np.diag([7.65 * nr[0] / 32, 7.65 * nr[1] / 32, 7.65 * nr[2] / 32])
+    if skew:
+        L[1, 0] = 0.4 * L[0, 0]
+        L[2, 1] = 0.3 * L[1, 1]
+    return L
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+@pytest.mark.parametrize("nr", SIZES)
+def test_fft_r2c_c2r(lib, nr, prec):
+    torch = _torch()
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(nr)
+    L = _lattice(nr)
+    plan = lib.Plan(nr, L, precision=prec)
+    g = O.Grid(L, nr)
+    xd = torch.tensor(x, dtype=_dt(prec), device="cuda")
+    out = torch.empty(nr[0], nr[1], nr[2] // 2 + 1, dtype=_cdt(prec), device="cuda")
+    lib.check(lib.load().gbofdft_fft_r2c(plan.handle, lib.ptr(xd), lib.ptr(out), lib.stream_ptr()))
+    ref = O.fft(x, g)
+    tol = 1e-12 if prec == 1 else 3e-6
+    scale = np.abs(ref).max()
+    assert np.abs(out.cpu().numpy() - ref).max() <= tol * scale * np.log2(max(nr))
+    back = torch.empty(nr, dtype=_dt(prec), device="cuda")
+    spec = torch.tensor(ref, dtype=_cdt(prec), device="cuda")
+    spec_copy = spec.clone()
+    lib.check(lib.load().gbofdft_fft_c2r(plan.handle, lib.ptr(spec), lib.ptr(back), lib.stream_ptr()))
+    assert torch.equal(spec, spec_copy), "c2r must not modify its input"
+    ref2 = O.ifft(ref, g)
+    assert np.abs(back.cpu().numpy() - ref2).max() <= tol * np.abs(ref2).max() * np.log2(max(nr))
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+@pytest.mark.parametrize("skew", [False, True])
+@pytest.mark.parametrize("full", [False, True])
+@pytest.mark.parametrize("kernel", ["hartree", "g2"])
+def test_convolve(lib, prec, skew, full, kernel):
+    torch = _torch()
+    nr = (12, 10, 16)
+    L = _lattice(nr, skew)
+    rng = np.random.default_rng(2)
+    x = rng.random(nr) + 0.1
+    g = O.Grid(L, nr, full=full)
+    K = 4 * np.pi * g.invgg if kernel == "hartree" else g.gg
+    ref = O.ifft(O.fft(x, g) * K, g)
+    plan = lib.Plan(nr, L, precision=prec, full=full)
+    xd = torch.tensor(x, dtype=_dt(prec), device="cuda")
+    out = torch.empty_like(xd)
+    k = lib.KER_HARTREE if kernel == "hartree" else lib.KER_G2
+    lib.check(lib.load().gbofdft_convolve(plan.handle, lib.ptr(xd), lib.ptr(out), k, None, 1.0, lib.stream_ptr()))
+    tol = 1e-12 if prec == 1 else 2e-5
+    assert np.abs(out.cpu().numpy() - ref).max() <= tol * np.abs(ref).max()
+
+
+def _eval_gpu(lib, plan, rho, kedf, vloc, e_ion, prec, calc_e=True):
+    torch = _torch()
+    dt = _dt(prec)
+    rd = torch.tensor(np.ascontiguousarray(rho), dtype=dt, device="cuda")
+    f = lib.Functional()
+    f.tf, f.tf_x, f.vw, f.vw_y = 1, 1.0, 1, 1.0
+    kern = None
+    if kedf == "WT":
+        rho0 = float(rho.mean())
+        kern = torch.empty(plan.nr[0], plan.nr[1], plan.n2h, dtype=dt, device="cuda")
+        lib.check(lib.load().gbofdft_wt_kernel(plan.handle, rho0, 1.0, 5 / 6, 5 / 6, lib.ptr(kern), lib.stream_ptr()))
+        f.wt, f.wt_alpha, f.wt_beta, f.wt_kernel = 1, 5 / 6, 5 / 6, kern.data_ptr()
+    f.xc, f.hartree = 1, 1
+    vd = None
+    if vloc is not None:
+        vd = torch.tensor(vloc, dtype=dt, device="cuda")
+        f.vloc = vd.data_ptr()
+    f.e_ion = e_ion
+    pot = torch.empty_like(rd)
+    en = torch.zeros(lib.NE, dtype=torch.float64, device="cuda")
+    lib.check(lib.load().gbofdft_eval(plan.handle, lib.ptr(rd), f, lib.ptr(pot), lib.ptr(en),
+                                      (lib.CALC_E if calc_e else 0) | lib.CALC_V, lib.stream_ptr()))
+    torch.cuda.synchronize()
+    return en.cpu().numpy(), pot.cpu().numpy()
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+def test_eval_fde_wt(lib, golden, prec):
+    """KEDF WT + LDA + Hartree + PP on the reference's test density (full grid)."""
+    d = golden("fde")
+    g = O.Grid(d["lattice"], d["nr"], full=True)
+    rho = d["rho"]
+    from dftpy_gb300 import systems
+    tab = {"Al": systems.analytic_pp_table(3.0, 1.0)}
+    vloc = O.local_pp(g, d["positions"], ["Al"] * 2, tab)
+    plan = lib.Plan(d["nr"], d["lattice"], precision=prec, full=True)
+    en, pot = _eval_gpu(lib, plan, rho, "WT", vloc, 0.0, prec)
+    e_tf, v_tf = O.tf(rho, g)
+    e_vw, v_vw = O.vw(rho, g)
+    e_wt, v_wt = O.WTNL()(rho, g)
+    e_xc, v_xc = O.lda(rho, g)
+    e_h, v_h = O.hartree(rho, g)
+    e_pp = float(np.einsum("ijk,ijk->", vloc, rho) * g.dV)
+    ref = dict(TF=e_tf, VW=e_vw, NL=e_wt, XC=e_xc, HARTREE=e_h, PSEUDO=e_pp)
+    etol = 1e-10 if prec == 1 else 2e-5
+    for i, k in enumerate(["TF", "VW", "NL", "XC", "HARTREE", "PSEUDO"]):
+        assert abs(en[i] - ref[k]) <= etol * max(1.0, abs(ref[k])), (k, en[i], ref[k])
+    # the reference's own asserted KEDF(WT) value
+    assert abs(en[0] + en[1] + en[2] - 2.916818700014412) <= (1e-10 if prec == 1 else 2e-5)
+    vref = v_tf + v_vw + v_wt + v_xc + v_h + vloc
+    vtol = 1e-10 if prec == 1 else 2e-5
+    assert np.abs(pot - vref).max() <= vtol * np.abs(vref).max()
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+def test_eval_al4_tfvw(lib, golden, prec):
+    """TFVW + LDA + Hartree + PP (PME) at the converged config-1 density."""
+    a = golden("al4")
+    from dftpy_gb300 import systems
+    st = systems.config_al4(0)
+    ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
+    rho = a["rho"]
+    e_ref, v_ref = ev(rho)
+    plan = lib.Plan(st.nr, st.lattice, precision=prec)
+    en, pot = _eval_gpu(lib, plan, rho, "TFVW", ev.vloc, ev.ewald["energy"], prec)
+    etol = 1e-10 if prec == 1 else 1e-5
+    assert abs(en[lib.E_TOTAL] - e_ref) <= etol * abs(e_ref)
+    assert abs(en[lib.E_TOTAL] - float(a["E_final"])) <= (1e-8 if prec == 1 else 1e-4)
+    # FP32: the vW potential divides FFT output by sqrt(rho), which amplifies
+    # single-precision round-off where the density is low
+    vtol = 1e-10 if prec == 1 else 1e-3
+    assert np.abs(pot - v_ref).max() <= vtol * np.abs(v_ref).max()
+
+
+COMPONENTS = ["TF", "VW", "WT", "XC", "HARTREE", "PP", "VW+HARTREE", "HARTREE+VW+WT"]
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+@pytest.mark.parametrize("comp", COMPONENTS)
+@pytest.mark.parametrize("case", ["fde", "rand"])
+def test_eval_single_components(lib, golden, prec, comp, case):
+    torch = _torch()
+    if case == "fde":
+        d = golden("fde")
+        nr, L, full, rho = tuple(int(x) for x in d["nr"]), d["lattice"], True, d["rho"]
+    else:
+        nr, L, full = (12, 10, 16), _lattice((12, 10, 16), True), False
+        rho = 0.02 + 0.01 * np.random.default_rng(3).random(nr)
+    g = O.Grid(L, nr, full=full)
+    vloc = np.sin(np.arange(np.prod(nr)).reshape(nr) * 0.01)
+    parts = comp.split("+")
+    f = lib.Functional()
+    eref, vref = 0.0, np.zeros(nr)
+    kern = None
+    dt = _dt(prec)
+    plan = lib.Plan(nr, L, precision=prec, full=full)
+    for c in parts:
+        if c == "TF":
+            f.tf, f.tf_x = 1, 1.0
+            e, v = O.tf(rho, g)
+        elif c == "VW":
+            f.vw, f.vw_y = 1, 1.0
+            e, v = O.vw(rho, g)
+        elif c == "WT":
+            kern = torch.empty(nr[0], nr[1], nr[2] // 2 + 1, dtype=dt, device="cuda")
+            lib.check(lib.load().gbofdft_wt_kernel(plan.handle, float(rho.mean()), 1.0, 5 / 6, 5 / 6,
+                                                   lib.ptr(kern), lib.stream_ptr()))
+            f.wt, f.wt_alpha, f.wt_beta, f.wt_kernel = 1, 5 / 6, 5 / 6, kern.data_ptr()
+            e, v = O.WTNL()(rho, g)
+        elif c == "XC":
+            f.xc = 1
+            e, v = O.lda(rho, g)
+        elif c == "HARTREE":
+            f.hartree = 1
+            e, v = O.hartree(rho, g)
+        else:
+            e, v = float(np.einsum("ijk,ijk->", vloc, rho) * g.dV), vloc
+        eref += e
+        vref = vref + v
+    rd = torch.tensor(np.ascontiguousarray(rho), dtype=dt, device="cuda")
+    vd = torch.tensor(vloc, dtype=dt, device="cuda")
+    if "PP" in parts:
+        f.vloc = vd.data_ptr()
+    pot = torch.empty_like(rd)
+    en = torch.zeros(lib.NE, dtype=torch.float64, device="cuda")
+    lib.check(lib.load().gbofdft_eval(plan.handle, lib.ptr(rd), f, lib.ptr(pot), lib.ptr(en),
+                                      lib.CALC_E | lib.CALC_V, lib.stream_ptr()))
+    torch.cuda.synchronize()
+    tol = 1e-10 if prec == 1 else 3e-5
+    e = float(en[lib.E_TOTAL])
+    assert abs(e - eref) <= tol * max(1.0, abs(eref)), (e, eref)
+    p = pot.cpu().numpy()
+    assert np.abs(p - vref).max() <= tol * np.abs(vref).max()

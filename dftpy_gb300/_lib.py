@@ -63,6 +63,7 @@ _lib = None
 _P = ctypes.c_void_p
 _SIGS = [
     ("gbofdft_version", ctypes.c_int, []),
+    ("gbofdft_launch_count", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     ("gbofdft_plan_create", ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
@@ -141,6 +142,12 @@ def ptr(t):
     if not t.is_contiguous():
         raise ValueError("gbofdft: buffers must be C-contiguous (got strides %s)" % (tuple(t.stride()),))
     return ctypes.c_void_p(t.data_ptr())
+
+
+def launch_count():
+    n = ctypes.c_int64()
+    check(load().gbofdft_launch_count(ctypes.byref(n)))
+    return int(n.value)
 
 
 def aligned_ptr(t, align=256):

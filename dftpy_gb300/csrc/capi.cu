@@ -9,7 +9,12 @@
 
 #include "plan.h"
 
+#include <atomic>
+
 static thread_local char g_err[1024] = "";
+static std::atomic<long long> g_launches(0);
+
+void gb_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int gb_set_error(int code, const char* fmt, ...) {
   va_list ap;
@@ -45,6 +50,12 @@ static void det_inv(const double* L, double* inv, double* det) {
 extern "C" {
 
 int gbofdft_version(void) { return GBOFDFT_ABI_VERSION; }
+
+int gbofdft_launch_count(int64_t* count) {
+  GB_REQUIRE(count, "launch_count: null argument");
+  *count = (int64_t)g_launches.load(std::memory_order_relaxed);
+  return GBOFDFT_OK;
+}
 
 int gbofdft_last_error(char* buf, size_t len) {
   size_t n = strlen(g_err);

@@ -20,8 +20,11 @@ int gb_set_error(int code, const char* fmt, ...);
                           #call, cudaGetErrorString(_e));                          \
   } while (0)
 
+void gb_count_launch();
+
 #define GB_CHECK_LAUNCH()                                                          \
   do {                                                                             \
+    gb_count_launch();                                                             \
     cudaError_t _e = cudaGetLastError();                                           \
     if (_e != cudaSuccess)                                                         \
       return gb_set_error(GBOFDFT_ERR_CUDA, "%s:%d launch: %s", __FILE__, __LINE__, \

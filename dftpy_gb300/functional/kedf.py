@@ -41,7 +41,7 @@ class KEDF(AbstractFunctional):
         density moves by more than 1e-6 or the grid changes."""
         rho0 = self.options.get("rho0", None)
         if not rho0:
-            rho0 = rho.amean()
+            rho0 = float(rho.as_subclass(torch.Tensor).to(torch.float64).mean())
         s = self.ke_kernel_saved
         shape = tuple(rho.shape)
         if abs(s["rho0"] - rho0) > 1e-6 or s["shape"] != shape or s["dtype"] != rho.dtype:

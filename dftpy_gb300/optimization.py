@@ -129,7 +129,13 @@ class Optimization:
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
-            r, out = self._run(r32.to(torch.float64), o["econv"], eps, o["maxiter"])
+            # the FP32 stage conserves the electron number only to single
+            # precision: restore the guess's integral before refining in FP64
+            r64 = r32.to(torch.float64)
+            n_in = float(rho.as_subclass(torch.Tensor).to(torch.float64).sum())
+            n_out = float(r64.as_subclass(torch.Tensor).sum())
+            r64 = r64 * (n_in / n_out)
+            r, out = self._run(r64, o["econv"], eps, o["maxiter"])
             self.stats["stages"].append(dict(precision="fp64", **out))
         else:
             raise ValueError("precision must be 'fp64', 'fp32' or 'mixed', got %r" % (prec,))

@@ -1,0 +1,66 @@
+"""Repeat the functional evaluation of the 256-atom / 128^3 WT workload.
+
+``python -m dftpy_gb300.profile_eval --precision fp32 --calc V --reps 3``
+sets the structure up, runs warm-up evaluations, then ``reps`` evaluations
+inside an NVTX range named ``eval`` (so a profiler can select exactly those
+launches with ``--nvtx --nvtx-include eval/``) and prints the CUDA-event
+time per evaluation.
+"""
+import argparse
+import os
+import sys
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--calc", default="V", choices=["V", "EV"])
+    p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--workload", default="al256", choices=["al256", "al4"])
+    a = p.parse_args()
+    import torch
+    from . import _lib, systems
+    from . import functional as F
+    from .field import DirectField
+    from .grid import DirectGrid
+    from .ions import Ions
+    st = systems.config_al256(0) if a.workload == "al256" else systems.config_al4(0)
+    grid = DirectGrid(st.lattice, st.nr, full=False)
+    ions = Ions(st.symbols, positions=st.positions, cell=st.lattice)
+    ps = F.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": F.AnalyticPP(3.0, 1.0)}, PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="WT"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    dt = torch.float32 if a.precision == "fp32" else torch.float64
+    g = torch.Generator(device="cuda").manual_seed(0)
+    base = st.nelec / st.volume
+    x = (base * (1.0 + 0.05 * torch.randn(tuple(st.nr), generator=g, device="cuda", dtype=torch.float64))).to(dt)
+    rho = DirectField(grid, data=x)
+    f = total.spec(rho).ctypes()
+    plan = grid.plan(dt)
+    xr = rho.as_subclass(torch.Tensor).contiguous()
+    pot = torch.empty_like(xr)
+    en = torch.empty(_lib.NE, dtype=torch.float64, device="cuda")
+    calc = _lib.CALC_V | (_lib.CALC_E if a.calc == "EV" else 0)
+    L = _lib.load()
+    s = _lib.stream_ptr()
+    for _ in range(a.warmup):
+        _lib.check(L.gbofdft_eval(plan.handle, _lib.ptr(xr), f, _lib.ptr(pot), _lib.ptr(en), calc, s))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("eval")
+    e0.record()
+    for _ in range(a.reps):
+        _lib.check(L.gbofdft_eval(plan.handle, _lib.ptr(xr), f, _lib.ptr(pot), _lib.ptr(en), calc, s))
+    e1.record()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    print("eval %s %s %s: %.1f us per evaluation" % (a.workload, a.precision, a.calc,
+                                                     e0.elapsed_time(e1) * 1000.0 / a.reps))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -61,6 +61,9 @@ typedef struct gbofdft_plan gbofdft_plan;
 /* ABI version of the loaded library. */
 int gbofdft_version(void);
 
+/* Number of kernels this library has launched in this process (monotonic). */
+int gbofdft_launch_count(int64_t* count);
+
 /* Copy the last error message (thread-local) into buf; returns its length. */
 int gbofdft_last_error(char* buf, size_t len);
 

@@ -113,8 +113,22 @@ class Grid:
         return np.pi ** 2 / (2.0 * spacing ** 2)        # math_utils.py:331
 
 
+_FFT_WORKERS = 1
+
+
+def set_fft_workers(n):
+    """Threads for the oracle's FFTs (1: numpy pocketfft, the reference's own
+    backend here; >1: scipy's pocketfft with worker threads)."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = max(1, int(n))
+
+
 def fft(x, grid):
     """``DirectField.fft`` (``field.py:373-390``)."""
+    if _FFT_WORKERS > 1:
+        import scipy.fft as sf
+        f = sf.fftn if grid.full else sf.rfftn
+        return f(x, workers=_FFT_WORKERS) * grid.dV
     if grid.full:
         return np.fft.fftn(x) * grid.dV
     return np.fft.rfftn(x) * grid.dV
@@ -122,9 +136,14 @@ def fft(x, grid):
 
 def ifft(xg, grid):
     """``ReciprocalField.ifft(force_real=True)`` (``field.py:739-764``)."""
+    if _FFT_WORKERS > 1:
+        import scipy.fft as sf
+        if grid.full:
+            return sf.ifftn(xg, workers=_FFT_WORKERS).real / grid.dV
+        return sf.irfftn(xg, s=grid.nr, axes=(0, 1, 2), workers=_FFT_WORKERS) / grid.dV
     if grid.full:
         return np.fft.ifftn(xg).real / grid.dV
-    return np.fft.irfftn(xg, s=grid.nr) / grid.dV
+    return np.fft.irfftn(xg, s=grid.nr, axes=(0, 1, 2)) / grid.dV
 
 
 # ----------------------------------------------------------------------------

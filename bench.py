@@ -170,8 +170,11 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1000.0)
         energies.append(opt.energy)
-        evals.append([(st["precision"], st["n_eval_ev"], st["n_eval_v"], st["converged"]) for st in
-                      opt.stats["stages"]])
+        evals.append([{"precision": st["precision"], "n_eval_ev": st["n_eval_ev"], "n_eval_v": st["n_eval_v"],
+                       "converged": st["converged"], "n_iter": st["n_iter"], "n_sync": st["n_sync"],
+                       "t_sync_s": round(st["t_sync"], 4), "t_host_s": round(st["t_total"], 4),
+                       "last_dE": [round(e - st["history"][-1], 12) for e in st["history"][-5:]]}
+                      for st in opt.stats["stages"]])
     launches = _lib.launch_count() - l0
     return times, energies, evals, launches
 

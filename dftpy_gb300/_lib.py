@@ -54,7 +54,8 @@ class TnResult(ctypes.Structure):
     _fields_ = [("energy", ctypes.c_double), ("mu", ctypes.c_double), ("converged", ctypes.c_int),
                 ("n_iter", ctypes.c_int), ("n_eval_ev", ctypes.c_int), ("n_eval_v", ctypes.c_int),
                 ("energies", ctypes.c_double * 8), ("history", ctypes.POINTER(ctypes.c_double)),
-                ("history_cap", ctypes.c_int), ("n_history", ctypes.c_int)]
+                ("history_cap", ctypes.c_int), ("n_history", ctypes.c_int), ("n_sync", ctypes.c_int),
+                ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double)]
 
 
 _lib = None

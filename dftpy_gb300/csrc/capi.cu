@@ -10,11 +10,29 @@
 #include "plan.h"
 
 #include <atomic>
+#include <map>
+#include <mutex>
 
 static thread_local char g_err[1024] = "";
 static std::atomic<long long> g_launches(0);
 
 void gb_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// dynamic shared-memory grants already made with cudaFuncSetAttribute
+static std::mutex g_smem_mu;
+static std::map<std::pair<const void*, int>, int> g_smem;
+
+int gb_smem_granted(const void* kern, int dev) {
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  auto it = g_smem.find({kern, dev});
+  return it == g_smem.end() ? 0 : it->second;
+}
+
+void gb_smem_grant(const void* kern, int dev, int bytes) {
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  int& v = g_smem[{kern, dev}];
+  if (bytes > v) v = bytes;
+}
 
 int gb_set_error(int code, const char* fmt, ...) {
   va_list ap;
@@ -89,7 +107,11 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   memset(p, 0, sizeof(*p));
   for (int a = 0; a < 3; ++a) p->n[a] = nr[a];
   p->n2h = nr[2] / 2 + 1;
-  p->ld2 = p->n2h;
+  // internal spectrum rows padded to whole 128-byte lines
+  {
+    const int per_line = precision == GBOFDFT_F64 ? 8 : 16;
+    p->ld2 = (p->n2h + per_line - 1) / per_line * per_line;
+  }
   p->full = full ? 1 : 0;
   p->prec = precision;
   cudaGetDevice(&p->device);

@@ -12,6 +12,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <chrono>
+
 #include "dcsrch.h"
 #include "plan.h"
 
@@ -119,11 +121,21 @@ struct TnState {
   cudaStream_t st;
   double host[S_COUNT];
   int n_ev, n_v;
+  int n_sync;
+  double t_sync;  // host seconds blocked in stream synchronisation
+  double t_start;
 };
 
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 static int ts_sync(TnState& s) {
+  const double t0 = now_s();
   GB_CUDA(cudaMemcpyAsync(s.host, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
   GB_CUDA(cudaStreamSynchronize(s.st));
+  s.t_sync += now_s() - t0;
+  ++s.n_sync;
   return 0;
 }
 
@@ -414,6 +426,9 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   res->n_eval_ev = s.n_ev;
   res->n_eval_v = s.n_v;
   res->n_history = nh;
+  res->n_sync = s.n_sync;
+  res->t_sync = s.t_sync;
+  res->t_total = now_s() - s.t_start;
   for (int k = 0; k < GBOFDFT_NE; ++k) res->energies[k] = s.host[S_EN + k];
   return 0;
 }
@@ -457,6 +472,7 @@ int gbofdft_optimize_tn(gbofdft_plan* p, const gbofdft_functional* f, void* rho_
   s.p = p;
   s.fn = f;
   s.st = (cudaStream_t)stream;
+  s.t_start = now_s();
   const size_t fb = ((gb_elem(p) * (size_t)p->N + 255) / 256) * 256;
   char* base = reinterpret_cast<char*>(workspace);
   for (int i = 0; i < F_NF; ++i) s.w.f[i] = base + fb * i;

@@ -16,10 +16,17 @@
 //                  epilogue either stores or assembles the OF-DFT potential
 //                  and the energy densities (compensated FP64 partial sums).
 #include <math.h>
+#include <stdlib.h>
+#include <string.h>
 #include "fft_core.cuh"
+#include "gkernels.cuh"
 #include "plan.h"
 
 using namespace gbfft;
+using gbk::ffreq;
+using gbk::gg_of;
+using gbk::sym_kernel;
+using gbk::kernel_value;
 
 namespace {
 
@@ -319,51 +326,6 @@ __global__ void __launch_bounds__(256) k_energy_final(const double* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// reciprocal-space kernels
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int ffreq(int i, int n) { return (i <= (n - 1) / 2) ? i : i - n; }
-
-template <typename T>
-__device__ __forceinline__ T gg_of(const GInfo& g, int m0, int m1, int m2) {
-  const T gx = (T)m0 * (T)g.bg[0] + (T)m1 * (T)g.bg[3] + (T)m2 * (T)g.bg[6];
-  const T gy = (T)m0 * (T)g.bg[1] + (T)m1 * (T)g.bg[4] + (T)m2 * (T)g.bg[7];
-  const T gz = (T)m0 * (T)g.bg[2] + (T)m1 * (T)g.bg[5] + (T)m2 * (T)g.bg[8];
-  return gx * gx + gy * gy + gz * gz;
-}
-
-// Evaluate a kernel K(|G|) at half-spectrum index (i0, i1, k2) in the
-// reference's convention: with full grids every axis uses fftfreq, and where
-// an index sits on a Nyquist plane the value is averaged with the one at
-// the conjugate partner (-i0, -i1, -k2) -- the real part of the inverse
-// transform sees exactly that average.  Half grids only average inside the
-// k2 = 0 and k2 = n2/2 planes, which are the ones irfftn symmetrises.
-template <typename T, typename F>
-__device__ __forceinline__ T sym_kernel(const GInfo& g, int i0, int i1, int k2, F kv) {
-  const int m0 = ffreq(i0, g.n0), m1 = ffreq(i1, g.n1);
-  const int m2 = g.full ? ffreq(k2, g.n2) : k2;
-  T k = kv(gg_of<T>(g, m0, m1, m2));
-  const bool nyq = ((g.n0 & 1) == 0 && 2 * i0 == g.n0) || ((g.n1 & 1) == 0 && 2 * i1 == g.n1) ||
-                   (g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2);
-  const bool plane = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
-  if (nyq && plane) {
-    const int p0 = ffreq((g.n0 - i0) % g.n0, g.n0), p1 = ffreq((g.n1 - i1) % g.n1, g.n1);
-    const int p2 = g.full ? ffreq((g.n2 - k2) % g.n2, g.n2) : k2;
-    k = (k + kv(gg_of<T>(g, p0, p1, p2))) * (T)0.5;
-  }
-  return k;
-}
-
-template <typename T>
-__device__ __forceinline__ T kernel_value(const GInfo& g, int type, const void* arr, int i0, int i1, int k2) {
-  if (type == KER_HARTREE)
-    return sym_kernel<T>(g, i0, i1, k2, [](T gg) { return gg > (T)0 ? (T)(4.0 * kPi) / gg : (T)0; });
-  if (type == KER_G2) return sym_kernel<T>(g, i0, i1, k2, [](T gg) { return gg; });
-  if (type == KER_ARRAY)
-    return ld(reinterpret_cast<const T*>(arr) + ((int64_t)i0 * g.n1 + i1) * g.n2h + k2);
-  return (T)1;
-}
-
-// ---------------------------------------------------------------------------
 // column passes
 // ---------------------------------------------------------------------------
 struct ColsArgs {
@@ -508,8 +470,22 @@ static int rows_fwd_t(gbofdft_plan* p, const void* in, void* spec, int64_t fstri
   return 0;
 }
 
+int gb_use_ct() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GBOFDFT_GENERIC_FFT");
+    v = (e && e[0] == '1') ? 0 : 1;
+  }
+  return v;
+}
+
 int gb_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf, const int* ops,
                 double beta, double scale, cudaStream_t st) {
+  if (gb_use_ct()) {
+    const int rc = p->prec == GBOFDFT_F64 ? gb_ct_rows_fwd_f64(p, in, spec, fstride, ld2, nf, ops, beta, scale, st)
+                                          : gb_ct_rows_fwd_f32(p, in, spec, fstride, ld2, nf, ops, beta, scale, st);
+    if (rc != 1) return rc;
+  }
   return p->prec == GBOFDFT_F64 ? rows_fwd_t<double>(p, in, spec, fstride, ld2, nf, ops, beta, scale, st)
                                 : rows_fwd_t<float>(p, in, spec, fstride, ld2, nf, ops, beta, scale, st);
 }
@@ -539,6 +515,14 @@ static int rows_inv_store_t(gbofdft_plan* p, const void* spec, int64_t fstride, 
 
 int gb_rows_inv_store(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out,
                       int64_t ostride, double scale, cudaStream_t st) {
+  if (gb_use_ct()) {
+    const int rc = p->prec == GBOFDFT_F64
+                       ? gb_ct_rows_inv_f64(p, spec, fstride, ld2, nf, out, ostride, scale, nullptr, nullptr, nullptr,
+                                            nullptr, 0, nullptr, nullptr, st)
+                       : gb_ct_rows_inv_f32(p, spec, fstride, ld2, nf, out, ostride, scale, nullptr, nullptr, nullptr,
+                                            nullptr, 0, nullptr, nullptr, st);
+    if (rc != 1) return rc;
+  }
   return p->prec == GBOFDFT_F64 ? rows_inv_store_t<double>(p, spec, fstride, ld2, nf, out, ostride, scale, st)
                                 : rows_inv_store_t<float>(p, spec, fstride, ld2, nf, out, ostride, scale, st);
 }
@@ -566,6 +550,20 @@ static int rows_inv_eval_t(gbofdft_plan* p, const void* spec, int64_t fstride, i
 
 int gb_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, const EvalDesc& ev,
                      const void* rho, const void* vloc, void* pot, int calc_e, double* energies, cudaStream_t st) {
+  if (gb_use_ct()) {
+    int64_t nblk = 0;
+    const int rc = p->prec == GBOFDFT_F64
+                       ? gb_ct_rows_inv_f64(p, spec, fstride, p->ld2, nf, nullptr, 0, 1.0, &ev, rho, vloc, pot, calc_e,
+                                            p->partials, &nblk, st)
+                       : gb_ct_rows_inv_f32(p, spec, fstride, p->ld2, nf, nullptr, 0, 1.0, &ev, rho, vloc, pot, calc_e,
+                                            p->partials, &nblk, st);
+    if (rc == 0 && calc_e) {
+      if (nblk > p->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
+      k_energy_final<<<1, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies);
+      GB_CHECK_LAUNCH();
+    }
+    if (rc != 1) return rc;
+  }
   return p->prec == GBOFDFT_F64
              ? rows_inv_eval_t<double>(p, spec, fstride, nf, ev, rho, vloc, pot, calc_e, energies, st)
              : rows_inv_eval_t<float>(p, spec, fstride, nf, ev, rho, vloc, pot, calc_e, energies, st);
@@ -605,6 +603,11 @@ static int cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf,
 
 int gb_cols(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, int dir, double scale,
             cudaStream_t st) {
+  if (gb_use_ct()) {
+    const int rc = p->prec == GBOFDFT_F64 ? gb_ct_cols_f64(p, spec, fstride, ld2, nf, axis, dir, scale, nullptr, st)
+                                          : gb_ct_cols_f32(p, spec, fstride, ld2, nf, axis, dir, scale, nullptr, st);
+    if (rc != 1) return rc;
+  }
   return p->prec == GBOFDFT_F64 ? cols_t<double>(p, spec, fstride, ld2, nf, axis, dir, scale, st)
                                 : cols_t<float>(p, spec, fstride, ld2, nf, axis, dir, scale, st);
 }
@@ -625,6 +628,13 @@ static int cols_conv_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, in
 
 int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, const KerDesc& kd, double scale,
                  cudaStream_t st) {
+  if (gb_use_ct()) {
+    KerDesc k2 = kd;
+    for (int f = 0; f < nf; ++f) k2.coef[f] = kd.coef[f] * scale;
+    const int rc = p->prec == GBOFDFT_F64 ? gb_ct_cols_f64(p, spec, fstride, ld2, nf, 0, -1, 1.0, &k2, st)
+                                          : gb_ct_cols_f32(p, spec, fstride, ld2, nf, 0, -1, 1.0, &k2, st);
+    if (rc != 1) return rc;
+  }
   return p->prec == GBOFDFT_F64 ? cols_conv_t<double>(p, spec, fstride, ld2, nf, kd, scale, st)
                                 : cols_conv_t<float>(p, spec, fstride, ld2, nf, kd, scale, st);
 }

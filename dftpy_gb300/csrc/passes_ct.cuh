@@ -1,0 +1,497 @@
+// Compile-time-size versions of the FFT passes of passes.cu (same data
+// layout, same semantics), instantiated for the grid sizes of the workloads.
+// Each launcher returns 1 when the size has no specialisation (the caller
+// then uses the generic runtime-radix kernels), 0 on success, or an error.
+#pragma once
+#include <math.h>
+#include <string.h>
+#include <type_traits>
+
+#include "fft_ct.cuh"
+#include "gkernels.cuh"
+#include "plan.h"
+
+namespace gbct {
+
+constexpr double kZero = 1e-30;
+
+template <typename F>
+__host__ inline bool ct_dispatch(int n, F&& f) {
+  switch (n) {
+    case 32: f(std::integral_constant<int, 32>{}); return true;
+    case 64: f(std::integral_constant<int, 64>{}); return true;
+    case 96: f(std::integral_constant<int, 96>{}); return true;
+    case 128: f(std::integral_constant<int, 128>{}); return true;
+    case 160: f(std::integral_constant<int, 160>{}); return true;
+    case 256: f(std::integral_constant<int, 256>{}); return true;
+    case 360: f(std::integral_constant<int, 360>{}); return true;
+    default: return false;
+  }
+}
+
+template <typename T> struct RowsCfg;            // row pairs per CTA (per field)
+template <> struct RowsCfg<float> { static constexpr int RP = 4; };
+template <> struct RowsCfg<double> { static constexpr int RP = 4; };
+// threads of a row-pass CTA: TPL per line, one line per (field, row pair)
+template <typename T, int N> constexpr int rows_threads_max() { return Tpl<N>::value * RowsCfg<T>::RP * GB_MAX_FIELDS; }
+template <typename T, int N> struct ColsCfg {     // columns per tile
+  static constexpr int TB = (sizeof(T) == 4 && N <= 256) ? 16 : 8;
+};
+
+// ---- pointwise functions -----------------------------------------------------
+// x^(1/2), x^(5/6) and friends for x >= 1e-30 (the reference's clamps)
+template <typename T> __device__ __forceinline__ T sqrt_pos(T x) { return x * rsqrt_d(x); }
+
+template <typename T> __device__ __forceinline__ T pow_beta_ct(T x, double beta) {
+  if (fabs(beta - 5.0 / 6.0) < 1e-15) {
+    const T z3 = rcbrt_d(x), z2 = rsqrt_d(x);
+    return (x * z2) * (x * z3 * z3);         // x^(1/2) x^(1/3)
+  }
+  return pow(x, (T)beta);
+}
+
+template <typename T>
+__device__ __forceinline__ T prologue_ct(int op, T rho, double beta) {
+  if (op == OP_SQRT) return sqrt_pos<T>(rho > (T)0 ? rho : (T)kZero);
+  if (op == OP_POWB) return pow_beta_ct<T>(rho < (T)kZero ? (T)kZero : rho, beta);
+  return rho;
+}
+
+// ---- rows forward ---------------------------------------------------------------
+// One CTA: RP row pairs of the input, all nf derived fields transformed at
+// once (line = field * RP + pair; TPL threads per line).
+struct CtRowsFwd {
+  const void* in;
+  void* out;
+  int64_t fstride;
+  int nrows, ld2, nf;
+  int op[GB_MAX_FIELDS];
+  double beta, scale;
+  const void* tw;
+};
+
+template <typename T, int N>
+__global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_fwd(CtRowsFwd a) {
+  constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nl = a.nf * RP;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + N;
+  cpx<T>* B = A + nl * NP;
+  T* R = reinterpret_cast<T*>(B + nl * NP);      // [2 RP][N] real input rows
+  const int tid = threadIdx.x, l = tid / TPL, lane = tid % TPL;
+  const int64_t base = (int64_t)blockIdx.x * 2 * RP;
+  const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
+  const T* in = reinterpret_cast<const T*>(a.in);
+  for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
+    const int64_t row = base + idx / N;
+    R[idx] = row < a.nrows ? __ldg(in + row * N + idx % N) : (T)0;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nl * N; idx += blockDim.x) {
+    const int line = idx / N, j = idx % N;
+    const int f = line / RP, l2 = line % RP;
+    const int op = a.op[f];
+    const int64_t ra = base + 2 * l2;
+    const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], a.beta) : (T)0;
+    const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], a.beta) : (T)0;
+    A[sw<T, NP>(line, j)] = cpx<T>{x0, x1};
+  }
+  __syncthreads();
+  cpx<T>* res = fft<-1, T, N>(A, B, tw, l, lane, true);
+  cpx<T>* out = reinterpret_cast<cpx<T>*>(a.out);
+  const T half = (T)(0.5 * a.scale);
+  for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
+    const int line = idx / NH, k = idx % NH;
+    const int f = line / RP, l2 = line % RP;
+    const int64_t ra = base + 2 * l2, rb = ra + 1;
+    if (ra >= a.nrows) continue;
+    const cpx<T> Z = res[sw<T, NP>(line, k)];
+    const cpx<T> Zc = res[sw<T, NP>(line, k == 0 ? 0 : N - k)];
+    cpx<T>* o = out + f * a.fstride;
+    o[ra * a.ld2 + k] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
+    if (rb < a.nrows) o[rb * a.ld2 + k] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
+  }
+}
+
+// ---- rows inverse ----------------------------------------------------------------
+struct CtRowsInv {
+  const void* in;
+  int64_t fstride;
+  int nrows, ld2, nf;
+  const void* tw;
+  void* out;
+  int64_t ostride;
+  double scale;
+  EvalDesc ev;
+  const void* rho;
+  const void* vloc;
+  void* pot;
+  double* partials;
+  int calc_e;
+};
+
+// irfftn line build (all fields) + inverse FFT; result line (f * RP + pair)
+// holds row 2 pair in .x and row 2 pair + 1 in .y.
+template <typename T, int N>
+__device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t base, cpx<T>* tw, cpx<T>* A,
+                                                     cpx<T>* B) {
+  constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
+  const int tid = threadIdx.x, l = tid / TPL, lane = tid % TPL;
+  const int nl = a.nf * RP;
+  const cpx<T>* src0 = reinterpret_cast<const cpx<T>*>(a.in);
+  for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
+    const int line = idx / NH, k = idx % NH;
+    const int f = line / RP, l2 = line % RP;
+    const cpx<T>* src = src0 + f * a.fstride;
+    const int64_t ra = base + 2 * l2, rb = ra + 1;
+    cpx<T> va = {(T)0, (T)0}, vb = {(T)0, (T)0};
+    if (ra < a.nrows) va = src[ra * a.ld2 + k];
+    if (rb < a.nrows) vb = src[rb * a.ld2 + k];
+    if (k == 0 || 2 * k == N) { va.y = (T)0; vb.y = (T)0; }
+    A[sw<T, NP>(line, k)] = cpx<T>{va.x - vb.y, va.y + vb.x};
+    if (k > 0 && 2 * k < N) A[sw<T, NP>(line, N - k)] = cpx<T>{va.x + vb.y, vb.x - va.y};
+  }
+  __syncthreads();
+  return fft<1, T, N>(A, B, tw, l, lane, true);
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_store(CtRowsInv a) {
+  constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nl = a.nf * RP;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + N;
+  cpx<T>* B = A + nl * NP;
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * 2 * RP;
+  const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
+  cpx<T>* res = ct_rows_inv_lines<T, N>(a, base, tw, A, B);
+  T* out = reinterpret_cast<T*>(a.out);
+  const T s = (T)a.scale;
+  for (int idx = tid; idx < a.nf * 2 * RP * N; idx += blockDim.x) {
+    const int f = idx / (2 * RP * N), r = idx % (2 * RP * N);
+    const int rr = r / N, j = r % N;
+    const int64_t row = base + rr;
+    if (row >= a.nrows) continue;
+    const cpx<T> z = res[sw<T, NP>(f * RP + (rr >> 1), j)];
+    out[f * a.ostride + row * N + j] = ((rr & 1) ? z.y : z.x) * s;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void pz_lda_ct(T rho, T& eps, T& pot, bool want_e) {
+  const T a = (T)0.0311, b = (T)-0.048, c = (T)0.0020, d = (T)-0.0116;
+  const T g = (T)-0.1423, b1 = (T)1.0529, b2 = (T)0.3334;
+  const T cx = (T)0.98474502184269654115;                 // (3/pi)^(1/3)
+  T rc, inv_rc;                                             // rho^(1/3), clamped at 1e-30
+  if (rho > (T)kZero) {
+    inv_rc = rcbrt_d(rho);
+    rc = rho * inv_rc * inv_rc;
+  } else {
+    rc = cbrt(rho);
+    if (rc < (T)kZero) rc = (T)kZero;
+    inv_rc = (T)1 / rc;
+  }
+  const T rs = (T)0.62035049089940001667 * inv_rc;        // (3/(4 pi))^(1/3) / rho^(1/3)
+  pot = -cx * rc;
+  eps = (T)(-0.75) * cx * rc;
+  if (rs < (T)1) {
+    const T lr = log(rs);
+    pot += lr * (a + (T)(2.0 / 3.0) * c * rs) + b - (T)(1.0 / 3.0) * a + (T)(1.0 / 3.0) * ((T)2 * d - c) * rs;
+    if (want_e) eps += a * lr + b + c * rs * lr + d * rs;
+  } else {
+    const T sq = rs * rsqrt_d(rs);
+    const T inv = (T)1 / ((T)1 + b1 * sq + b2 * rs);
+    pot += (g + ((T)(7.0 / 6.0) * g * b1) * sq + ((T)(4.0 / 3.0) * g * b2 * rs)) * inv * inv;
+    if (want_e) eps += g * inv;
+  }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(CtRowsInv a) {
+  constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nl = (a.nf > 0 ? a.nf : 1) * RP;
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + N;
+  cpx<T>* B = A + nl * NP;
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * 2 * RP;
+  const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
+  cpx<T>* res = A;
+  if (a.nf > 0) res = ct_rows_inv_lines<T, N>(a, base, tw, A, B);
+  const EvalDesc& ev = a.ev;
+  const T* rhop = reinterpret_cast<const T*>(a.rho);
+  const T* vlocp = reinterpret_cast<const T*>(a.vloc);
+  T* potp = reinterpret_cast<T*>(a.pot);
+  const bool want_e = a.calc_e != 0;
+  const T ctf = (T)2.87123400018819181594;               // (3/10)(3 pi^2)^(2/3)
+  const T alpha = (T)ev.wt_alpha;
+  const bool b56 = fabs(ev.wt_beta - 5.0 / 6.0) < 1e-15;
+  double es[6] = {0, 0, 0, 0, 0, 0};
+  for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
+    const int rr = idx / N, j = idx % N;
+    const int64_t row = base + rr;
+    if (row >= a.nrows) continue;
+    const int64_t gidx = row * N + j;
+    const int pr = rr >> 1;
+    const bool odd = rr & 1;
+    const T rho = __ldg(rhop + gidx);
+    const bool pos = rho > (T)kZero;
+    // rho^(-1/3) and rho^(-1/2) for positive densities (shared by TF, vW, WT)
+    T z3 = (T)0, z2 = (T)0;
+    if (pos) { z3 = rcbrt_d(rho); z2 = rsqrt_d(rho); }
+    T pot = (T)0;
+    if (ev.tf) {
+      T r23;                                              // cbrt(rho^2)
+      if (pos) r23 = rho * z3;
+      else r23 = cbrt(rho * rho);
+      pot += (T)(5.0 / 3.0) * ctf * r23 * (T)ev.tf_x;
+      if (want_e) {
+        T r53;                                            // cbrt(rho^5)
+        if (pos) r53 = rho * rho * z3;
+        else { T r5 = rho * rho; r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho; r53 = cbrt(r5); }
+        es[0] += (double)(r53 * ctf) * ev.tf_x;
+      }
+    }
+    if (ev.vw) {
+      const cpx<T> zz = res[sw<T, NP>(ev.slot_vw * RP + pr, j)];
+      const T w = odd ? zz.y : zz.x;
+      // 1 / max(sqrt(rho_m), 1e-30), rho_m = rho if rho > 0 else 1e-30
+      const T inv_sq = pos ? z2 : (rho > (T)0 ? (T)1 / fmax(sqrt(rho), (T)kZero) : (T)1e15);
+      const T v = (T)0.5 * w * inv_sq;
+      pot += v * (T)ev.vw_y;
+      if (want_e && rho > (T)0) es[1] += (double)(rho * v) * ev.vw_y;
+    }
+    if (ev.wt) {
+      const cpx<T> zz = res[sw<T, NP>(ev.slot_wt * RP + pr, j)];
+      const T kc = odd ? zz.y : zz.x;
+      T rb_over_rc;                                       // rc^(beta - 1), rc = max(rho, 1e-30)
+      if (b56) {
+        if (pos) rb_over_rc = rho * z3 * z3 * z2;          // rho^(1/3) rho^(-1/2)
+        else { const T rc = (T)kZero; rb_over_rc = sqrt(rc) * cbrt(rc) / rc; }
+      } else {
+        const T rc = rho < (T)kZero ? (T)kZero : rho;
+        rb_over_rc = pow(rc, (T)ev.wt_beta) / rc;
+      }
+      const T v = (T)2 * alpha * rb_over_rc * kc;
+      pot += v;
+      if (want_e) es[2] += (double)(v * rho / ((T)2 * alpha));
+    }
+    if (ev.xc) {
+      T eps, vx;
+      pz_lda_ct<T>(rho, eps, vx, want_e);
+      pot += vx;
+      if (want_e) es[3] += (double)(eps * rho);
+    }
+    if (ev.hartree) {
+      const cpx<T> zz = res[sw<T, NP>(ev.slot_h * RP + pr, j)];
+      const T vh = odd ? zz.y : zz.x;
+      pot += vh;
+      if (want_e) es[4] += 0.5 * (double)vh * (double)rho;
+    }
+    if (ev.pp) {
+      const T vl = __ldg(vlocp + gidx);
+      pot += vl;
+      if (want_e) es[5] += (double)vl * (double)rho;
+    }
+    potp[gidx] = pot;
+  }
+  if (!want_e) return;
+  __shared__ double red[32][6];
+  const int lane32 = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const double v = warp_sum(es[c]);
+    if (lane32 == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  if (tid < 6) {
+    KSum s;
+    s.init();
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int w = 0; w < nw; ++w) s.add(red[w][tid]);
+    a.partials[(int64_t)blockIdx.x * GB_NE + tid] = s.value();
+  }
+}
+
+// ---- columns -------------------------------------------------------------------
+struct CtCols {
+  void* data;
+  int64_t fstride, stride, ostride;
+  int ncols;
+  const void* tw;
+  double scale;
+  GInfo gi;
+  KerDesc kd;
+};
+
+template <typename T, int N, int DIR, bool CONV>
+__global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB) k_ct_cols(CtCols a) {
+  constexpr int TB = ColsCfg<T, N>::TB, TPL = Tpl<N>::value, NP = Pad<T, N>::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
+  cpx<T>* A = tw + N;
+  cpx<T>* B = A + TB * NP;
+  const int tid = threadIdx.x, l = tid / TPL, lane = tid % TPL;
+  const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
+  const int c0 = blockIdx.x * TB;
+  const int nc = min(TB, a.ncols - c0);
+  const int f = blockIdx.z, outer = blockIdx.y;
+  cpx<T>* base = reinterpret_cast<cpx<T>*>(a.data) + f * a.fstride + outer * a.ostride + c0;
+  for (int idx = tid; idx < N * TB; idx += blockDim.x) {
+    const int c = idx % TB, j = idx / TB;
+    A[sw<T, NP>(c, j)] = c < nc ? base[(int64_t)j * a.stride + c] : cpx<T>{(T)0, (T)0};
+  }
+  __syncthreads();
+  cpx<T>* res;
+  if constexpr (!CONV) {
+    res = fft<DIR, T, N>(A, B, tw, l, lane, true);
+  } else {
+    res = fft<-1, T, N>(A, B, tw, l, lane, true);
+    const int type = a.kd.type[f];
+    const T coef = (T)a.kd.coef[f];
+    const void* arr = a.kd.arr[f];
+    for (int idx = tid; idx < N * TB; idx += blockDim.x) {
+      const int c = idx % TB, j = idx / TB;
+      if (c >= nc) continue;
+      const T kv = gbk::kernel_value<T>(a.gi, type, arr, j, outer, c0 + c) * coef;
+      const int p = sw<T, NP>(c, j);
+      res[p] = c_scale(res[p], kv);
+    }
+    __syncthreads();
+    cpx<T>* other = (res == A) ? B : A;
+    res = fft<1, T, N>(res, other, tw, l, lane, true);
+  }
+  const T s = (T)a.scale;
+  for (int idx = tid; idx < N * TB; idx += blockDim.x) {
+    const int c = idx % TB, j = idx / TB;
+    if (c < nc) base[(int64_t)j * a.stride + c] = c_scale(res[sw<T, NP>(c, j)], s);
+  }
+}
+
+// ---- launchers -------------------------------------------------------------------
+// Raise a kernel's dynamic shared-memory limit once to the largest size it
+// has been launched with (keyed by kernel address and device).
+int gb_smem_granted(const void* kern, int dev);
+void gb_smem_grant(const void* kern, int dev, int bytes);
+
+template <typename K> inline int ct_smem(K kern, size_t bytes) {
+  if (bytes <= 48 * 1024) return 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const void* key = reinterpret_cast<const void*>(kern);
+  if (gb_smem_granted(key, dev) >= (int)bytes) return 0;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return gb_set_error(GBOFDFT_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
+  gb_smem_grant(key, dev, (int)bytes);
+  return 0;
+}
+
+template <typename T>
+int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf, const int* ops,
+                double beta, double scale, cudaStream_t st) {
+  int rc = 1;
+  ct_dispatch(p->n[2], [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
+    CtRowsFwd a;
+    a.in = in; a.out = spec; a.fstride = fstride;
+    a.nrows = p->n[0] * p->n[1]; a.ld2 = ld2; a.nf = nf;
+    for (int f = 0; f < GB_MAX_FIELDS; ++f) a.op[f] = f < nf ? ops[f] : OP_RHO;
+    a.beta = beta; a.scale = scale; a.tw = p->tw[2];
+    const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP) + sizeof(T) * 2 * RP * N;
+    if ((rc = ct_smem(k_ct_rows_fwd<T, N>, sm))) return;
+    const int nblk = (a.nrows + 2 * RP - 1) / (2 * RP);
+    k_ct_rows_fwd<T, N><<<nblk, Tpl<N>::value * RP * nf, sm, st>>>(a);
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "ct_rows_fwd: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+template <typename T>
+int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out, int64_t ostride,
+                double scale, const EvalDesc* ev, const void* rho, const void* vloc, void* pot, int calc_e,
+                double* partials, int64_t* nblk_out, cudaStream_t st) {
+  int rc = 1;
+  ct_dispatch(p->n[2], [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
+    CtRowsInv a;
+    memset(&a, 0, sizeof(a));
+    a.in = spec; a.fstride = fstride; a.nrows = p->n[0] * p->n[1]; a.ld2 = ld2; a.nf = nf; a.tw = p->tw[2];
+    a.out = out; a.ostride = ostride; a.scale = scale;
+    const int nblk = (a.nrows + 2 * RP - 1) / (2 * RP);
+    if (nblk_out) *nblk_out = nblk;
+    if (ev) {
+      a.ev = *ev; a.rho = rho; a.vloc = vloc; a.pot = pot; a.calc_e = calc_e; a.partials = partials;
+      const int nfl = nf > 0 ? nf : 1;
+      const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nfl * RP * NP);
+      if ((rc = ct_smem(k_ct_rows_inv_eval<T, N>, sm))) return;
+      k_ct_rows_inv_eval<T, N><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+    } else {
+      const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP);
+      if ((rc = ct_smem(k_ct_rows_inv_store<T, N>, sm))) return;
+      k_ct_rows_inv_store<T, N><<<nblk, Tpl<N>::value * RP * nf, sm, st>>>(a);
+    }
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "ct_rows_inv: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+template <typename T, int DIR, bool CONV>
+int ct_cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, double scale,
+              const KerDesc* kd, cudaStream_t st) {
+  int rc = 1;
+  ct_dispatch(p->n[axis], [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    constexpr int TB = ColsCfg<T, N>::TB, NP = Pad<T, N>::NP;
+    CtCols a;
+    memset(&a, 0, sizeof(a));
+    a.data = spec; a.fstride = fstride;
+    a.stride = axis == 1 ? ld2 : (int64_t)p->n[1] * ld2;
+    a.ostride = axis == 1 ? (int64_t)p->n[1] * ld2 : ld2;
+    a.ncols = p->n2h; a.tw = p->tw[axis]; a.scale = scale;
+    a.gi = p->gi;
+    if (kd) a.kd = *kd;
+    const size_t sm = sizeof(cpx<T>) * (N + 2 * TB * NP);
+    if ((rc = ct_smem(k_ct_cols<T, N, DIR, CONV>, sm))) return;
+    dim3 grid((p->n2h + TB - 1) / TB, p->n[axis == 1 ? 0 : 1], nf);
+    k_ct_cols<T, N, DIR, CONV><<<grid, Tpl<N>::value * TB, sm, st>>>(a);
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "ct_cols: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+}  // namespace gbct
+
+// Instantiate the launchers of one precision (one translation unit each).
+#define GB_CT_DEFINE(T, SUF)                                                                                    \
+  int gb_ct_rows_fwd_##SUF(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf,      \
+                           const int* ops, double beta, double scale, cudaStream_t st) {                      \
+    return gbct::ct_rows_fwd<T>(p, in, spec, fstride, ld2, nf, ops, beta, scale, st);                          \
+  }                                                                                                            \
+  int gb_ct_rows_inv_##SUF(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out,     \
+                           int64_t ostride, double scale, const EvalDesc* ev, const void* rho, const void* vloc, \
+                           void* pot, int calc_e, double* partials, int64_t* nblk, cudaStream_t st) {           \
+    return gbct::ct_rows_inv<T>(p, spec, fstride, ld2, nf, out, ostride, scale, ev, rho, vloc, pot, calc_e,      \
+                                partials, nblk, st);                                                            \
+  }                                                                                                            \
+  int gb_ct_cols_##SUF(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, int dir,        \
+                       double scale, const KerDesc* kd, cudaStream_t st) {                                      \
+    if (kd) return gbct::ct_cols_t<T, -1, true>(p, spec, fstride, ld2, nf, axis, scale, kd, st);               \
+    return dir < 0 ? gbct::ct_cols_t<T, -1, false>(p, spec, fstride, ld2, nf, axis, scale, nullptr, st)         \
+                   : gbct::ct_cols_t<T, 1, false>(p, spec, fstride, ld2, nf, axis, scale, nullptr, st);         \
+  }

@@ -1,0 +1,4 @@
+// FP32 instantiations of the compile-time-size passes.
+#include "passes_ct.cuh"
+
+GB_CT_DEFINE(float, f32)

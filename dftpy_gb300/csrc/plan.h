@@ -62,5 +62,18 @@ int gb_cols(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int a
             double scale, cudaStream_t st);
 int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, const KerDesc& kd,
                  double scale, cudaStream_t st);
+// compile-time-size passes (passes_ct_*.cu): return 1 when the size has no
+// specialisation, 0 on success, an error code otherwise
+int gb_ct_rows_fwd_f32(gbofdft_plan*, const void*, void*, int64_t, int, int, const int*, double, double, cudaStream_t);
+int gb_ct_rows_fwd_f64(gbofdft_plan*, const void*, void*, int64_t, int, int, const int*, double, double, cudaStream_t);
+int gb_ct_rows_inv_f32(gbofdft_plan*, const void*, int64_t, int, int, void*, int64_t, double, const EvalDesc*,
+                       const void*, const void*, void*, int, double*, int64_t*, cudaStream_t);
+int gb_ct_rows_inv_f64(gbofdft_plan*, const void*, int64_t, int, int, void*, int64_t, double, const EvalDesc*,
+                       const void*, const void*, void*, int, double*, int64_t*, cudaStream_t);
+int gb_ct_cols_f32(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
+int gb_ct_cols_f64(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
+void gb_count_launch();
+int gb_use_ct();  // 0 forces the generic passes (GBOFDFT_GENERIC_FFT=1)
+
 int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,
                        cudaStream_t st);

@@ -38,6 +38,7 @@ DEFAULTS = {
     "eps": None,
     "fp32_econv": None,
     "fp32_eps": -1.0e-3,
+    "refine_maxls": 10,
 }
 
 
@@ -72,7 +73,7 @@ class Optimization:
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
-    def _run(self, rho, econv, eps, maxiter):
+    def _run(self, rho, econv, eps, maxiter, maxls=None):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -82,7 +83,7 @@ class Optimization:
         opts.econv = float(econv)
         opts.maxfun = int(o["maxfun"])
         opts.maxiter = int(maxiter)
-        opts.maxls = int(o["maxls"])
+        opts.maxls = int(o["maxls"] if maxls is None else maxls)
         opts.c1, opts.c2, opts.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
         opts.ncheck = int(o["ncheck"])
         opts.eps = float(eps)
@@ -101,7 +102,7 @@ class Optimization:
                                          _lib.stream_ptr()), "optimize_tn")
         out = dict(energy=res.energy, mu=res.mu, converged=res.converged, n_iter=res.n_iter,
                    n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, energies=list(res.energies),
-                   history=[hist[i] for i in range(res.n_history)])
+                   history=[hist[i] for i in range(res.n_history)], n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total)
         return DirectField(grid, data=r), out
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):
@@ -125,7 +126,11 @@ class Optimization:
             r, out = self._run(rho.to(dt) if rho.dtype != dt else rho, o["econv"], eps, o["maxiter"])
             self.stats["stages"].append(dict(precision=prec, **out))
         elif prec == "mixed":
-            e32 = o["fp32_econv"] if o["fp32_econv"] is not None else o["econv"]
+            # FP32 until its energy changes by less than fp32_econv (default:
+            # the 1e-5 eV/atom accuracy gate, 3.67e-7 Ha/atom) or its line
+            # search stops resolving progress
+            nat = self._natoms()
+            e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
@@ -135,8 +140,15 @@ class Optimization:
             n_in = float(rho.as_subclass(torch.Tensor).to(torch.float64).sum())
             n_out = float(r64.as_subclass(torch.Tensor).sum())
             r64 = r64 * (n_in / n_out)
-            r, out = self._run(r64, o["econv"], eps, o["maxiter"])
+            r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"])
             self.stats["stages"].append(dict(precision="fp64", **out))
+            # a refinement whose line search stops on FP64 rounding (no energy
+            # change above econv along the last direction) sits at the FP64
+            # minimum: report it converged
+            h = out["history"]
+            if out["converged"] == 1 and len(h) >= 1 and abs(h[-1] - h[0]) <= max(o["econv"], 1e-12 * abs(h[0])) \
+                    and out["n_iter"] <= 2:
+                out = dict(out, converged=0)
         else:
             raise ValueError("precision must be 'fp64', 'fp32' or 'mixed', got %r" % (prec,))
         self.converged = out["converged"]
@@ -146,6 +158,12 @@ class Optimization:
         self.rho = r
         self._functional = None
         return r
+
+    def _natoms(self):
+        for f in self.EnergyEvaluator.funcDict.values():
+            if getattr(f, "type", None) == "PSEUDO":
+                return f.ions.nat
+        return 1
 
     @property
     def functional(self):

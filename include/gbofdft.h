@@ -205,6 +205,9 @@ typedef struct gbofdft_tn_result {
   double* history;        /* optional host array receiving the energy history */
   int history_cap;
   int n_history;
+  int n_sync;             /* host synchronisations performed */
+  double t_sync;          /* host seconds spent waiting in them (scalar read-backs) */
+  double t_total;         /* host seconds in gbofdft_optimize_tn */
 } gbofdft_tn_result;
 
 int gbofdft_tn_options_default(gbofdft_tn_options* opts);

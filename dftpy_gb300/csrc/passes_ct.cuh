@@ -379,9 +379,6 @@ __global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB) k_ct_cols(C
 // ---- launchers -------------------------------------------------------------------
 // Raise a kernel's dynamic shared-memory limit once to the largest size it
 // has been launched with (keyed by kernel address and device).
-int gb_smem_granted(const void* kern, int dev);
-void gb_smem_grant(const void* kern, int dev, int bytes);
-
 template <typename K> inline int ct_smem(K kern, size_t bytes) {
   if (bytes <= 48 * 1024) return 0;
   int dev = 0;

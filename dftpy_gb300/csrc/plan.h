@@ -73,6 +73,8 @@ int gb_ct_rows_inv_f64(gbofdft_plan*, const void*, int64_t, int, int, void*, int
 int gb_ct_cols_f32(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
 int gb_ct_cols_f64(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
 void gb_count_launch();
+int gb_smem_granted(const void* kern, int dev);
+void gb_smem_grant(const void* kern, int dev, int bytes);
 int gb_use_ct();  // 0 forces the generic passes (GBOFDFT_GENERIC_FFT=1)
 
 int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,

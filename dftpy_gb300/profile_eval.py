@@ -18,6 +18,8 @@ def main():
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--workload", default="al256", choices=["al256", "al4"])
+    p.add_argument("--solve", default=None, choices=["mixed", "fp64", "fp32"],
+                   help="instead of single evaluations, run whole TN solves (NVTX range 'solve')")
     a = p.parse_args()
     import torch
     from . import _lib, systems
@@ -32,6 +34,33 @@ def main():
     total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="WT"),
                               XCFunctional=F.Functional(type="XC", name="LDA"),
                               HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    if a.solve:
+        from .optimization import Optimization
+        rho0 = DirectField(grid)
+        rho0[:] = st.nelec / st.volume
+
+        def run():
+            o = Optimization(EnergyEvaluator=total, optimization_method="TN",
+                             optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100,
+                                                   "precision": a.solve})
+            o.optimize_rho(guess_rho=rho0)
+            return o
+        for _ in range(a.warmup):
+            run()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("solve")
+        e0.record()
+        for _ in range(a.reps):
+            o = run()
+        e1.record()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        print("solve %s %s: %.2f ms per solve, E=%.10f, stages %s" % (
+            a.workload, a.solve, e0.elapsed_time(e1) / a.reps, o.energy,
+            [(s["precision"], s["n_eval_ev"], s["n_eval_v"]) for s in o.stats["stages"]]))
+        return 0
     dt = torch.float32 if a.precision == "fp32" else torch.float64
     g = torch.Generator(device="cuda").manual_seed(0)
     base = st.nelec / st.volume

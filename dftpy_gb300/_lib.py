@@ -73,6 +73,9 @@ _SIGS = [
     ("gbofdft_fft_r2c", ctypes.c_int, [_P, _P, _P, _P]),
     ("gbofdft_fft_c2r", ctypes.c_int, [_P, _P, _P, _P]),
     ("gbofdft_convolve", ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P, ctypes.c_double, _P]),
+    ("gbofdft_convolve_noalloc", ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                                ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P,
+                                                ctypes.c_double, _P]),
     ("gbofdft_eval", ctypes.c_int, [_P, _P, ctypes.POINTER(Functional), _P, _P, ctypes.c_int, _P]),
     ("gbofdft_wt_kernel", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _P, _P]),

@@ -100,6 +100,23 @@ enum gbofdft_kernel { GBOFDFT_KER_NONE = 0, GBOFDFT_KER_HARTREE = 1, GBOFDFT_KER
 int gbofdft_convolve(gbofdft_plan* plan, const void* in, void* out, int kernel, const void* kernel_array,
                      double coef, void* stream);
 
+/*
+ * Allocation-free variant of gbofdft_convolve, for callers that cannot
+ * allocate device memory (code running under another framework's allocator,
+ * or code that must avoid the implicit synchronisation of cudaMalloc /
+ * cudaFree).  No counterpart in the reference: it exists for those callers.
+ * Takes the grid directly (no plan: creating one allocates) and keeps its
+ * scratch -- twiddle tables and one spectrum -- in a fixed 16 MiB device
+ * array inside the library (held by every GPU that loads it, until exit).
+ * Grids whose scratch does not fit are rejected (GBOFDFT_ERR_UNSUPPORTED),
+ * e.g. 96^3 fits in FP64, 128^3 in FP32 only.  All calls share the array:
+ * calls that overlap on the GPU race; serialise them.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress): make it before any
+ * stream capture.  Same arguments and result as gbofdft_convolve otherwise.
+ */
+int gbofdft_convolve_noalloc(const int nr[3], const double lattice[9], int precision, int full, const void* in,
+                             void* out, int kernel, const void* kernel_array, double coef, void* stream);
+
 /* Functional composition for gbofdft_eval (TotalFunctional of
  * KEDF(TF/vW/WT) + XC(LDA) + HARTREE + PSEUDO). */
 typedef struct gbofdft_functional {

@@ -153,7 +153,7 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
     for _ in range(warmup):
         solve(total, rho0, precision)
     torch.cuda.synchronize()
-    times, energies, evals = [], [], []
+    times, energies, evals, glue = [], [], [], []
     l0 = _lib.launch_count()
     for _ in range(steps):
         flush.zero_()                      # 512 MB write: evicts L2 between steps
@@ -170,12 +170,14 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1000.0)
         energies.append(opt.energy)
+        glue.append(opt.stats.get("t_glue", 0.0))
         evals.append([{"precision": st["precision"], "n_eval_ev": st["n_eval_ev"], "n_eval_v": st["n_eval_v"],
                        "converged": st["converged"], "n_iter": st["n_iter"], "n_sync": st["n_sync"],
                        "t_sync_s": round(st["t_sync"], 4), "t_host_s": round(st["t_total"], 4),
                        "last_dE": [round(e - st["history"][-1], 12) for e in st["history"][-5:]]}
                       for st in opt.stats["stages"]])
     launches = _lib.launch_count() - l0
+    evals[-1].append({"python_glue_s": round(glue[-1], 4)})
     return times, energies, evals, launches
 
 

@@ -86,28 +86,36 @@ __device__ __forceinline__ void reduce_finalize(KSum (&acc)[NV], double* partial
   }
 }
 
-// f(i, double* contributions[NV]) for i in [0, n)
-template <int NV, typename F>
+// f(i, ACC* contributions[NV]) for i in [0, n).  Each thread accumulates its
+// elements in the field precision ACC (a handful per thread); the per-thread
+// sums are combined in FP64 (compensated at the CTA and grid level).
+template <int NV, typename ACC, typename F>
 __global__ void __launch_bounds__(kRedThreads) k_map_reduce(int64_t n, F f, double* partials, double* out,
                                                            unsigned* counter) {
-  KSum acc[NV > 0 ? NV : 1];
+  constexpr int NA = NV > 0 ? NV : 1;
+  ACC acc[NA];
 #pragma unroll
-  for (int k = 0; k < (NV > 0 ? NV : 1); ++k) acc[k].init();
+  for (int k = 0; k < NA; ++k) acc[k] = (ACC)0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double c[NV > 0 ? NV : 1];
+    ACC c[NA];
     f(i, c);
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k].add(c[k]);
+    for (int k = 0; k < NV; ++k) acc[k] += c[k];
   }
-  if constexpr (NV > 0) reduce_finalize<NV>(acc, partials, out, counter);
+  if constexpr (NV > 0) {
+    KSum ks[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { ks[k].init(); ks[k].add((double)acc[k]); }
+    reduce_finalize<NV>(ks, partials, out, counter);
+  }
 }
 
-template <int NV, typename F>
+template <int NV, typename ACC, typename F>
 int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st) {
   int nb = (int)((n + kRedThreads * 4 - 1) / (kRedThreads * 4));
   if (nb > kRedBlocks) nb = kRedBlocks;
   if (nb < 1) nb = 1;
-  k_map_reduce<NV><<<nb, kRedThreads, 0, st>>>(n, f, w.partials, w.sc + slot, w.counter);
+  k_map_reduce<NV, ACC><<<nb, kRedThreads, 0, st>>>(n, f, w.partials, w.sc + slot, w.counter);
   GB_CHECK_LAUNCH();
   return 0;
 }
@@ -159,18 +167,18 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   // ---- initial phi (optimization.py:305-316) --------------------------------
   {
     T* phi = F<T>(s, F_PHI);
-    rc = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+    rc = launch_mr<2, T>(w, N, [=] __device__(int64_t i, T* c) {
       const T r = rio[i];
       const T ph = r > (T)0 ? sqrt(r) : (sizeof(T) == 8 ? (T)1e-300 : (T)1e-30);
       phi[i] = ph;
-      c[0] = (double)r;
-      c[1] = (double)ph * (double)ph;
+      c[0] = r;
+      c[1] = ph * ph;
     }, S_A, st);
     if (rc) return rc;
     if ((rc = ts_sync(s))) return rc;
     const T fac = (T)sqrt(s.host[S_A] / s.host[S_B]);
     T* rho = F<T>(s, F_RHO);
-    rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+    rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) {
       const T ph = phi[i] * fac;
       phi[i] = ph;
       rho[i] = ph * ph;
@@ -183,12 +191,12 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     T* phi = F<T>(s, F_PHI);
     T* pot = F<T>(s, F_POT);
     T* rho = F<T>(s, F_RHO);
-    int r = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+    int r = launch_mr<2, T>(w, N, [=] __device__(int64_t i, T* c) {
       const T ph = phi[i];
       const T rr = ph * ph;
       rho[i] = rr;
-      c[0] = (double)pot[i] * (double)rr;
-      c[1] = (double)rr;
+      c[0] = pot[i] * rr;
+      c[1] = rr;
     }, S_A, st);
     if (r) return r;
     if ((r = ts_sync(s))) return r;
@@ -196,10 +204,10 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     mu = (s.host[S_A] * dV) / (s.host[S_B] * dV);
     const T muT = (T)mu;
     T* res0 = F<T>(s, F_RES0);
-    r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+    r = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
       const T v = (pot[i] - muT) * phi[i];
       res0[i] = v;
-      c[0] = (double)v * (double)v;
+      c[0] = v * v;
     }, S_C, st);
     resN = 0.0;
     return r;
@@ -232,13 +240,13 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       T* cgp = F<T>(s, F_CGP);
       T* dir = F<T>(s, F_DIR);
       T* phic = F<T>(s, F_PHI);
-      rc = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
+      rc = launch_mr<2, T>(w, N, [=] __device__(int64_t i, T* c) {
         const T r = -res0[i];
         cgr[i] = r;
         cgp[i] = r;
         dir[i] = (T)0;
-        c[0] = (double)r * (double)r;
-        c[1] = (double)phic[i] * (double)phic[i];
+        c[0] = r * r;
+        c[1] = phic[i] * phic[i];
       }, S_A, st);
       if (rc) return rc;
       if ((rc = ts_sync(s))) return rc;
@@ -257,7 +265,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
         T* rho1 = F<T>(s, F_TMP);
         const T eT = (T)epsi, bT = (T)beta;
         const bool first = (j == 0);
-        rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+        rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) {
           T pv = cgp[i];
           if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
           const T p1 = phi[i] + eT * pv;
@@ -270,22 +278,22 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
         T* ap = F<T>(s, F_AP);
         const T muT = (T)mu;
         const T inv_e = (T)(1.0 / epsi);
-        rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+        rc = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
           const T a = ((pot1[i] - muT) * phi1[i] - res0[i]) * inv_e;
           ap[i] = a;
-          c[0] = (double)cgp[i] * (double)a;
+          c[0] = cgp[i] * a;
         }, S_PAP, st);
         if (rc) return rc;
         const double* scd = w.sc;
         const double r0c = r0Norm;
-        rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+        rc = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
           const double pap = scd[S_PAP];
-          if (pap < 0.0) { c[0] = 0.0; return; }
+          if (pap < 0.0) { c[0] = (T)0; return; }
           const T alpha = (T)(r0c / pap);
           dir[i] += alpha * cgp[i];
           const T r = cgr[i] - alpha * ap[i];
           cgr[i] = r;
-          c[0] = (double)r * (double)r;
+          c[0] = r * r;
         }, S_R1, st);
         if (rc) return rc;
         if ((rc = ts_sync(s))) return rc;
@@ -294,7 +302,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
           if (j == 0) {
             // direction = r0Norm / pAp * p
             const T sc = (T)(r0Norm / pAp);
-            rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { dir[i] = sc * cgp[i]; }, S_A, st);
+            rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) { dir[i] = sc * cgp[i]; }, S_A, st);
             if (rc) return rc;
           }
           break;
@@ -323,28 +331,28 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       T* phi = F<T>(s, F_PHI);
       T* p = F<T>(s, F_P);
       T* pot = F<T>(s, F_POT);
-      int r = launch_mr<2>(w, N, [=] __device__(int64_t i, double* c) {
-        c[0] = (double)phi[i] * (double)phi[i];
-        c[1] = (double)p[i] * (double)phi[i];
+      int r = launch_mr<2, T>(w, N, [=] __device__(int64_t i, T* c) {
+        c[0] = phi[i] * phi[i];
+        c[1] = p[i] * phi[i];
       }, S_A, st);
       if (r) return r;
       if ((r = ts_sync(s))) return r;
       const double Ne = s.host[S_A] * dV;
       const T fac = (T)(s.host[S_B] * dV / Ne);
-      r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+      r = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
         const T v = p[i] - fac * phi[i];
         p[i] = v;
-        c[0] = (double)v * (double)v;
+        c[0] = v * v;
       }, S_C, st);
       if (r) return r;
       if ((r = ts_sync(s))) return r;
       const double pNorm = s.host[S_C] * dV;
       theta0 = sqrt(pNorm / Ne);
       const T sc = (T)sqrt(Ne / pNorm);
-      r = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+      r = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
         const T v = p[i] * sc;
         p[i] = v;
-        c[0] = (double)pot[i] * (double)phi[i] * (double)v;
+        c[0] = pot[i] * phi[i] * v;
       }, S_D, st);
       if (r) return r;
       if ((r = ts_sync(s))) return r;
@@ -355,7 +363,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     if (d0 * 2.0 > 0.0) {  // "Change to steepest descent" (optimization.py:371-380)
       T* p = F<T>(s, F_P);
       T* res0 = F<T>(s, F_RES0);
-      rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { p[i] = -res0[i]; }, S_A, st);
+      rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) { p[i] = -res0[i]; }, S_A, st);
       if (rc) return rc;
       if ((rc = orthonormalize())) return rc;
     }
@@ -375,7 +383,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       T* phi1 = F<T>(s, F_PHI1);
       T* rho1 = F<T>(s, F_TMP);
       const T ct = (T)cos(stp), sn = (T)sin(stp);
-      rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) {
+      rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) {
         const T v = phi[i] * ct + p[i] * sn;
         phi1[i] = v;
         rho1[i] = v * v;
@@ -383,9 +391,9 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       if (rc) return rc;
       T* pot1 = F<T>(s, F_POT1);
       if ((rc = ts_eval(s, rho1, pot1, true))) return rc;
-      rc = launch_mr<1>(w, N, [=] __device__(int64_t i, double* c) {
+      rc = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
         const T p2 = p[i] * ct - phi[i] * sn;
-        c[0] = (double)pot1[i] * (double)phi1[i] * (double)p2;
+        c[0] = pot1[i] * phi1[i] * p2;
       }, S_A, st);
       if (rc) return rc;
       if ((rc = ts_sync(s))) return rc;
@@ -415,7 +423,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   // final density = phi^2
   {
     T* phi = F<T>(s, F_PHI);
-    rc = launch_mr<0>(w, N, [=] __device__(int64_t i, double* c) { rio[i] = phi[i] * phi[i]; }, S_A, st);
+    rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) { rio[i] = phi[i] * phi[i]; }, S_A, st);
     if (rc) return rc;
     if ((rc = ts_sync(s))) return rc;
   }

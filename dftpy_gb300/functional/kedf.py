@@ -30,6 +30,7 @@ class KEDF(AbstractFunctional):
         self.options["kedf"] = self.name
         # kernel cache, as the reference's ke_kernel_saved (kedf/__init__.py:96-106)
         self.ke_kernel_saved = {"Kernel": None, "rho0": 0.0, "shape": None, "dtype": None}
+        self._kernels_by_dtype = {}
         self.energies = {}
 
     @property
@@ -42,16 +43,18 @@ class KEDF(AbstractFunctional):
         rho0 = self.options.get("rho0", None)
         if not rho0:
             rho0 = float(rho.as_subclass(torch.Tensor).to(torch.float64).mean())
-        s = self.ke_kernel_saved
+        s = self._kernels_by_dtype.setdefault(rho.dtype, {"Kernel": None, "rho0": 0.0, "shape": None,
+                                                          "dtype": rho.dtype})
+        self.ke_kernel_saved = s
         shape = tuple(rho.shape)
-        if abs(s["rho0"] - rho0) > 1e-6 or s["shape"] != shape or s["dtype"] != rho.dtype:
+        if abs(s["rho0"] - rho0) > 1e-6 or s["shape"] != shape:
             g = rho.grid
             plan = g.plan(rho.dtype)
             k = torch.empty((int(g.nrR[0]), int(g.nrR[1]), int(g.nrR[2]) // 2 + 1), dtype=rho.dtype, device="cuda")
             _lib.check(_lib.load().gbofdft_wt_kernel(
                 plan.handle, float(rho0), float(self.options.get("x", 1.0)), float(self.alpha),
                 float(self.beta), _lib.ptr(k), _lib.stream_ptr()), "wt_kernel")
-            s.update(Kernel=k, rho0=rho0, shape=shape, dtype=rho.dtype)
+            s.update(Kernel=k, rho0=rho0, shape=shape)
         return s["Kernel"]
 
     @property

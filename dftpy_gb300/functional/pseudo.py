@@ -107,7 +107,7 @@ class LocalPseudo(AbstractFunctional):
                 raise ValueError("There is no pseudopotential for {:4s} atom".format(key))
         self.ions.set_charges(self.zval)
         self._vreal = {}
-        self._v = None
+        self._vG = None
         self.ewald = None
 
     def _device_inputs(self):
@@ -118,7 +118,7 @@ class LocalPseudo(AbstractFunctional):
 
     def local_PP(self):
         """v_loc(G) and v_loc(r) in FP64 (``local_PP``, ``:237-246``)."""
-        if self._v is not None:
+        if getattr(self, "_vG", None) is not None:
             return
         g = self.grid
         plan = g.plan(torch.float64)

@@ -12,6 +12,7 @@ the FP32 energy stops resolving progress, then FP64 iterations from that
 density to the requested ``econv``).  Reductions are FP64 in every mode.
 """
 import ctypes
+import time
 
 import numpy as np
 import torch
@@ -120,6 +121,7 @@ class Optimization:
             raise TypeError("guess_rho must be a DirectField")
         prec = o["precision"] or ("fp64" if rho.dtype == torch.float64 else "fp32")
         self.stats = {"stages": []}
+        t_start = time.perf_counter()
         if prec in ("fp64", "fp32"):
             dt = torch.float64 if prec == "fp64" else torch.float32
             eps = o["eps"] if o["eps"] is not None else (1e-9 if dt == torch.float64 else o["fp32_eps"])
@@ -151,6 +153,8 @@ class Optimization:
                 out = dict(out, converged=0)
         else:
             raise ValueError("precision must be 'fp64', 'fp32' or 'mixed', got %r" % (prec,))
+        self.stats["t_wall"] = time.perf_counter() - t_start
+        self.stats["t_glue"] = self.stats["t_wall"] - sum(st["t_total"] for st in self.stats["stages"])
         self.converged = out["converged"]
         self.mu = out["mu"]
         self.energy = out["energy"]

@@ -23,6 +23,17 @@ class GbofdftError(RuntimeError):
     pass
 
 
+class Lwt(ctypes.Structure):
+    """Mirror of ``gbofdft_lwt``."""
+    _fields_ = [("interp", ctypes.c_int), ("kdd", ctypes.c_int), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("ratio", ctypes.c_double), ("ldw", ctypes.c_double),
+                ("etamax", ctypes.c_double), ("neta", ctypes.c_int), ("ktab_c", ctypes.c_void_p),
+                ("ktab_end", ctypes.c_double), ("dtab_c", ctypes.c_void_p), ("dtab_end", ctypes.c_double),
+                ("kfmin_opt", ctypes.c_double), ("kfmax_opt", ctypes.c_double),
+                ("kfmin_state", ctypes.c_double), ("kfmax_state", ctypes.c_double),
+                ("work", ctypes.c_void_p), ("work_bytes", ctypes.c_int64), ("nknots", ctypes.c_int)]
+
+
 class Functional(ctypes.Structure):
     """Mirror of ``gbofdft_functional``."""
     _fields_ = [
@@ -31,7 +42,7 @@ class Functional(ctypes.Structure):
         ("wt", ctypes.c_int), ("wt_alpha", ctypes.c_double), ("wt_beta", ctypes.c_double),
         ("wt_kernel", ctypes.c_void_p),
         ("xc", ctypes.c_int), ("hartree", ctypes.c_int),
-        ("vloc", ctypes.c_void_p), ("e_ion", ctypes.c_double),
+        ("vloc", ctypes.c_void_p), ("e_ion", ctypes.c_double), ("lwt", ctypes.POINTER(Lwt)),
     ]
 
 
@@ -79,6 +90,8 @@ _SIGS = [
     ("gbofdft_eval", ctypes.c_int, [_P, _P, ctypes.POINTER(Functional), _P, _P, ctypes.c_int, _P]),
     ("gbofdft_wt_kernel", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _P, _P]),
+    ("gbofdft_lwt_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_mgp_table", ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, _P, _P]),
     ("gbofdft_setup_workspace_bytes", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_vloc", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P, ctypes.c_int,
                                     ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P, _P]),

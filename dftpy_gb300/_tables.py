@@ -99,3 +99,46 @@ def pme_bm(nr, order=10):
             den += Mn[k] * np.exp(-1j * k * q)
         out.append(num / den)
     return np.concatenate(out).astype(np.complex128)
+
+
+# inverse Lindhard function, large-eta series coefficients in 1/eta^2
+# (kedf/kernel.py:72-136)
+_LIND_LARGE = (-0.13714285714285712, -6.39999999999999875e-2, -3.77825602968460128e-2,
+               -2.51824061652633074e-2, -1.80879839616166146e-2, -1.36715733124818332e-2,
+               -1.07236045520990083e-2, -8.65192783339199453e-3, -7.1372762502456763e-3,
+               -5.9945117538835746e-3, -5.10997527675418131e-3, -4.41060829979912465e-3,
+               -3.84763737842981233e-3, -3.38745061493813488e-3, -3.00624946457977689e-3)
+
+
+def lindhard(eta, lbda, mu, tol=1e-10):
+    """Inverse Lindhard function on a 1-D table (``kernel.py:14-136``), the
+    same branches as the device evaluation of the WT kernel."""
+    eta = np.asarray(eta, float)
+    out = eta.copy()
+    tol2 = tol / 10
+    c0 = (eta > tol2) & (np.abs(eta - 1.0) > tol2)
+    e = eta[c0]
+    out[c0] = 1.0 / (0.5 + 0.25 * (1.0 - e ** 2) * np.log((1.0 + e) / np.abs(1.0 - e)) / e) - 3.0 * mu * e ** 2 - lbda
+    c1 = eta < tol
+    e = eta[c1]
+    out[c1] = 1.0 - lbda + e ** 2 * (1.0 / 3.0 - 3.0 * mu)
+    c2 = np.abs(eta - 1.0) < tol
+    e = eta[c2]
+    out[c2] = 2.0 - lbda - 3.0 * mu + 20.0 * (e - 1.0)
+    c3 = eta > 3.65
+    e = eta[c3]
+    inv = 1.0 / e ** 2
+    s = _LIND_LARGE[-1]
+    for c in _LIND_LARGE[-2::-1]:
+        s = c + inv * s
+    out[c3] = 3.0 * (1.0 - mu) * e ** 2 - lbda - 0.6 + inv * s
+    return out
+
+
+def spline_values_deriv(x, c):
+    """First derivative of a ``spline_notaknot`` spline at its knots."""
+    d = np.empty(x.size)
+    d[:-1] = c[:, 1]
+    h = x[-1] - x[-2]
+    d[-1] = c[-1, 1] + h * (2.0 * c[-1, 2] + 3.0 * h * c[-1, 3])
+    return d

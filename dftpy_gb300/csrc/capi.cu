@@ -270,6 +270,9 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
   }
   if (!rc)
     rc = gb_rows_inv_eval(p, p->spec, fs, nf, ev, rho, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
+  if (!rc && f->lwt)
+    rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
+                     st);
   return rc;
 }
 

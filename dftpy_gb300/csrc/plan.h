@@ -77,5 +77,8 @@ int gb_smem_granted(const void* kern, int dev);
 void gb_smem_grant(const void* kern, int dev, int bytes);
 int gb_use_ct();  // 0 forces the generic passes (GBOFDFT_GENERIC_FFT=1)
 
+int gb_lwt_eval(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double* energies, int calc_v,
+                int calc_e, cudaStream_t st);
+
 int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,
                        cudaStream_t st);

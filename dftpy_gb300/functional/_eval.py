@@ -1,4 +1,6 @@
 """One call of ``gbofdft_eval`` for a set of functional components."""
+import ctypes
+
 import torch
 
 from .. import _lib
@@ -21,9 +23,10 @@ class Spec:
         self.hartree = False
         self.vloc = None
         self.e_ion = 0.0
+        self.lwt = None           # LWTTerm descriptor (gbofdft_lwt)
 
     def merge(self, other):
-        for k in ("tf", "vw", "wt", "hartree"):
+        for k in ("tf", "vw", "wt", "hartree", "lwt"):
             if getattr(self, k) and getattr(other, k):
                 raise ValueError("functional component %s given twice" % k)
         if self.xc and other.xc:
@@ -46,6 +49,8 @@ class Spec:
             out.xc = other.xc
         if other.vloc is not None:
             out.vloc = other.vloc
+        if other.lwt is not None:
+            out.lwt = other.lwt
         out.e_ion = self.e_ion + other.e_ion
         return out
 
@@ -58,6 +63,8 @@ class Spec:
         f.xc, f.hartree = int(self.xc), int(self.hartree)
         f.vloc = self.vloc.data_ptr() if self.vloc is not None else None
         f.e_ion = float(self.e_ion)
+        if self.lwt is not None:
+            f.lwt = ctypes.pointer(self.lwt)
         return f
 
 

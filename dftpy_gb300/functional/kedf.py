@@ -10,6 +10,10 @@ from .output import AbstractFunctional, FunctionalOutput
 from ._eval import Spec, evaluate
 
 KEDF_PARTS = {
+    "LMGP": ("TF", "VW", "LWT"),
+    "LMGP-NL": ("LWT",),
+    "LWT": ("TF", "VW", "LWT"),
+    "LWT-NL": ("LWT",),
     "TF": ("TF",),
     "VW": ("VW",),
     "TFVW": ("TF", "VW"),
@@ -32,6 +36,12 @@ class KEDF(AbstractFunctional):
         self.ke_kernel_saved = {"Kernel": None, "rho0": 0.0, "shape": None, "dtype": None}
         self._kernels_by_dtype = {}
         self.energies = {}
+        self._lwt = None
+        if "LWT" in KEDF_PARTS[self.name]:
+            from .lwt import LWTTerm
+            kt = "MGP" if self.name.startswith("LMGP") else "WT"
+            opts = {k: v for k, v in self.options.items() if k not in ("kedf", "y", "sigma")}
+            self._lwt = LWTTerm(kerneltype=kt, **opts)
 
     @property
     def parts(self):
@@ -79,6 +89,8 @@ class KEDF(AbstractFunctional):
                 raise NotImplementedError("WT with alpha != beta is not part of this path")
             sp.wt, sp.wt_alpha, sp.wt_beta = True, float(self.alpha), float(self.beta)
             sp.wt_kernel = self._wt_kernel(rho)
+        if "LWT" in parts:
+            sp.lwt = self._lwt.prepare(rho)
         return sp
 
     def compute(self, density, calcType={"E", "V"}, split=False, **kwargs):
@@ -87,7 +99,7 @@ class KEDF(AbstractFunctional):
         if en is not None:
             if split:
                 res = {}
-                for p, slot in (("TF", _lib.E_TF), ("VW", _lib.E_VW), ("WT", _lib.E_NL)):
+                for p, slot in (("TF", _lib.E_TF), ("VW", _lib.E_VW), ("WT", _lib.E_NL), ("LWT", _lib.E_NL)):
                     if p in self.parts:
                         res[p if p != "WT" else "NL"] = FunctionalOutput(name=p, energy=float(en[slot]))
                         self.energies[p] = float(en[slot])

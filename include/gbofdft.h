@@ -117,8 +117,45 @@ int gbofdft_convolve(gbofdft_plan* plan, const void* in, void* out, int kernel, 
 int gbofdft_convolve_noalloc(const int nr[3], const double lattice[9], int precision, int full, const void* in,
                              void* out, int kernel, const void* kernel_array, double coef, void* stream);
 
+/*
+ * LWT / LMGP nonlocal kinetic term (kedf/lwt.py:82-341 LWTPotentialEnergy):
+ * kernel K(q / k_F(r)) interpolated between k_F knots k_min ratio^i.  The
+ * kernel tables are cubic splines on the uniform grid eta_j = j etamax /
+ * (neta - 1): ktab_c (neta-1 pieces x 4 coefficients, device) of K(eta) and
+ * dtab_c of K'(eta) (-eta) (lwt.py:553-561), with their values at etamax.
+ * kfmin_state / kfmax_state carry the automatic k_F bounds across calls
+ * (guess_kf_bound, lwt.py:36-79); set them <= 0 for a fresh start.
+ */
+typedef struct gbofdft_lwt {
+  int interp;              /* 0 linear, 1 hermite */
+  int kdd;                 /* 1..3 (the reference's default 3) */
+  double alpha, beta, ratio, ldw;
+  double etamax;
+  int neta;
+  const double* ktab_c;
+  double ktab_end;
+  const double* dtab_c;
+  double dtab_end;
+  double kfmin_opt, kfmax_opt;     /* fixed bounds (> 0) or automatic (<= 0) */
+  double kfmin_state, kfmax_state; /* automatic bounds carried between calls */
+  void* work;                      /* device workspace, 256-byte aligned */
+  int64_t work_bytes;              /* >= gbofdft_lwt_workspace_bytes */
+  int nknots;                      /* out: knots used by the last call */
+} gbofdft_lwt;
+
+int gbofdft_lwt_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
+
+/*
+ * MGP kernel table (kedf/kernel.py:267-322 MGPKernelTable): table_out[j] =
+ * (4/5) C_TF (5/6) / maxpoints * sum_{i=1..maxpoints} G(eta_j t_i^(-1/3)) t_i^(-1/6),
+ * t_i = i / maxpoints, G the cubic spline (pieces coef, knots gp[0..m-1], end
+ * values beyond) of the inverse Lindhard function.  All pointers device.
+ */
+int gbofdft_mgp_table(const double* gp, const double* coef, int m, const double* eta, int neta, int maxpoints,
+                      double* table_out, void* stream);
+
 /* Functional composition for gbofdft_eval (TotalFunctional of
- * KEDF(TF/vW/WT) + XC(LDA) + HARTREE + PSEUDO). */
+ * KEDF(TF/vW/WT/LWT) + XC(LDA) + HARTREE + PSEUDO). */
 typedef struct gbofdft_functional {
   int tf;                /* Thomas-Fermi, kedf/tf.py:66-80 */
   double tf_x;
@@ -131,6 +168,8 @@ typedef struct gbofdft_functional {
   int hartree;           /* hartree.py:24-45 */
   const void* vloc;      /* real field (local pseudopotential) or NULL, pseudo/__init__.py:219-234 */
   double e_ion;          /* constant ion-ion energy added to the total */
+  gbofdft_lwt* lwt;      /* LWT/LMGP nonlocal term or NULL (its energy goes to the NL slot); the
+                            call reads the density extrema back to the host to place the knots */
 } gbofdft_functional;
 
 /*

@@ -1010,3 +1010,216 @@ def _tn_direction(evaluator, res0, phi, mu, maxfun, dV):
         r0Norm = r1Norm
         p = res + beta * p
     return direction
+
+
+# ----------------------------------------------------------------------------
+# LWT / LMGP: density-dependent kernel by interpolation over k_F knots
+# ----------------------------------------------------------------------------
+def spline_eval_clamped(sp, u):
+    """splev(..., ext=3): values beyond the knot range take the end values."""
+    x, c = sp
+    u = np.asarray(u, float)
+    lo, hi = x[0], x[-1]
+    out = spline_eval(sp, np.clip(u, lo, hi))
+    return out
+
+
+def mgp_kernel_table(eta, maxpoints=1000):
+    """``MGPKernelTable`` (``kedf/kernel.py:267-322``) for a 1-D eta grid, no
+    symmetrisation: sum over t = i/maxpoints of G(eta / t^(1/3)) / t^(1/6),
+    G = spline of the inverse Lindhard function (TF and vW removed) on a
+    log grid."""
+    dt = 1.0 / maxpoints
+    coe = 4.0 / 5.0 * C_TF * 5.0 / 6.0 * dt
+    gp = np.logspace(np.log10(eta[1] / 10), np.log10(eta[-1] + 2), num=eta.size)
+    sp = spline_notaknot(gp, lindhard(gp, 1.0, 1.0))
+    kernel = np.zeros_like(eta)
+    for i in range(1, maxpoints + 1):
+        t = i * dt
+        kernel += spline_eval_clamped(sp, eta / np.cbrt(t)) / t ** (1.0 / 6.0)
+    return kernel * coe
+
+
+def lwt_tables(kerneltype="MGP", etamax=50.0, neta=50000, maxpoints=1000, x=1.0, y=1.0):
+    """Kernel and kernel-derivative splines (``LWT``, ``kedf/lwt.py:531-561``, order 3)."""
+    eta = np.linspace(0, etamax, neta)
+    if kerneltype == "MGP":
+        table = mgp_kernel_table(eta, maxpoints)
+    elif kerneltype == "WT":
+        table = lindhard(eta, x, 1.0) * (4.0 / 5.0 * C_TF)     # WTKernelTable, kernel.py:337-345
+    else:
+        raise ValueError(kerneltype)
+    sp = spline_notaknot(eta, table)
+    dtab = spline_eval_deriv(sp, eta) * (-1.0 * eta)
+    spd = spline_notaknot(eta, dtab)
+    return dict(eta=eta, table=table, sp=sp, spd=spd, etamax=etamax)
+
+
+def lwt_kernel_kf(q, kf, sp, etamax):
+    """``LWTKernelKf`` (``kernel.py:379-405``) with a spline table."""
+    eta = q / kf
+    K = np.where(eta < etamax, spline_eval(sp, np.minimum(eta, etamax)), spline_eval(sp, etamax))
+    if q.flat[0] < ZERO:
+        K.flat[0] = 0.0
+    return K
+
+
+def guess_kf_bound(kf, saved, kfmin=None, kfmax=None, kftol=1e-3):
+    """``guess_kf_bound`` (``lwt.py:36-79``); ``saved`` carries kfmin/kfmax across calls."""
+    kfmin_prev = saved.get("kfmin")
+    kfmax_prev = saved.get("kfmax")
+    if kfmin is not None and kfmax is not None:
+        return [kfmin, kfmax]
+    kf_l = kf.min()
+    kf_r = kf.max()
+    if kfmin_prev is None:
+        kfmin_prev = 10
+        if kfmin is None:
+            kfmin = kf_l
+    if kfmax_prev is None:
+        kfmax_prev = 1.0
+        if kfmax is None:
+            kfmax = kf_r
+    if kfmin is None or kfmin > kfmin_prev:
+        kfmin = kfmin_prev
+    if kfmax is None or kfmax < kfmax_prev:
+        kfmax = kfmax_prev
+    if kfmin > kf_l:
+        kfl = [1E-5, 1E-4, 5E-3, 1E-3, 5E-3, 1E-2, 5E-2, 0.1, 0.5, 1.0]
+        ratio = kf_l / kfmin
+        for i in range(len(kfl) - 1, 0, -1):
+            if ratio > kfl[i]:
+                kfmin *= kfl[i]
+                break
+    if kfmin < kftol:
+        kfmin = kftol
+    if kfmax < kf_r:
+        dk = kf_r - kfmax
+        kfmax += (np.round(dk / 0.5) + 1) * 0.5
+    saved["kfmin"] = kfmin
+    saved["kfmax"] = kfmax
+    return [kfmin, kfmax]
+
+
+def kf_knots(kfmin, kfmax, ratio=1.15):
+    """Geometric k_F knots (``lwt.py:171-187``, nsp and delta unset)."""
+    nsp = int(np.ceil(np.log(kfmax / kfmin) / np.log(ratio))) + 1
+    kflists = kfmin * ratio ** np.arange(nsp)
+    kflists[0] -= 1e-16
+    kflists[-1] += 1e-16
+    return kflists
+
+
+class LWTNL:
+    """``LWTPotentialEnergy`` (``kedf/lwt.py:82-341``) with the reference's
+    defaults of the direct API: kdd 3, ratio 1.15, alpha = beta = 5/6, no
+    lump factor, ldw 1/6.  ``interp``: "linear" or "hermite"."""
+
+    def __init__(self, kerneltype="MGP", interp="linear", etamax=50.0, neta=50000, maxpoints=1000, ratio=1.15,
+                 kdd=3, alpha=5.0 / 6.0, beta=5.0 / 6.0, ldw=None):
+        self.kerneltype, self.interp = kerneltype, interp
+        self.etamax, self.neta, self.maxpoints = etamax, neta, maxpoints
+        self.ratio, self.kdd, self.alpha, self.beta, self.ldw = ratio, kdd, alpha, beta, ldw
+        self.tables = None
+        self.saved = {"kfmin": None, "kfmax": None}
+        self.last_knots = None
+
+    def __call__(self, rho, grid, calc_e=True, calc_v=True):
+        if self.tables is None:
+            self.tables = lwt_tables(self.kerneltype, self.etamax, self.neta, self.maxpoints)
+        tab = self.tables
+        q = grid.q
+        alpha, beta = self.alpha, self.beta
+        kf = 2.0 * np.cbrt(3.0 * np.pi ** 2 * rho)
+        if abs(kf.max() - kf.min()) < 1e-8:
+            return 0.0, np.zeros_like(rho)
+        kfmin, kfmax = guess_kf_bound(kf, self.saved)
+        kdd = self.kdd if calc_v else 1
+        kf = np.where(kf > kfmax, kfmax, kf)
+        kfl = kf_knots(kfmin, kfmax, self.ratio)
+        self.last_knots = kfl
+        nsp = kfl.size
+        rc = rho.copy()
+        rc[~(rho > 0)] = 1e-30
+        rA = rc ** alpha
+        rA1 = rA / rc
+        rB, rB1 = (rA, rA1) if abs(alpha - beta) < 1e-8 else (rc ** beta, rc ** beta / rc)
+        rBG = fft(rB, grid)
+        mcalc = kdd > 1 or self.interp == "hermite"
+        pot1 = np.zeros_like(rho)
+        pot3 = np.zeros_like(rho)
+        pot2G = None
+        for i in range(nsp - 1):
+            if i == 0:
+                K0 = lwt_kernel_kf(q, kfl[0], tab["sp"], self.etamax)
+                p0 = ifft(K0 * rBG, grid)
+                if mcalc:
+                    D0 = lwt_kernel_kf(q, kfl[0], tab["spd"], self.etamax) / kfl[0]
+                    m0 = ifft(D0 * rBG, grid)
+            else:
+                p0, K0 = p1, K1
+                if mcalc:
+                    m0, D0 = m1, D1
+            K1 = lwt_kernel_kf(q, kfl[i + 1], tab["sp"], self.etamax)
+            p1 = ifft(K1 * rBG, grid)
+            if mcalc:
+                D1 = lwt_kernel_kf(q, kfl[i + 1], tab["spd"], self.etamax) / kfl[i + 1]
+                m1 = ifft(D1 * rBG, grid)
+            mask = (kf > kfl[i]) & (kf < kfl[i + 1] + 1e-18)
+            if i == 0:
+                small = kf < kfl[0] + 1e-18
+                t = (kf - kfl[0]) / kfl[0]
+                pot1[small] = p0[small] * t[small]
+                if kdd > 1:
+                    rhoU = rA * small
+                    if pot2G is None:
+                        pot2G = K0 * fft(rhoU * t, grid)
+                    if kdd == 3:
+                        pot3[mask] = m0[mask] * t[mask]
+            rhoU = rA * mask
+            Dkf = kfl[i + 1] - kfl[i]
+            t = (kf - kfl[i]) / Dkf
+            if self.interp == "linear":
+                t0 = 1 - t
+                pot1[mask] = p0[mask] * t0[mask] + p1[mask] * t[mask]
+                if kdd > 1:
+                    g = K0 * fft(rhoU * t0, grid) + K1 * fft(rhoU * t, grid)
+                    pot2G = g if pot2G is None else pot2G + g
+                    if kdd == 3:
+                        pot3[mask] = m0[mask] * t0[mask] + m1[mask] * t[mask]
+            else:
+                t2 = t * t
+                t3 = t2 * t
+                h00 = 2.0 * t3 - 3.0 * t2 + 1.0
+                h10 = t3 - 2.0 * t2 + t
+                h01 = 1.0 - h00
+                h11 = t3 - t2
+                pot1[mask] = h00[mask] * p0[mask] + h01[mask] * p1[mask] + Dkf * (h10[mask] * m0[mask]
+                                                                                    + h11[mask] * m1[mask])
+                if kdd > 1:
+                    g = (K0 * fft(rhoU * h00, grid) + K1 * fft(rhoU * h01, grid)
+                         + Dkf * (D0 * fft(rhoU * h10, grid) + D1 * fft(rhoU * h11, grid)))
+                    pot2G = g if pot2G is None else pot2G + g
+                    if kdd == 3:
+                        tm, t2m, t3m = t[mask], t2[mask], t3[mask]
+                        h00D = 6.0 * t2m - 6 * tm
+                        h10D = 3.0 * t2m - 4 * tm + 1.0
+                        h01D = -h00D
+                        h11D = 3.0 * t2m - 2 * tm
+                        pot3[mask] = (h00D * p0[mask] + h01D * p1[mask]) / Dkf + h10D * m0[mask] + h11D * m1[mask]
+        pot2 = ifft(pot2G, grid) if (calc_v and pot2G is not None) else pot1.copy()
+        ldw = 1.0 / 6.0 if self.ldw is None else self.ldw
+        factor = np.ones_like(rho)
+        rhov = rho.max()
+        m = rho < 1e-6
+        ld = max(0.1, ldw)
+        factor[m] = np.abs(rho[m]) ** ld / (rhov ** ld)
+        factor[rho < 0] = 0.0
+        pot1 = pot1 * factor
+        e = float((rA * pot1).sum() * grid.dV) if calc_e else None
+        if not calc_v:
+            return e, None
+        pot2 = pot2 * factor
+        pot3 = pot3 * factor
+        pot = pot1 * alpha * rA1 + pot2 * beta * rB1 + pot3 * (kf / 3.0) * rA1
+        return e, pot

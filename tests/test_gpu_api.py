@@ -154,3 +154,58 @@ def test_tn_al4_mixed_precision(api, golden):
     E = total.Energy(rho.to(api["torch"].float64))
     # 1e-5 eV/atom of the FP64 reference solve
     assert abs(E - float(a["E_final"])) < 1e-5 / 27.211386 * st.nat
+
+
+@pytest.mark.parametrize("interp", ["linear", "hermite"])
+@pytest.mark.parametrize("prec", [1, 0])
+def test_lmgp_reference_fixture(api, golden, interp, prec):
+    """KEDF LMGP (TF + vW + LMGP-NL) on the reference's test density (full grid,
+    non-orthogonal cell) against the reference-generated energy and potential
+    (test_functional.py:29-34 asserts 2.9145872498710492 for linear)."""
+    torch = api["torch"]
+    F = api["functional"]
+    d = golden("fde")
+    grid = api["grid"].DirectGrid(d["lattice"], tuple(int(x) for x in d["nr"]), full=True)
+    dt = torch.float64 if prec == 1 else torch.float32
+    rho = api["field"].DirectField(grid, data=np.ascontiguousarray(d["rho"]), dtype=dt)
+    ke = F.Functional(type="KEDF", name="LMGP", interp=interp)
+    out = ke(rho)
+    E = float(d["E_LMGP_" + interp])
+    vs = d["Vs_LMGP_" + interp]
+    etol, vtol = (1e-10, 1e-9) if prec == 1 else (2e-5, 2e-3)
+    assert abs(out.energy - E) <= etol * abs(E), (out.energy, E)
+    v = out.potential.to_numpy().ravel()[d["sample_idx"]]
+    assert np.abs(v - vs).max() <= vtol * np.abs(vs).max()
+    if interp == "linear" and prec == 1:
+        assert abs(out.energy - 2.9145872498710492) < 1e-10
+        assert ke._lwt.d.nknots == 15
+
+
+def test_tn_al4_lmgp_matches_oracle(api):
+    """TN with LMGP + LDA + Hartree + PP (config-5 functional, config-1 size)
+    against the oracle's TN solve: energy within 1e-6 Ha/atom."""
+    torch = api["torch"]
+    F = api["functional"]
+    st = systems.config_al4(0)
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = F.LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="LMGP"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho0 = api["field"].DirectField(grid)
+    rho0[:] = st.nelec / st.volume
+    opt = api["opt"].Optimization(EnergyEvaluator=total, optimization_method="TN",
+                                  optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100})
+    rho = opt.optimize_rho(guess_rho=rho0)
+    # oracle: same functional, same TN
+    ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
+    lw = O.LWTNL("MGP", "linear")
+
+    def evaluator(r, calc_e):
+        e, v = ev(r, calc_e)
+        e2, v2 = lw(r, ev.grid, calc_e=calc_e, calc_v=True)
+        return (None if e is None else e + e2), v + v2
+    ref = O.optimize_tn(evaluator, np.full(st.nr, st.nelec / st.volume), ev.grid, econv=1e-7, maxfun=50,
+                        maxiter=100)
+    assert opt.converged == 0
+    assert abs(opt.energy - ref["energy"]) < 1e-6 * st.nat, (opt.energy, ref["energy"])

@@ -10,11 +10,12 @@ def spline_notaknot(x, y):
     """Cubic spline through (x, y) with not-a-knot ends.
 
     ``scipy.interpolate.splrep(x, y, k=3, s=0)`` (FITPACK) builds exactly this
-    interpolant (interior knots at x[2..m-3]); here it is computed directly:
-    second derivatives from a tridiagonal system (the two not-a-knot rows
-    reduced with their neighbours), solved by the Thomas algorithm.
-    Returns (x, c) with c[i] = (a, b, c, d) of a + b u + c u^2 + d u^3 on
-    [x[i], x[i+1]], u = t - x[i].
+    interpolant (interior knots at x[2..m-3]); here it is computed directly.
+    Unknowns are the second derivatives M; the not-a-knot conditions (third
+    derivative continuous at x[1] and x[m-2]) express M[0] and M[m-1] through
+    their neighbours, which leaves a diagonally dominant tridiagonal system
+    for M[1..m-2] (Thomas algorithm).  Returns (x, c) with c[i] = (a, b, c, d)
+    of a + b u + c u^2 + d u^3 on [x[i], x[i+1]], u = t - x[i].
     """
     x = np.asarray(x, float)
     y = np.asarray(y, float)
@@ -23,40 +24,37 @@ def spline_notaknot(x, y):
         raise ValueError("spline needs >= 4 points")
     h = np.diff(x)
     delta = np.diff(y) / h
-    lo = np.zeros(n)
-    di = np.zeros(n)
-    up = np.zeros(n)
-    r = np.zeros(n)
-    lo[1:n - 1] = h[:-1]
-    di[1:n - 1] = 2.0 * (h[:-1] + h[1:])
-    up[1:n - 1] = h[1:]
-    r[1:n - 1] = 6.0 * (delta[1:] - delta[:-1])
-    f = h[0] / h[1]
-    di[0] = h[1] - f * h[0]
-    up[0] = -(h[0] + h[1]) - f * 2.0 * (h[0] + h[1])
-    r[0] = -f * r[1]
-    f = h[n - 2] / h[n - 3]
-    di[n - 1] = h[n - 3] - f * h[n - 2]
-    lo[n - 1] = -(h[n - 3] + h[n - 2]) - f * 2.0 * (h[n - 3] + h[n - 2])
-    r[n - 1] = -f * r[n - 2]
-    # Thomas algorithm
-    cp = np.zeros(n)
-    dp = np.zeros(n)
+    m = n - 2                                   # unknowns M[1..n-2]
+    lo = h[:-1].copy()                          # row j: lo M[j] + di M[j+1] + up M[j+2]
+    di = 2.0 * (h[:-1] + h[1:])
+    up = h[1:].copy()
+    r = 6.0 * (delta[1:] - delta[:-1])
+    # M0 = ((h0 + h1) M1 - h0 M2) / h1
+    di[0] += h[0] * (h[0] + h[1]) / h[1]
+    up[0] -= h[0] * h[0] / h[1]
+    # M[n-1] = ((h[n-3] + h[n-2]) M[n-2] - h[n-2] M[n-3]) / h[n-3]
+    a, b = h[n - 3], h[n - 2]
+    di[m - 1] += b * (a + b) / a
+    lo[m - 1] -= b * b / a
+    cp = np.zeros(m)
+    dp = np.zeros(m)
     cp[0] = up[0] / di[0]
     dp[0] = r[0] / di[0]
-    for i in range(1, n):
-        m = di[i] - lo[i] * cp[i - 1]
-        cp[i] = up[i] / m if i < n - 1 else 0.0
-        dp[i] = (r[i] - lo[i] * dp[i - 1]) / m
+    for i in range(1, m):
+        den = di[i] - lo[i] * cp[i - 1]
+        cp[i] = up[i] / den if i < m - 1 else 0.0
+        dp[i] = (r[i] - lo[i] * dp[i - 1]) / den
     M = np.zeros(n)
-    M[-1] = dp[-1]
-    for i in range(n - 2, -1, -1):
-        M[i] = dp[i] - cp[i] * M[i + 1]
-    a = y[:-1]
-    b = delta - h * (2.0 * M[:-1] + M[1:]) / 6.0
-    c = M[:-1] / 2.0
-    d = (M[1:] - M[:-1]) / (6.0 * h)
-    return x, np.ascontiguousarray(np.stack([a, b, c, d], axis=1))
+    M[m] = dp[m - 1]
+    for i in range(m - 2, -1, -1):
+        M[i + 1] = dp[i] - cp[i] * M[i + 2]
+    M[0] = ((h[0] + h[1]) * M[1] - h[0] * M[2]) / h[1]
+    M[n - 1] = ((a + b) * M[n - 2] - b * M[n - 3]) / a
+    ca = y[:-1]
+    cb = delta - h * (2.0 * M[:-1] + M[1:]) / 6.0
+    cc = M[:-1] / 2.0
+    cd = (M[1:] - M[:-1]) / (6.0 * h)
+    return x, np.ascontiguousarray(np.stack([ca, cb, cc, cd], axis=1))
 
 
 def quartic_coefficients(vp):

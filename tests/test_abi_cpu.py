@@ -102,3 +102,31 @@ def test_pme_bm_table():
     bm = pme_bm(nr, 10)
     b0, b1, b2 = bm[:12], bm[12:22], bm[22:]
     np.testing.assert_allclose(np.einsum("i,j,k->ijk", b0, b1, b2), B, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "log", "short"])
+def test_host_spline_grids(kind):
+    """Not-a-knot spline on the grids the tables use (uniform eta grids
+    included, where the end rows degenerate for a naive elimination)."""
+    from scipy.interpolate import splev, splrep
+    from dftpy_gb300._tables import lindhard, spline_notaknot, spline_values_deriv
+    if kind == "uniform":
+        x = np.linspace(0, 50, 50000)
+        y = lindhard(x, 1.0, 1.0)
+    elif kind == "log":
+        x = np.logspace(-5, np.log10(52), 50000)
+        y = lindhard(x, 1.0, 1.0)
+    else:
+        x = np.linspace(0.0, 1.0, 6)
+        y = np.sin(3 * x)
+    xs, c = spline_notaknot(x, y)
+    tck = splrep(x, y)
+    u = np.random.default_rng(1).uniform(x[0], x[-1], 20000)
+    i = np.clip(np.searchsorted(xs, u, side="right") - 1, 0, xs.size - 2)
+    t = u - xs[i]
+    v = c[i, 0] + t * (c[i, 1] + t * (c[i, 2] + t * c[i, 3]))
+    ref = splev(u, tck)
+    assert np.max(np.abs(v - ref)) <= 1e-12 * max(1.0, np.abs(ref).max())
+    d = spline_values_deriv(xs, c)
+    dref = splev(x, tck, der=1)
+    assert np.max(np.abs(d - dref)) <= 1e-9 * max(1.0, np.abs(dref).max())

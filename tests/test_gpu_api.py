@@ -207,5 +207,8 @@ def test_tn_al4_lmgp_matches_oracle(api):
         return (None if e is None else e + e2), v + v2
     ref = O.optimize_tn(evaluator, np.full(st.nr, st.nelec / st.volume), ev.grid, econv=1e-7, maxfun=50,
                         maxiter=100)
-    assert opt.converged == 0
+    # the reference algorithm stops this solve on a line-search failure after
+    # a few iterations (status 1); the device solve must end the same way at
+    # the same energy
+    assert opt.converged == ref["converged"], (opt.converged, ref["converged"])
     assert abs(opt.energy - ref["energy"]) < 1e-6 * st.nat, (opt.energy, ref["energy"])

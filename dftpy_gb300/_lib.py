@@ -97,6 +97,12 @@ _SIGS = [
                                     ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P, _P]),
     ("gbofdft_ewald", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P]),
+    ("gbofdft_forces_workspace_bytes", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_pp_forces", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P,
+                                         ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P]),
+    ("gbofdft_ewald_forces", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P,
+                                            _P]),
     ("gbofdft_tn_options_default", ctypes.c_int, [ctypes.POINTER(TnOptions)]),
     ("gbofdft_tn_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_optimize_tn", ctypes.c_int, [_P, ctypes.POINTER(Functional), _P, ctypes.POINTER(TnOptions), _P,
@@ -176,6 +182,12 @@ def aligned_ptr(t, align=256):
 def setup_workspace_bytes(plan, nat):
     n = ctypes.c_int64()
     check(load().gbofdft_setup_workspace_bytes(plan.handle, int(nat), ctypes.byref(n)), "setup_workspace_bytes")
+    return int(n.value)
+
+
+def forces_workspace_bytes(plan, nat):
+    n = ctypes.c_int64()
+    check(load().gbofdft_forces_workspace_bytes(plan.handle, int(nat), ctypes.byref(n)), "forces_workspace_bytes")
     return int(n.value)
 
 

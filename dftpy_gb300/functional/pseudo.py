@@ -116,19 +116,28 @@ class LocalPseudo(AbstractFunctional):
         species = torch.tensor([keys.index(s) for s in self.ions.symbols], dtype=torch.int32, device="cuda")
         return keys, spos, species
 
+    def _device_setup(self):
+        """Device copies of the positions, species, v(|G|) tables and PME b(m)."""
+        if getattr(self, "_dev", None) is None:
+            keys, spos, species = self._device_inputs()
+            self._tables = [_VTable(*self._pp[k][:2]) for k in keys]
+            tabs = (_lib.VTable * len(keys))(*[t.ctypes() for t in self._tables])
+            bm = None
+            if self.PME:
+                bm = torch.tensor(pme_bm(self.grid.nrR, self.BsplineOrder).view(np.float64), device="cuda")
+            self._dev = (keys, spos, species, tabs, bm)
+        return self._dev
+
     def local_PP(self):
         """v_loc(G) and v_loc(r) in FP64 (``local_PP``, ``:237-246``)."""
         if getattr(self, "_vG", None) is not None:
             return
         g = self.grid
         plan = g.plan(torch.float64)
-        keys, spos, species = self._device_inputs()
-        self._tables = [_VTable(*self._pp[k][:2]) for k in keys]
-        tabs = (_lib.VTable * len(keys))(*[t.ctypes() for t in self._tables])
+        keys, spos, species, tabs, bm = self._device_setup()
         nb = _lib.setup_workspace_bytes(plan, self.ions.nat)
         work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
         wptr = _lib.aligned_ptr(work, 256)
-        bm = torch.tensor(pme_bm(g.nrR, self.BsplineOrder).view(np.float64), device="cuda") if self.PME else None
         n0, n1, n2 = (int(x) for x in g.nrR)
         vG = torch.empty((n0, n1, n2 // 2 + 1), dtype=torch.complex128, device="cuda")
         vR = torch.empty((n0, n1, n2), dtype=torch.float64, device="cuda")
@@ -138,6 +147,28 @@ class LocalPseudo(AbstractFunctional):
             _lib.stream_ptr()), "vloc")
         self._vG = vG
         self._vreal[torch.float64] = vR
+
+    def forces(self, rho):
+        """Forces of the local pseudopotential on the ions, nat x 3 numpy array
+        (``forces``, ``:260-271``: ``_ForcePME`` with PME, ``_Force`` without).
+        The transforms run in the density's precision; sums in FP64."""
+        if rho is None:
+            raise AttributeError("Must specify rho")
+        if not isinstance(rho, DirectField):
+            raise TypeError("rho must be DirectField")
+        if rho.ndim > 3:
+            rho = DirectField(self.grid, data=rho.sum(dim=0))
+        keys, spos, species, tabs, bm = self._device_setup()
+        plan = self.grid.plan(rho.dtype)
+        nat = self.ions.nat
+        nb = _lib.forces_workspace_bytes(plan, nat)
+        work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
+        F = torch.empty((nat, 3), dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().gbofdft_pp_forces(
+            plan.handle, _lib.ptr(rho), len(keys), tabs, nat, _lib.ptr(spos), _lib.ptr(species), int(self.PME),
+            self.BsplineOrder, _lib.ptr(bm) if bm is not None else None, _lib.aligned_ptr(work, 256), nb,
+            _lib.ptr(F), _lib.stream_ptr()), "pp_forces")
+        return F.cpu().numpy()
 
     def vreal_of(self, dtype):
         self.local_PP()
@@ -236,10 +267,10 @@ class ewald:
         e += -4.0 * math.pi * (1.0 / (4.0 * self.eta * self.grid.volume) / 2.0) * float(q.sum()) ** 2
         return e
 
-    def _gpu_parts(self):
-        if self._parts is None:
+    def _device_setup(self):
+        """rmax, lattice images and device copies of positions, charges, b(m)."""
+        if getattr(self, "_dev", None) is None:
             g = self.grid
-            plan = g.plan(torch.float64)
             rmax = _erfcinv(self.precision / 3.0) / math.sqrt(self.eta)
             L = np.sqrt((g.lattice ** 2).sum(axis=1))
             N = np.ceil(rmax / L).astype(int)
@@ -251,16 +282,43 @@ class ewald:
             spos = torch.tensor(ions.get_scaled_positions(), dtype=torch.float64, device="cuda").contiguous()
             q = torch.tensor(ions.charges, dtype=torch.float64, device="cuda").contiguous()
             bm = torch.tensor(pme_bm(g.nrR, self.order).view(np.float64), device="cuda") if self.PME else None
-            nb = _lib.setup_workspace_bytes(plan, ions.nat)
+            self._dev = (rmax, images, pos, spos, q, bm)
+        return self._dev
+
+    def _gpu_parts(self):
+        if self._parts is None:
+            plan = self.grid.plan(torch.float64)
+            rmax, images, pos, spos, q, bm = self._device_setup()
+            nat = self.ions.nat
+            nb = _lib.setup_workspace_bytes(plan, nat)
             work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
             out = torch.zeros(2, dtype=torch.float64, device="cuda")
             _lib.check(_lib.load().gbofdft_ewald(
-                plan.handle, ions.nat, _lib.ptr(pos), _lib.ptr(spos), _lib.ptr(q), float(self.eta), float(rmax),
+                plan.handle, nat, _lib.ptr(pos), _lib.ptr(spos), _lib.ptr(q), float(self.eta), float(rmax),
                 _lib.ptr(images), int(images.shape[0]), int(self.PME), int(self.order),
                 _lib.ptr(bm) if bm is not None else None, _lib.aligned_ptr(work, 256), nb, _lib.ptr(out),
                 _lib.stream_ptr()), "ewald")
             self._parts = [float(x) for x in out.cpu().numpy()]
         return self._parts
+
+    @property
+    def forces(self):
+        """Ion-ion forces, nat x 3 numpy array (``forces``, ``ewald.py:510-521``):
+        ``Forces_real`` plus ``Forces_rec_PME`` or ``Forces_rec``, in FP64."""
+        if getattr(self, "_forces", None) is None:
+            plan = self.grid.plan(torch.float64)
+            rmax, images, pos, spos, q, bm = self._device_setup()
+            nat = self.ions.nat
+            nb = _lib.forces_workspace_bytes(plan, nat)
+            work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
+            F = torch.empty((nat, 3), dtype=torch.float64, device="cuda")
+            _lib.check(_lib.load().gbofdft_ewald_forces(
+                plan.handle, nat, _lib.ptr(pos), _lib.ptr(spos), _lib.ptr(q), float(self.eta), float(rmax),
+                _lib.ptr(images), int(images.shape[0]), int(self.PME), int(self.order),
+                _lib.ptr(bm) if bm is not None else None, _lib.aligned_ptr(work, 256), nb, _lib.ptr(F),
+                _lib.stream_ptr()), "ewald_forces")
+            self._forces = F.cpu().numpy()
+        return self._forces
 
     def Energy_real(self):
         return self._gpu_parts()[0]

@@ -5,6 +5,8 @@ PSEUDO), ``compute`` issues ONE fused device evaluation (``gbofdft_eval``):
 one read of rho, shared transform passes, one write of the total potential.
 Any other AbstractFunctional falls back to summing the members' outputs.
 """
+import numpy as np
+
 from .. import _lib
 from .kedf import KEDF
 from .output import AbstractFunctional, FunctionalOutput
@@ -100,3 +102,28 @@ class TotalFunctional(AbstractFunctional):
                 parts["II"] = r
             parts["TOTAL"] = parts["TOTAL"] + r
         return parts if split else parts["TOTAL"]
+
+    def get_forces(self, rho, ions=None, split=False, **kwargs):
+        """Forces on the ions, nat x 3 (Ha/Bohr) (``get_forces``,
+        ``total_functional.py:148-174``): every member with a ``forces`` method
+        plus the Ewald forces; ``split=True`` returns them by member key with
+        the Ewald part under ``"II"`` and the sum under ``"TOTAL"``."""
+        ew = self.ewald
+        if ions is None:
+            if ew is None:
+                raise ValueError("Please provide ions for forces")
+            ions = ew.ions
+        forces = {"TOTAL": np.zeros((ions.nat, 3))}
+        for key, func in self.funcDict.items():
+            if hasattr(func, "forces"):
+                f = func.forces(rho)
+                if f is not None:
+                    if split:
+                        forces[key] = f
+                    forces["TOTAL"] = forces["TOTAL"] + f
+        if ew is not None:
+            f = ew.forces
+            if split:
+                forces["II"] = f
+            forces["TOTAL"] = forces["TOTAL"] + f
+        return forces if split else forces["TOTAL"]

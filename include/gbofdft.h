@@ -235,6 +235,36 @@ int gbofdft_ewald(gbofdft_plan* plan, int nat, const double* pos_dev, const doub
                   const double* charges_dev, double eta, double rmax, const double* images_dev, int nimg, int pme,
                   int order, const double* bm_dev, void* work, int64_t work_bytes, double* out_dev, void* stream);
 
+/* ---- forces on the ions -------------------------------------------------- */
+
+/* Device workspace bytes for gbofdft_pp_forces / gbofdft_ewald_forces with nat atoms. */
+int gbofdft_forces_workspace_bytes(const gbofdft_plan* plan, int nat, int64_t* bytes);
+
+/*
+ * Forces of the local pseudopotential on the ions for the density rho
+ * (device, plan precision): forces_dev = nat x 3 doubles (Ha/Bohr),
+ * overwritten.  Arguments as gbofdft_vloc; pme != 0 gathers the B-spline
+ * derivative of ifft(rhoG conj(B) vline_s) per species, pme == 0 sums the
+ * exact structure factor over the half-space G mask.  At most 65535 atoms.
+ * Replaces LocalPseudo.force -> _ForcePME / _Force
+ * (src/dftpy/functional/pseudo/__init__.py:457-523).
+ */
+int gbofdft_pp_forces(gbofdft_plan* plan, const void* rho, int nspec, const gbofdft_vtable* tables, int nat,
+                      const double* spos_dev, const int* species_dev, int pme, int order, const double* bm_dev,
+                      void* work, int64_t work_bytes, double* forces_dev, void* stream);
+
+/*
+ * Ewald forces on the ions, real-space part plus reciprocal part (PME or
+ * exact), written to forces_dev (nat x 3 doubles, Ha/Bohr).  eta, rmax and
+ * the images as for gbofdft_ewald.
+ * Replaces ewald.forces, Forces_real, Forces_rec, Forces_rec_PME
+ * (src/dftpy/ewald.py:510-604, 810-857).
+ */
+int gbofdft_ewald_forces(gbofdft_plan* plan, int nat, const double* pos_dev, const double* spos_dev,
+                         const double* charges_dev, double eta, double rmax, const double* images_dev, int nimg,
+                         int pme, int order, const double* bm_dev, void* work, int64_t work_bytes,
+                         double* forces_dev, void* stream);
+
 /* ---- direct density optimisation (truncated Newton) ---------------------- */
 
 /* Options of Optimization(optimization_method="TN") (optimization.py:64-77). */

@@ -499,6 +499,23 @@ def pp_forces_pme(rho, grid, positions, symbols, tables, order=10):
     return F
 
 
+def pp_forces_exact(rho, grid, positions, symbols, tables):
+    """``LocalPseudo._Force`` (``pseudo/__init__.py:457-473``): exact structure
+    factor over the half-space mask, ``2/Omega sum G vline Im(rhoG e^{+iG.R})``."""
+    rhoG = fft(rho, grid)
+    g = grid.g
+    mask = grid.mask
+    q = grid.q
+    F = np.zeros((len(symbols), 3))
+    vls = {key: vline(q, *tables[key]) for key in set(symbols)}
+    for i, s in enumerate(symbols):
+        istrf = np.exp(1j * np.einsum("lijk,l->ijk", g, positions[i]))
+        den = vls[s][mask] * (rhoG[mask] * istrf[mask]).imag
+        for j in range(3):
+            F[i, j] = np.einsum("i,i->", g[j][mask], den)
+    return F * 2.0 / grid.volume
+
+
 # ----------------------------------------------------------------------------
 # Ewald (ion-ion), PME or exact reciprocal part
 # ----------------------------------------------------------------------------

@@ -61,6 +61,53 @@ def test_local_pseudo_and_ewald(api, golden, case, pme):
         assert abs(ref["rec"] - 7.606943756474895) < 1e-5
 
 
+@pytest.mark.parametrize("pme", [True, False])
+@pytest.mark.parametrize("case", ["al4", "fde"])
+def test_forces_match_oracle_and_fixture(api, golden, case, pme):
+    """PP and Ewald forces (FP64) against the oracle (1e-10 Ha/Bohr) and the
+    forces the reference computed for the same density."""
+    if case == "al4":
+        d = golden("al4")
+        st = systems.config_al4(0)
+        lat, nr, pos, sym, full = st.lattice, st.nr, st.positions, st.symbols, False
+    else:
+        d = golden("fde")
+        lat, nr, pos, sym, full = d["lattice"], tuple(int(x) for x in d["nr"]), d["positions"], ["Al", "Al"], True
+    rho_np = np.ascontiguousarray(d["rho"])
+    grid = api["grid"].DirectGrid(lat, nr, full=full)
+    ions = api["ions"].Ions(sym, positions=pos, cell=lat)
+    ps = api["functional"].LocalPseudo(grid=grid, ions=ions, PP_list=_pp(api, sym), PME=pme)
+    rho = api["field"].DirectField(grid, data=rho_np)
+    g = O.Grid(lat, nr, full=full)
+    tab = {s: systems.analytic_pp_table(*systems.SPECIES[s]) for s in set(sym)}
+    f_pp = ps.forces(rho)
+    ref_pp = (O.pp_forces_pme if pme else O.pp_forces_exact)(rho_np, g, pos, sym, tab)
+    np.testing.assert_allclose(f_pp, ref_pp, rtol=0, atol=1e-10)
+    f_ii = ps.get_ewald().forces
+    q = np.array([systems.SPECIES[s][0] for s in sym])
+    np.testing.assert_allclose(f_ii, O.ewald_forces(g, pos, q, pme=pme), rtol=0, atol=1e-9)
+    if case == "fde":
+        np.testing.assert_allclose(f_pp, d["F_PP_PME" if pme else "F_PP_EXACT"], rtol=0, atol=1e-10)
+        np.testing.assert_allclose(f_ii, d["EW_forces_pme" if pme else "EW_forces"], rtol=0, atol=1e-9)
+    elif pme:
+        np.testing.assert_allclose(f_pp, d["forces_pp"], rtol=0, atol=1e-10)
+        np.testing.assert_allclose(f_ii, d["forces_ii"], rtol=0, atol=1e-9)
+
+
+def test_forces_fp32_density(api, golden):
+    """PME PP forces from an FP32 density agree with the FP64 ones to FP32
+    transform accuracy (far inside the 1e-5 Ha/Bohr force gate)."""
+    torch = api["torch"]
+    d = golden("al4")
+    st = systems.config_al4(0)
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = api["functional"].LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    rho = api["field"].DirectField(grid, data=np.ascontiguousarray(d["rho"]))
+    f64 = ps.forces(rho)
+    f32 = ps.forces(rho.to(torch.float32))
+    assert np.abs(f32 - f64).max() < 1e-6
+
+
 def test_total_functional_fused_vs_members(api, golden):
     """Fused single-launch evaluation equals the sum of the members' outputs."""
     torch = api["torch"]
@@ -133,6 +180,10 @@ def test_tn_al4_matches_reference_solve(api, golden):
     # same control flow as the reference: evaluation counts within a couple
     assert abs(s["n_eval_ev"] - int(a["n_ev"])) <= 2 and abs(s["n_eval_v"] - int(a["n_v"])) <= 6
     assert np.abs(rho.to_numpy() - a["rho"]).max() < 1e-5
+    F = total.get_forces(rho)
+    assert np.abs(F - a["forces"]).max() < 1e-5
+    parts = total.get_forces(rho, split=True)
+    np.testing.assert_allclose(parts["TOTAL"], parts["PSEUDO"] + parts["II"], rtol=0, atol=1e-14)
 
 
 def test_tn_al256_wt_matches_reference_solve(api, golden):
@@ -145,6 +196,8 @@ def test_tn_al256_wt_matches_reference_solve(api, golden):
     assert abs(E - float(a["E_final"])) < 1e-6 * st.nat
     r = rho.to_numpy().ravel()[a["sample_idx"]]
     assert np.abs(r - a["rho_s"]).max() < 1e-4
+    # forces of the converged density within 1e-5 Ha/Bohr of the reference's
+    assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
 
 
 def test_tn_al4_mixed_precision(api, golden):
@@ -154,6 +207,7 @@ def test_tn_al4_mixed_precision(api, golden):
     E = total.Energy(rho.to(api["torch"].float64))
     # 1e-5 eV/atom of the FP64 reference solve
     assert abs(E - float(a["E_final"])) < 1e-5 / 27.211386 * st.nat
+    assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
 
 
 @pytest.mark.parametrize("interp", ["linear", "hermite"])

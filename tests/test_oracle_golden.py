@@ -73,6 +73,9 @@ def test_local_pseudo(fde, pme):
     if pme:
         f = O.pp_forces_pme(rho, g, d["positions"], sym, tab)
         np.testing.assert_allclose(f, d["F_PP_PME"], atol=1e-12)
+    else:
+        f = O.pp_forces_exact(rho, g, d["positions"], sym, tab)
+        np.testing.assert_allclose(f, d["F_PP_EXACT"], atol=1e-12)
 
 
 @pytest.mark.parametrize("pme", [True, False])

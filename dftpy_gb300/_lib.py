@@ -97,6 +97,10 @@ _SIGS = [
                                     ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P, _P]),
     ("gbofdft_ewald", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P]),
+    ("gbofdft_density_normalize", ctypes.c_int, [_P, _P, ctypes.c_double, ctypes.c_double, _P, _P]),
+    ("gbofdft_density_guess", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P,
+                                             ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P,
+                                             ctypes.c_double, ctypes.c_double, _P]),
     ("gbofdft_forces_workspace_bytes", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_pp_forces", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P,
                                          ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P, _P]),

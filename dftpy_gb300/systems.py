@@ -33,6 +33,17 @@ def analytic_pp_table(Z, rc, npts=10000, gmin=1e-4, gmax=30.0):
     return gp, vp
 
 
+ATOMIC_SIGMA = {"Al": 0.9, "Mg": 1.1}   # Gaussian valence-density widths (Bohr)
+
+
+def atomic_density_table(Z, sigma, npts=1000, qmax=10.0):
+    """|G| grid and the Fourier transform Z exp(-(G sigma)^2 / 2) of a normalised
+    Gaussian valence density of Z electrons (a reciprocal-space atomic density
+    table for ``DensityGenerator(r=..., arho=...)``)."""
+    q = np.linspace(0.0, qmax, npts)
+    return q, Z * np.exp(-0.5 * (q * sigma) ** 2)
+
+
 @dataclass
 class Structure:
     """A periodic cell with atoms (Bohr) and its real-space grid."""

@@ -235,6 +235,34 @@ int gbofdft_ewald(gbofdft_plan* plan, int nat, const double* pos_dev, const doub
                   const double* charges_dev, double eta, double rmax, const double* images_dev, int nimg, int pme,
                   int order, const double* bm_dev, void* work, int64_t work_bytes, double* out_dev, void* stream);
 
+/* ---- density guesses -------------------------------------------------------- */
+
+/*
+ * In place on rho (plan precision, device): rho[rho < dtol] = dtol, then
+ * nc = sum(rho) dV (FP64, fixed order) and, if ncharge > 1e-6,
+ * rho *= ncharge / nc.  nc_dev (device double, may be NULL) receives nc.
+ * Pass dtol = -HUGE_VAL to skip the clamp, ncharge = 0 to skip the scaling.
+ * Replaces the clamp-and-scale step of DensityGenerator.guess_rho_atom and
+ * get_3d_value_recipe (src/dftpy/density/density.py:226-234, 288-297).
+ */
+int gbofdft_density_normalize(gbofdft_plan* plan, void* rho, double dtol, double ncharge, double* nc_dev,
+                              void* stream);
+
+/*
+ * Superposed atomic densities from per-species reciprocal-space tables
+ * rho_s(|G|) (same table format and structure-factor options as
+ * gbofdft_vloc; a table is 0 from gmax on and, with q4 = 0, below gmin),
+ * written to rho_recip (half spectrum) and rho (real space), then clamped at
+ * dtol and scaled to ncharge electrons as gbofdft_density_normalize.
+ * Workspace: gbofdft_setup_workspace_bytes.
+ * Replaces DensityGenerator.guess_rho -> get_3d_value_recipe
+ * (src/dftpy/density/density.py:151-197, 252-300).
+ */
+int gbofdft_density_guess(gbofdft_plan* plan, int nspec, const gbofdft_vtable* tables, int nat,
+                          const double* spos_dev, const int* species_dev, int pme, int order, const double* bm_dev,
+                          void* work, int64_t work_bytes, void* rho_recip, void* rho, double dtol, double ncharge,
+                          void* stream);
+
 /* ---- forces on the ions -------------------------------------------------- */
 
 /* Device workspace bytes for gbofdft_pp_forces / gbofdft_ewald_forces with nat atoms. */

@@ -460,6 +460,44 @@ def local_pp_recip(grid, positions, symbols, tables, pme=True, order=10):
     return v
 
 
+def radial_to_3d(q, table):
+    """``RadialGrid.to_3d_grid`` (``grid.py:766-779``): interpolating cubic
+    spline of the (|G|, value) table, 0 outside [q[0], q[-1])."""
+    gp, vp = (np.asarray(t, float) for t in table)
+    sp = spline_notaknot(gp, vp)
+    out = np.zeros_like(q)
+    m = (q < gp[-1]) & (q >= gp[0])
+    out[m] = spline_eval(sp, q[m])
+    return out
+
+
+def density_guess_recipe(grid, positions, symbols, tables, ncharge, pme=True, order=10, dtol=1e-30):
+    """``get_3d_value_recipe`` with ``direct=True`` (``density/density.py:252-300``):
+    superposed reciprocal-space atomic tables, inverse transform, clamp at
+    ``dtol``, scale to ``ncharge``."""
+    q = grid.q
+    rg = np.zeros(grid.nrG, dtype=np.complex128)
+    spos = np.linalg.solve(grid.lattice.T, np.asarray(positions).T).T % 1.0
+    for key in sorted(set(symbols)):
+        line = radial_to_3d(q, tables[key])
+        idx = [i for i, s in enumerate(symbols) if s == key]
+        if pme:
+            Q = pme_qarray(grid, spos[idx], np.ones(len(idx)), order)
+            rg = rg + line * fft(Q, grid)
+        else:
+            g = grid.g
+            for i in idx:
+                rg += line * np.exp(-1j * np.einsum("lijk,l->ijk", g, positions[i]))
+    if pme:
+        rg = rg * bspline_barray(grid, order) * grid.nnr / grid.volume
+    rho = ifft(rg, grid)
+    rho[rho < dtol] = dtol
+    nc = rho.sum() * grid.dV
+    if ncharge > 1e-6:
+        rho = rho * (ncharge / nc)
+    return rho
+
+
 def local_pp(grid, positions, symbols, tables, pme=True, order=10):
     """Real-space v_loc (``LocalPseudo.local_PP``, ``pseudo/__init__.py:237-246``)."""
     return ifft(local_pp_recip(grid, positions, symbols, tables, pme, order), grid)

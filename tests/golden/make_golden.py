@@ -17,6 +17,9 @@ al4.npz      32^3, 4 Al: full TN optimisation (TFVW+LDA+Hartree+analytic PP,
              PME), converged density, energies, forces, evaluation counts.
 al256.npz    128^3, 256 Al, WT: full TN optimisation; scalars and a density
              sample (the full field is 16 MB).
+guess.npz    superposed atomic densities (``get_3d_value_recipe``, PME and
+             exact) from Gaussian reciprocal-space tables on the 4-Al grid and
+             on the skewed ``Al_fde_rho.pp`` grid (full=True).
 dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
              (``LineSearchDcsrch2``) on analytic 1-D functions.
 """
@@ -237,6 +240,32 @@ def gen_al256():
     np.savez_compressed(HERE / "al256.npz", **out)
 
 
+def gen_guess():
+    """get_3d_value_recipe (density/density.py:252-300) on two grids."""
+    from dftpy.density.density import get_3d_value_recipe
+    out = {}
+    fde = np.load(HERE / "fde.npz")
+    st = systems.config_al4(seed=0)
+    cases = {"al4": (st.lattice.copy(), st.nr, st.positions.copy(), list(st.symbols), False),
+             "fde": (fde["lattice"], tuple(int(x) for x in fde["nr"]), fde["positions"], ["Al", "Al"], True)}
+    for name, (lat, nr, pos, sym, full) in cases.items():
+        grid = DirectGrid(lattice=lat.copy(), nr=nr, full=full)
+        ions = Ions(symbols=sym, positions=pos.copy(), cell=lat.copy(), units="au")
+        ions.set_charges({s: systems.SPECIES[s][0] for s in set(sym)})
+        r, arho = {}, {}
+        for s_ in set(sym):
+            r[s_], arho[s_] = systems.atomic_density_table(systems.SPECIES[s_][0], systems.ATOMIC_SIGMA[s_])
+        idx = sample_index(int(np.prod(nr)))
+        out[name + "_idx"] = idx
+        for pme in (True, False):
+            rho = get_3d_value_recipe(r, arho, ions, grid, ncharge=None, rho=None, dtol=1e-30, direct=True,
+                                      pme=pme, order=10)
+            tag = name + ("_pme" if pme else "_exact")
+            out[tag + "_s"] = np.asarray(rho).ravel()[idx]
+            out[tag + "_c"] = checksums(rho)
+    np.savez_compressed(HERE / "guess.npz", **out)
+
+
 def gen_dcsrch():
     """Trial-step sequences of the reference line search on 1-D test functions."""
     cases = {
@@ -268,7 +297,7 @@ def gen_dcsrch():
     print("dcsrch: %d cases" % len(cases))
 
 
-GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch}
+GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

@@ -266,3 +266,66 @@ def test_tn_al4_lmgp_matches_oracle(api):
     # the same energy
     assert opt.converged == ref["converged"], (opt.converged, ref["converged"])
     assert abs(opt.energy - ref["energy"]) < 1e-6 * st.nat, (opt.energy, ref["energy"])
+
+
+@pytest.mark.parametrize("pme", [True, False])
+@pytest.mark.parametrize("case", ["al4", "fde"])
+def test_density_guess_matches_reference(api, golden, case, pme):
+    """Superposed atomic densities on the GPU against the reference's
+    get_3d_value_recipe output (FP64: 1e-12 of max rho) and the oracle; the
+    FP32 plan to 1e-6 relative; the electron count exactly restored."""
+    torch = api["torch"]
+    from dftpy_gb300.density import DensityGenerator
+    d = golden("guess")
+    if case == "al4":
+        st = systems.config_al4(0)
+        lat, nr, pos, sym, full = st.lattice, st.nr, st.positions, list(st.symbols), False
+    else:
+        f = golden("fde")
+        lat, nr, pos, sym, full = f["lattice"], tuple(int(x) for x in f["nr"]), f["positions"], ["Al", "Al"], True
+    grid = api["grid"].DirectGrid(lat, nr, full=full)
+    ions = api["ions"].Ions(sym, positions=pos, cell=lat)
+    ions.set_charges({s: systems.SPECIES[s][0] for s in set(sym)})
+    r, arho = {}, {}
+    for s in set(sym):
+        r[s], arho[s] = systems.atomic_density_table(systems.SPECIES[s][0], systems.ATOMIC_SIGMA[s])
+    gen = DensityGenerator(r=r, arho=arho)
+    rho = gen.guess_rho(ions, grid=grid, pme=pme)
+    x = rho.to_numpy()
+    tag = case + ("_pme" if pme else "_exact")
+    ref = d[tag + "_s"]
+    assert np.abs(x.ravel()[d[case + "_idx"]] - ref).max() <= 1e-12 * np.abs(ref).max()
+    nel = sum(systems.SPECIES[s][0] for s in sym)
+    assert abs(rho.integral() - nel) < 1e-10
+    g = O.Grid(lat, nr, full=full)
+    tab = {s: (r[s], arho[s]) for s in set(sym)}
+    o = O.density_guess_recipe(g, pos, sym, tab, nel, pme=pme)
+    assert np.abs(x - o).max() <= 1e-12 * np.abs(o).max()
+    rho32 = DensityGenerator(r=r, arho=arho).guess_rho(
+        ions, grid=grid, rho=api["field"].DirectField(grid, dtype=torch.float32), pme=pme)
+    assert rho32.dtype == torch.float32
+    assert np.abs(rho32.to_numpy().astype(np.float64) - o).max() <= 1e-6 * np.abs(o).max()
+
+
+def test_tn_from_atomic_guess(api, golden):
+    """A TN solve started from the superposed atomic density reaches the
+    reference's energy."""
+    from dftpy_gb300.density import DensityGenerator
+    a = golden("al4")
+    st = systems.config_al4(0)
+    F = api["functional"]
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ions = _ions(api, st)
+    ps = F.LocalPseudo(grid=grid, ions=ions, PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="TFVW"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    r, arho = {}, {}
+    for s in set(st.symbols):
+        r[s], arho[s] = systems.atomic_density_table(systems.SPECIES[s][0], systems.ATOMIC_SIGMA[s])
+    rho0 = DensityGenerator(r=r, arho=arho).guess_rho(ps.ions, grid=grid)
+    opt = api["opt"].Optimization(EnergyEvaluator=total, optimization_method="TN",
+                                  optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100})
+    rho = opt.optimize_rho(guess_rho=rho0)
+    assert opt.converged == 0
+    assert abs(total.Energy(rho) - float(a["E_final"])) < 1e-6 * st.nat

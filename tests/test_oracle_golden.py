@@ -141,3 +141,23 @@ def test_tn_solve_al4(golden):
     assert np.abs(r["rho"] - a["rho"]).max() < 1e-5
     F = ev.forces(r["rho"])
     np.testing.assert_allclose(F, a["forces"], atol=1e-5)
+
+
+@pytest.mark.parametrize("pme", [True, False])
+@pytest.mark.parametrize("case", ["al4", "fde"])
+def test_density_guess_recipe(golden, case, pme):
+    """Superposed atomic densities (get_3d_value_recipe) against the reference."""
+    d = golden("guess")
+    if case == "al4":
+        st = systems.config_al4(0)
+        lat, nr, pos, sym, full = st.lattice, st.nr, st.positions, list(st.symbols), False
+    else:
+        f = golden("fde")
+        lat, nr, pos, sym, full = f["lattice"], tuple(int(x) for x in f["nr"]), f["positions"], ["Al", "Al"], True
+    g = O.Grid(lat, nr, full=full)
+    tab = {s: systems.atomic_density_table(systems.SPECIES[s][0], systems.ATOMIC_SIGMA[s]) for s in set(sym)}
+    nel = sum(systems.SPECIES[s][0] for s in sym)
+    rho = O.density_guess_recipe(g, pos, sym, tab, nel, pme=pme)
+    tag = case + ("_pme" if pme else "_exact")
+    np.testing.assert_allclose(rho.ravel()[d[case + "_idx"]], d[tag + "_s"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose([rho.sum(), (rho * rho).sum()], d[tag + "_c"][:2], rtol=1e-12)

@@ -172,6 +172,7 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         energies.append(opt.energy)
         glue.append(opt.stats.get("t_glue", 0.0))
         evals.append([{"precision": st["precision"], "n_eval_ev": st["n_eval_ev"], "n_eval_v": st["n_eval_v"],
+                       "n_eval_hess_f32": st.get("n_eval_hess", 0),
                        "converged": st["converged"], "n_iter": st["n_iter"], "n_sync": st["n_sync"],
                        "t_sync_s": round(st["t_sync"], 4), "t_host_s": round(st["t_total"], 4),
                        "last_dE": [round(e - st["history"][-1], 12) for e in st["history"][-5:]]}

@@ -57,7 +57,8 @@ class TnOptions(ctypes.Structure):
     """Mirror of ``gbofdft_tn_options``."""
     _fields_ = [("econv", ctypes.c_double), ("maxfun", ctypes.c_int), ("maxiter", ctypes.c_int),
                 ("maxls", ctypes.c_int), ("c1", ctypes.c_double), ("c2", ctypes.c_double),
-                ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double)]
+                ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double),
+                ("pred_stop", ctypes.c_double)]
 
 
 class TnResult(ctypes.Structure):
@@ -66,7 +67,7 @@ class TnResult(ctypes.Structure):
                 ("n_iter", ctypes.c_int), ("n_eval_ev", ctypes.c_int), ("n_eval_v", ctypes.c_int),
                 ("energies", ctypes.c_double * 8), ("history", ctypes.POINTER(ctypes.c_double)),
                 ("history_cap", ctypes.c_int), ("n_history", ctypes.c_int), ("n_sync", ctypes.c_int),
-                ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double)]
+                ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double), ("n_eval_hess", ctypes.c_int)]
 
 
 _lib = None
@@ -109,6 +110,10 @@ _SIGS = [
                                             _P]),
     ("gbofdft_tn_options_default", ctypes.c_int, [ctypes.POINTER(TnOptions)]),
     ("gbofdft_tn_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_tn_hess_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_optimize_tn_split", ctypes.c_int, [_P, ctypes.POINTER(Functional), _P, ctypes.POINTER(Functional), _P,
+                                                 ctypes.POINTER(TnOptions), _P, ctypes.c_int64, _P, ctypes.c_int64,
+                                                 ctypes.POINTER(TnResult), _P]),
     ("gbofdft_optimize_tn", ctypes.c_int, [_P, ctypes.POINTER(Functional), _P, ctypes.POINTER(TnOptions), _P,
                                            ctypes.c_int64, ctypes.POINTER(TnResult), _P]),
     ("gbofdft_dcsrch", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.c_int64,

@@ -122,16 +122,23 @@ int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st) {
 
 }  // namespace
 
+// Fields of the Hessian-precision inner loop (split mode only)
+enum { H_PHI = 0, H_RB, H_POT, H_CGR, H_CGP, H_AP, H_DIR, H_BEST, H_PHI1, H_POT1, H_TMP, H_NF };
+
 struct TnState {
   gbofdft_plan* p;
   const gbofdft_functional* fn;
   Ws w;
   cudaStream_t st;
   double host[S_COUNT];
-  int n_ev, n_v;
+  int n_ev, n_v, n_hv;
   int n_sync;
   double t_sync;  // host seconds blocked in stream synchronisation
   double t_start;
+  // split mode: Hessian products in another precision (hp != nullptr)
+  gbofdft_plan* hp;
+  const gbofdft_functional* hfn;
+  void* hf[H_NF];
 };
 
 static double now_s() {
@@ -155,6 +162,140 @@ static int ts_eval(TnState& s, const void* rho, void* pot, bool want_e) {
 
 template <typename T>
 static T* F(TnState& s, int i) { return reinterpret_cast<T*>(s.w.f[i]); }
+
+// Field pointers of the TN inner loop (get_direction_TN) in precision TH.
+// rb is the finite-difference base (V(phi) - mu) phi evaluated in TH; the
+// right-hand side is the outer residual.  In the single-precision-pair
+// ("split") mode the inner loop runs on TH copies; otherwise its fields are
+// the outer ones and rb is the outer residual itself.
+template <typename TH>
+struct DirFields {
+  TH *phi, *rb, *cgr, *cgp, *ap, *dir, *best, *phi1, *rho1, *pot1;
+};
+
+// TN direction (optimization.py:91-147) with Hessian products
+//   A p = ((V(phi + eps p) - mu)(phi + eps p) - rb) / eps
+// evaluated by `plan`/`fn` in precision TH; CG on A dir = -res0 (res0 in T).
+// The direction is left in F_P (precision T).
+template <typename T, typename TH>
+static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional* fn, const DirFields<TH>& d,
+                        double mu, double eps_fixed, double eps_rel, int maxfun) {
+  const int64_t N = s.p->N;
+  cudaStream_t st = s.st;
+  const Ws& w = s.w;
+  int rc;
+  const T* res0 = F<T>(s, F_RES0);
+  const bool split = (void*)d.phi != s.w.f[F_PHI];
+  TH* cgr = d.cgr;
+  TH* cgp = d.cgp;
+  TH* dir = d.dir;
+  TH* rb = d.rb;
+  const TH muH = (TH)mu;
+  if (split) {
+    // TH copy of phi and the finite-difference base at it
+    const T* phiT = F<T>(s, F_PHI);
+    TH* ph = d.phi;
+    TH* rho1 = d.rho1;
+    rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      const TH v = (TH)phiT[i];
+      ph[i] = v;
+      rho1[i] = v * v;
+    }, S_A, st);
+    if (rc) return rc;
+    ++s.n_hv;
+    if ((rc = gbofdft_eval(plan, rho1, fn, d.pot1, nullptr, GBOFDFT_CALC_V, st))) return rc;
+    TH* pot1 = d.pot1;
+    rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) { rb[i] = (pot1[i] - muH) * ph[i]; }, S_A, st);
+    if (rc) return rc;
+  }
+  {
+    TH* phic = d.phi;
+    rc = launch_mr<2, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      const TH r = -(TH)res0[i];
+      cgr[i] = r;
+      cgp[i] = r;
+      dir[i] = (TH)0;
+      c[0] = r * r;
+      c[1] = phic[i] * phic[i];
+    }, S_A, st);
+    if (rc) return rc;
+  }
+  if ((rc = ts_sync(s))) return rc;
+  double r0Norm = s.host[S_A];
+  const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
+  const double rConv = r0Norm * 0.1;
+  double rmin = 1e10;          // min(rLists) with rLists = [1e10]
+  double prev_min = 1e10;
+  bool use_best = false;
+  bool have_best = false;      // Best starts as the zero direction
+  double beta = 0.0;
+  for (int j = 0; j < maxfun; ++j) {
+    TH* phi = d.phi;
+    TH* phi1 = d.phi1;
+    TH* rho1 = d.rho1;
+    const TH eT = (TH)epsi, bT = (TH)beta;
+    const bool first = (j == 0);
+    rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      TH pv = cgp[i];
+      if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
+      const TH p1 = phi[i] + eT * pv;
+      phi1[i] = p1;
+      rho1[i] = p1 * p1;
+    }, S_A, st);
+    if (rc) return rc;
+    TH* pot1 = d.pot1;
+    if (split) ++s.n_hv; else ++s.n_v;
+    if ((rc = gbofdft_eval(plan, rho1, fn, pot1, nullptr, GBOFDFT_CALC_V, st))) return rc;
+    TH* ap = d.ap;
+    const TH inv_e = (TH)(1.0 / epsi);
+    rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      const TH a = ((pot1[i] - muH) * phi1[i] - rb[i]) * inv_e;
+      ap[i] = a;
+      c[0] = cgp[i] * a;
+    }, S_PAP, st);
+    if (rc) return rc;
+    const double* scd = w.sc;
+    const double r0c = r0Norm;
+    rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      const double pap = scd[S_PAP];
+      if (pap < 0.0) { c[0] = (TH)0; return; }
+      const TH alpha = (TH)(r0c / pap);
+      dir[i] += alpha * cgp[i];
+      const TH r = cgr[i] - alpha * ap[i];
+      cgr[i] = r;
+      c[0] = r * r;
+    }, S_R1, st);
+    if (rc) return rc;
+    if ((rc = ts_sync(s))) return rc;
+    const double pAp = s.host[S_PAP];
+    if (pAp < 0.0) {
+      if (j == 0) {
+        // direction = r0Norm / pAp * p
+        const TH sc = (TH)(r0Norm / pAp);
+        rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) { dir[i] = sc * cgp[i]; }, S_A, st);
+        if (rc) return rc;
+      }
+      break;
+    }
+    const double r1Norm = s.host[S_R1];
+    if (r1Norm < rmin) {
+      GB_CUDA(cudaMemcpyAsync(d.best, dir, sizeof(TH) * N, cudaMemcpyDeviceToDevice, st));
+      have_best = true;
+    }
+    prev_min = rmin;
+    if (r1Norm < rmin) rmin = r1Norm;
+    if (r1Norm < rConv) break;
+    if (r1Norm > 1000.0 * prev_min) { use_best = true; break; }
+    if (j > 10 && fabs(r0Norm - r1Norm) < 0.1 * r0Norm) { use_best = true; break; }
+    beta = r1Norm / r0Norm;
+    r0Norm = r1Norm;
+  }
+  // Best aliases the direction itself until the first improvement copies it
+  const TH* src = (use_best && have_best) ? d.best : dir;
+  T* p = F<T>(s, F_P);
+  rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) { p[i] = (T)src[i]; }, S_A, st);
+  return rc;
+}
 
 template <typename T>
 static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft_tn_result* res) {
@@ -234,96 +375,24 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   const double eps_rel = o.eps < 0 ? -o.eps : 0.0;
   for (it = 1; it < o.maxiter; ++it) {
     // ---- TN direction (optimization.py:91-147) -----------------------------
-    {
-      T* res0 = F<T>(s, F_RES0);
-      T* cgr = F<T>(s, F_CGR);
-      T* cgp = F<T>(s, F_CGP);
-      T* dir = F<T>(s, F_DIR);
-      T* phic = F<T>(s, F_PHI);
-      rc = launch_mr<2, T>(w, N, [=] __device__(int64_t i, T* c) {
-        const T r = -res0[i];
-        cgr[i] = r;
-        cgp[i] = r;
-        dir[i] = (T)0;
-        c[0] = r * r;
-        c[1] = phic[i] * phic[i];
-      }, S_A, st);
-      if (rc) return rc;
-      if ((rc = ts_sync(s))) return rc;
-      double r0Norm = s.host[S_A];
-      const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
-      const double rConv = r0Norm * 0.1;
-      double rmin = 1e10;          // min(rLists) with rLists = [1e10]
-      double prev_min = 1e10;
-      bool use_best = false;
-      bool have_best = false;      // Best starts as the zero direction
-      int j;
-      double beta = 0.0;
-      for (j = 0; j < o.maxfun; ++j) {
-        T* phi = F<T>(s, F_PHI);
-        T* phi1 = F<T>(s, F_PHI1);
-        T* rho1 = F<T>(s, F_TMP);
-        const T eT = (T)epsi, bT = (T)beta;
-        const bool first = (j == 0);
-        rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) {
-          T pv = cgp[i];
-          if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
-          const T p1 = phi[i] + eT * pv;
-          phi1[i] = p1;
-          rho1[i] = p1 * p1;
-        }, S_A, st);
-        if (rc) return rc;
-        T* pot1 = F<T>(s, F_POT1);
-        if ((rc = ts_eval(s, rho1, pot1, false))) return rc;
-        T* ap = F<T>(s, F_AP);
-        const T muT = (T)mu;
-        const T inv_e = (T)(1.0 / epsi);
-        rc = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
-          const T a = ((pot1[i] - muT) * phi1[i] - res0[i]) * inv_e;
-          ap[i] = a;
-          c[0] = cgp[i] * a;
-        }, S_PAP, st);
-        if (rc) return rc;
-        const double* scd = w.sc;
-        const double r0c = r0Norm;
-        rc = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {
-          const double pap = scd[S_PAP];
-          if (pap < 0.0) { c[0] = (T)0; return; }
-          const T alpha = (T)(r0c / pap);
-          dir[i] += alpha * cgp[i];
-          const T r = cgr[i] - alpha * ap[i];
-          cgr[i] = r;
-          c[0] = r * r;
-        }, S_R1, st);
-        if (rc) return rc;
-        if ((rc = ts_sync(s))) return rc;
-        const double pAp = s.host[S_PAP];
-        if (pAp < 0.0) {
-          if (j == 0) {
-            // direction = r0Norm / pAp * p
-            const T sc = (T)(r0Norm / pAp);
-            rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) { dir[i] = sc * cgp[i]; }, S_A, st);
-            if (rc) return rc;
-          }
-          break;
-        }
-        const double r1Norm = s.host[S_R1];
-        if (r1Norm < rmin) {
-          GB_CUDA(cudaMemcpyAsync(F<T>(s, F_BEST), dir, sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
-          have_best = true;
-        }
-        prev_min = rmin;
-        if (r1Norm < rmin) rmin = r1Norm;
-        if (r1Norm < rConv) break;
-        if (r1Norm > 1000.0 * prev_min) { use_best = true; break; }
-        if (j > 10 && fabs(r0Norm - r1Norm) < 0.1 * r0Norm) { use_best = true; break; }
-        beta = r1Norm / r0Norm;
-        r0Norm = r1Norm;
+    bool done_dir = false;
+    if constexpr (sizeof(T) == 8) {
+      if (s.hp) {
+        // split: FP64 residual, Hessian products in single precision
+        DirFields<float> d;
+        float** hf = reinterpret_cast<float**>(s.hf);
+        d.phi = hf[H_PHI]; d.rb = hf[H_RB]; d.cgr = hf[H_CGR]; d.cgp = hf[H_CGP]; d.ap = hf[H_AP];
+        d.dir = hf[H_DIR]; d.best = hf[H_BEST]; d.phi1 = hf[H_PHI1]; d.rho1 = hf[H_TMP]; d.pot1 = hf[H_POT1];
+        if ((rc = tn_direction<T, float>(s, s.hp, s.hfn, d, mu, eps_fixed, eps_rel, o.maxfun))) return rc;
+        done_dir = true;
       }
-      // Best aliases the direction itself until the first improvement copies it
-      if (use_best && have_best)
-        GB_CUDA(cudaMemcpyAsync(dir, F<T>(s, F_BEST), sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
-      GB_CUDA(cudaMemcpyAsync(F<T>(s, F_P), dir, sizeof(T) * N, cudaMemcpyDeviceToDevice, st));
+    }
+    if (!done_dir) {
+      DirFields<T> d;
+      d.phi = F<T>(s, F_PHI); d.rb = F<T>(s, F_RES0); d.cgr = F<T>(s, F_CGR); d.cgp = F<T>(s, F_CGP);
+      d.ap = F<T>(s, F_AP); d.dir = F<T>(s, F_DIR); d.best = F<T>(s, F_BEST); d.phi1 = F<T>(s, F_PHI1);
+      d.rho1 = F<T>(s, F_TMP); d.pot1 = F<T>(s, F_POT1);
+      if ((rc = tn_direction<T, T>(s, s.p, s.fn, d, mu, eps_fixed, eps_rel, o.maxfun))) return rc;
     }
     // ---- OrthogonalNormalization (optimization.py:204-225) -----------------
     double theta0 = 0.0, d0 = 0.0;
@@ -368,6 +437,13 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       if ((rc = orthonormalize())) return rc;
     }
     theta = fmin(theta0, theta);
+    // quadratic-model decrease of a Newton step along p: |g| theta0 / 2 with
+    // g = dE/dtheta at 0.  Below pred_stop the step cannot change the energy
+    // by more than the requested resolution: stop converged.
+    if (o.pred_stop > 0.0 && fabs(d0 * dV) * theta0 < o.pred_stop) {
+      converged = 0;
+      break;
+    }
     // ---- line search over the rotation angle (ValueAndDerivative) ----------
     Dcsrch ls;
     dcs_init(ls, o.c1, o.c2, o.xtol, 0.0, 3.14159265358979323846);
@@ -433,6 +509,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   res->n_iter = it;
   res->n_eval_ev = s.n_ev;
   res->n_eval_v = s.n_v;
+  res->n_eval_hess = s.n_hv;
   res->n_history = nh;
   res->n_sync = s.n_sync;
   res->t_sync = s.t_sync;
@@ -462,12 +539,42 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->xtol = 1e-12;
   o->ncheck = 2;
   o->eps = 0.0;
+  o->pred_stop = 0.0;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_tn_hess_workspace_bytes(const gbofdft_plan* hp, int64_t* bytes) {
+  GB_REQUIRE(hp && bytes, "tn_hess_workspace_bytes: null argument");
+  const size_t fb = ((gb_elem(hp) * (size_t)hp->N + 255) / 256) * 256;
+  *bytes = (int64_t)(fb * H_NF + 256);
   return GBOFDFT_OK;
 }
 
 int gbofdft_optimize_tn(gbofdft_plan* p, const gbofdft_functional* f, void* rho_io, const gbofdft_tn_options* o,
                         void* workspace, int64_t workspace_bytes, gbofdft_tn_result* res, void* stream) {
+  return gbofdft_optimize_tn_split(p, f, nullptr, nullptr, rho_io, o, workspace, workspace_bytes, nullptr, 0, res,
+                                   stream);
+}
+
+int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbofdft_plan* hp,
+                              const gbofdft_functional* hf, void* rho_io, const gbofdft_tn_options* o,
+                              void* workspace, int64_t workspace_bytes, void* hworkspace, int64_t hworkspace_bytes,
+                              gbofdft_tn_result* res, void* stream) {
   GB_REQUIRE(p && f && rho_io && o && workspace && res, "optimize_tn: null argument");
+  if (hp) {
+    GB_REQUIRE(hf && hworkspace, "optimize_tn_split: Hessian plan without functional or workspace");
+    GB_REQUIRE(p->prec == GBOFDFT_F64 && hp->prec == GBOFDFT_F32,
+               "optimize_tn_split: the outer plan must be FP64 and the Hessian plan FP32");
+    GB_REQUIRE(hp->n[0] == p->n[0] && hp->n[1] == p->n[1] && hp->n[2] == p->n[2] &&
+                   memcmp(hp->lattice, p->lattice, sizeof(p->lattice)) == 0 && hp->full == p->full,
+               "optimize_tn_split: the Hessian plan describes another grid");
+    int64_t hneed = 0;
+    gbofdft_tn_hess_workspace_bytes(hp, &hneed);
+    GB_REQUIRE(hworkspace_bytes >= hneed, "optimize_tn_split: Hessian workspace %lld bytes < %lld",
+               (long long)hworkspace_bytes, (long long)hneed);
+    GB_REQUIRE(((uintptr_t)hworkspace & 255) == 0, "optimize_tn_split: Hessian workspace must be 256-byte aligned");
+  }
+  GB_REQUIRE(o->pred_stop >= 0.0, "optimize_tn: pred_stop must be >= 0");
   int64_t need = 0;
   gbofdft_tn_workspace_bytes(p, &need);
   GB_REQUIRE(workspace_bytes >= need, "optimize_tn: workspace %lld bytes < %lld", (long long)workspace_bytes,
@@ -489,6 +596,13 @@ int gbofdft_optimize_tn(gbofdft_plan* p, const gbofdft_functional* f, void* rho_
   s.w.counter = reinterpret_cast<unsigned*>(s.w.sc + S_COUNT);
   GB_CUDA(cudaMemsetAsync(s.w.sc, 0, sizeof(double) * S_COUNT + 256, s.st));
   memset(res->energies, 0, sizeof(res->energies));
+  if (hp) {
+    s.hp = hp;
+    s.hfn = hf;
+    const size_t hb = ((gb_elem(hp) * (size_t)hp->N + 255) / 256) * 256;
+    char* hbase = reinterpret_cast<char*>(hworkspace);
+    for (int i = 0; i < H_NF; ++i) s.hf[i] = hbase + hb * i;
+  }
   return p->prec == GBOFDFT_F64 ? tn_run<double>(s, rho_io, *o, res) : tn_run<float>(s, rho_io, *o, res);
 }
 

@@ -10,6 +10,11 @@ Added option ``precision``: "fp64" (default for float64 densities, the
 reference's arithmetic), "fp32", or "mixed" (FP32 fields and transforms until
 the FP32 energy stops resolving progress, then FP64 iterations from that
 density to the requested ``econv``).  Reductions are FP64 in every mode.
+In the FP64 refinement of "mixed", ``refine="split"`` (default) evaluates
+the Hessian-vector products of the inner CG loop in FP32
+(``gbofdft_optimize_tn_split``) and stops once the model decrease of the next
+Newton step is below ``refine_pred_stop`` (default econv / 10);
+``refine="fp64"`` runs the plain FP64 TN to ``econv``.
 """
 import ctypes
 import time
@@ -40,6 +45,8 @@ DEFAULTS = {
     "fp32_econv": None,
     "fp32_eps": -1.0e-3,
     "refine_maxls": 10,
+    "refine": "split",
+    "refine_pred_stop": None,
 }
 
 
@@ -74,7 +81,7 @@ class Optimization:
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
-    def _run(self, rho, econv, eps, maxiter, maxls=None):
+    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -88,6 +95,7 @@ class Optimization:
         opts.c1, opts.c2, opts.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
         opts.ncheck = int(o["ncheck"])
         opts.eps = float(eps)
+        opts.pred_stop = float(pred_stop)
         spec = self.EnergyEvaluator.spec(rho)
         f = spec.ctypes()
         nb = ctypes.c_int64()
@@ -98,12 +106,24 @@ class Optimization:
         hist = (ctypes.c_double * 4096)()
         res.history = hist
         res.history_cap = 4096
-        _lib.check(L.gbofdft_optimize_tn(plan.handle, ctypes.byref(f), _lib.ptr(r), ctypes.byref(opts),
-                                         _lib.aligned_ptr(ws, 256), int(nb.value), ctypes.byref(res),
-                                         _lib.stream_ptr()), "optimize_tn")
+        if hess_rho is None:
+            _lib.check(L.gbofdft_optimize_tn(plan.handle, ctypes.byref(f), _lib.ptr(r), ctypes.byref(opts),
+                                             _lib.aligned_ptr(ws, 256), int(nb.value), ctypes.byref(res),
+                                             _lib.stream_ptr()), "optimize_tn")
+        else:
+            hplan = grid.plan(hess_rho.dtype)
+            hf = self.EnergyEvaluator.spec(hess_rho).ctypes()
+            hb = ctypes.c_int64()
+            _lib.check(L.gbofdft_tn_hess_workspace_bytes(hplan.handle, ctypes.byref(hb)))
+            hws = _workspace(grid, ("hess", hess_rho.dtype), int(hb.value))
+            _lib.check(L.gbofdft_optimize_tn_split(
+                plan.handle, ctypes.byref(f), hplan.handle, ctypes.byref(hf), _lib.ptr(r), ctypes.byref(opts),
+                _lib.aligned_ptr(ws, 256), int(nb.value), _lib.aligned_ptr(hws, 256), int(hb.value),
+                ctypes.byref(res), _lib.stream_ptr()), "optimize_tn_split")
         out = dict(energy=res.energy, mu=res.mu, converged=res.converged, n_iter=res.n_iter,
-                   n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, energies=list(res.energies),
-                   history=[hist[i] for i in range(res.n_history)], n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total)
+                   n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, n_eval_hess=res.n_eval_hess,
+                   energies=list(res.energies), history=[hist[i] for i in range(res.n_history)],
+                   n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total)
         return DirectField(grid, data=r), out
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):
@@ -142,7 +162,14 @@ class Optimization:
             n_in = float(rho.as_subclass(torch.Tensor).to(torch.float64).sum())
             n_out = float(r64.as_subclass(torch.Tensor).sum())
             r64 = r64 * (n_in / n_out)
-            r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"])
+            if o["refine"] == "split":
+                ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.1 * o["econv"]
+                r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
+                                   hess_rho=r32, pred_stop=ps)
+            elif o["refine"] == "fp64":
+                r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"])
+            else:
+                raise ValueError("refine must be 'split' or 'fp64', got %r" % (o["refine"],))
             self.stats["stages"].append(dict(precision="fp64", **out))
             # a refinement whose line search stops on FP64 rounding (no energy
             # change above econv along the last direction) sits at the FP64

@@ -306,6 +306,9 @@ typedef struct gbofdft_tn_options {
   double eps;    /* finite-difference step of the Hessian product: > 0 fixed
                     (the reference uses 1e-9), < 0 relative: |eps| ||phi|| / ||r0||
                     per TN direction (single precision), 0 -> 1e-9 */
+  double pred_stop; /* > 0: stop converged when the quadratic-model energy
+                       decrease of the next Newton step, |dE/dtheta| theta0 / 2,
+                       is below it (no reference counterpart); 0: off */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {
@@ -322,6 +325,7 @@ typedef struct gbofdft_tn_result {
   int n_sync;             /* host synchronisations performed */
   double t_sync;          /* host seconds spent waiting in them (scalar read-backs) */
   double t_total;         /* host seconds in gbofdft_optimize_tn */
+  int n_eval_hess;        /* potential evaluations in the Hessian plan (split mode) */
 } gbofdft_tn_result;
 
 int gbofdft_tn_options_default(gbofdft_tn_options* opts);
@@ -341,6 +345,24 @@ int gbofdft_tn_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
 int gbofdft_optimize_tn(gbofdft_plan* plan, const gbofdft_functional* f, void* rho_io,
                         const gbofdft_tn_options* opts, void* workspace, int64_t workspace_bytes,
                         gbofdft_tn_result* result, void* stream);
+
+/* Bytes of device workspace gbofdft_optimize_tn_split needs for its Hessian plan. */
+int gbofdft_tn_hess_workspace_bytes(const gbofdft_plan* hplan, int64_t* bytes);
+
+/*
+ * gbofdft_optimize_tn with the Hessian-vector products of the inner CG loop
+ * evaluated by a second, single-precision plan and functional on the same
+ * grid (hplan FP32, plan FP64): residual, orthonormalisation, line search and
+ * convergence test stay in FP64, each TN direction costs one FP32 base
+ * evaluation plus one FP32 evaluation per CG step.  opts->eps applies to the
+ * FP32 products (use a relative step, eps < 0).  hplan == NULL is
+ * gbofdft_optimize_tn.  No reference counterpart: a precision split of
+ * Optimization.optimize_rho's TN (optimization.py:91-147, 281-520).
+ */
+int gbofdft_optimize_tn_split(gbofdft_plan* plan, const gbofdft_functional* f, gbofdft_plan* hplan,
+                              const gbofdft_functional* hf, void* rho_io, const gbofdft_tn_options* opts,
+                              void* workspace, int64_t workspace_bytes, void* hworkspace, int64_t hworkspace_bytes,
+                              gbofdft_tn_result* result, void* stream);
 
 /*
  * One call of the More-Thuente line-search state machine (host only).

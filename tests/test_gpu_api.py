@@ -200,12 +200,27 @@ def test_tn_al256_wt_matches_reference_solve(api, golden):
     assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
 
 
-def test_tn_al4_mixed_precision(api, golden):
+@pytest.mark.parametrize("refine", ["split", "fp64"])
+def test_tn_al4_mixed_precision(api, golden, refine):
     a = golden("al4")
     st = systems.config_al4(0)
-    opt, rho, total = _solve(api, st, "TFVW", 1e-7, precision="mixed")
+    opt, rho, total = _solve(api, st, "TFVW", 1e-7, precision="mixed", refine=refine)
+    last = opt.stats["stages"][-1]
+    assert (last["n_eval_hess"] > 0) == (refine == "split")
     E = total.Energy(rho.to(api["torch"].float64))
     # 1e-5 eV/atom of the FP64 reference solve
+    assert abs(E - float(a["E_final"])) < 1e-5 / 27.211386 * st.nat
+    assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
+
+
+def test_tn_al256_mixed_split_refine(api, golden):
+    """256 Al, 128^3, WT: FP32 TN then FP64 refinement with FP32 Hessian
+    products; energy within 1e-5 eV/atom and forces within 1e-5 Ha/Bohr of the
+    reference's FP64 solve."""
+    a = golden("al256")
+    st = systems.config_al256(0)
+    opt, rho, total = _solve(api, st, "WT", 1e-7, precision="mixed")
+    E = total.Energy(rho)
     assert abs(E - float(a["E_final"])) < 1e-5 / 27.211386 * st.nat
     assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
 

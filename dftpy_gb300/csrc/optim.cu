@@ -10,6 +10,8 @@
 // order with compensated FP64 arithmetic), so results are deterministic.
 // Scalars cross to the host once per evaluation (one small D2H copy).
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
@@ -139,6 +141,7 @@ struct TnState {
   gbofdft_plan* hp;
   const gbofdft_functional* hfn;
   void* hf[H_NF];
+  bool verbose;   // GBOFDFT_TN_VERBOSE=1: per-iteration trace on stderr
 };
 
 static double now_s() {
@@ -222,6 +225,8 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
   }
   if ((rc = ts_sync(s))) return rc;
   double r0Norm = s.host[S_A];
+  const double r0_first = r0Norm;
+  int jend = 0;
   const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
   const double rConv = r0Norm * 0.1;
   double rmin = 1e10;          // min(rLists) with rLists = [1e10]
@@ -230,6 +235,7 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
   bool have_best = false;      // Best starts as the zero direction
   double beta = 0.0;
   for (int j = 0; j < maxfun; ++j) {
+    jend = j + 1;
     TH* phi = d.phi;
     TH* phi1 = d.phi1;
     TH* rho1 = d.rho1;
@@ -290,6 +296,9 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     beta = r1Norm / r0Norm;
     r0Norm = r1Norm;
   }
+  if (s.verbose)
+    fprintf(stderr, "[gbofdft tn]   cg %s steps %d r0 %.3e rmin %.3e eps %.3e best %d\n", split ? "split" : "same",
+            jend, r0_first, rmin, epsi, (int)(use_best && have_best));
   // Best aliases the direction itself until the first improvement copies it
   const TH* src = (use_best && have_best) ? d.best : dir;
   T* p = F<T>(s, F_P);
@@ -476,7 +485,13 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       fval = s.host[S_EN + GB_E_TOTAL];
       gval = 2.0 * s.host[S_A] * dV;
       accepted = true;
+      if (s.verbose)
+        fprintf(stderr, "[gbofdft tn] it %d ls %d stp %.6e f %.12f df %.3e g %.6e task %d\n", it, nls, stp, fval,
+                fval - energy, gval, task);
     }
+    if (s.verbose)
+      fprintf(stderr, "[gbofdft tn] it %d E %.12f d0*dV %.6e theta0 %.6e theta %.6e ls_end task %d nls %d\n", it,
+              energy, d0 * dV, theta0, theta, task, nls);
     if (nls >= o.maxls || task == DCS_WARN || task == DCS_ERROR || !accepted) {
       converged = 1;  // line search failed (optimization.py:440-444)
       break;
@@ -588,6 +603,10 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
   s.fn = f;
   s.st = (cudaStream_t)stream;
   s.t_start = now_s();
+  {
+    const char* v = getenv("GBOFDFT_TN_VERBOSE");
+    s.verbose = v && v[0] == '1';
+  }
   const size_t fb = ((gb_elem(p) * (size_t)p->N + 255) / 256) * 256;
   char* base = reinterpret_cast<char*>(workspace);
   for (int i = 0; i < F_NF; ++i) s.w.f[i] = base + fb * i;

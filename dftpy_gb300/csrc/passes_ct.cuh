@@ -38,22 +38,34 @@ template <typename T, int N> struct ColsCfg {     // columns per tile
   static constexpr int TB = (sizeof(T) == 4 && N <= 256) ? 16 : 8;
 };
 
+// A scalar kernel parameter in both precisions, converted on the host: the
+// FP32 kernels then run without double->float conversions, which execute on
+// the FP64 pipe (a slow one on this part).
+struct Sc {
+  double d;
+  float f;
+  void set(double v) { d = v; f = (float)v; }
+};
+template <typename T> __device__ __forceinline__ T sc(const Sc& s) {
+  if constexpr (sizeof(T) == 8) return s.d; else return s.f;
+}
+
 // ---- pointwise functions -----------------------------------------------------
 // x^(1/2), x^(5/6) and friends for x >= 1e-30 (the reference's clamps)
 template <typename T> __device__ __forceinline__ T sqrt_pos(T x) { return x * rsqrt_d(x); }
 
-template <typename T> __device__ __forceinline__ T pow_beta_ct(T x, double beta) {
-  if (fabs(beta - 5.0 / 6.0) < 1e-15) {
+template <typename T> __device__ __forceinline__ T pow_beta_ct(T x, bool b56, T beta) {
+  if (b56) {
     const T z3 = rcbrt_d(x), z2 = rsqrt_d(x);
     return (x * z2) * (x * z3 * z3);         // x^(1/2) x^(1/3)
   }
-  return pow(x, (T)beta);
+  return pow(x, beta);
 }
 
 template <typename T>
-__device__ __forceinline__ T prologue_ct(int op, T rho, double beta) {
+__device__ __forceinline__ T prologue_ct(int op, T rho, bool b56, T beta) {
   if (op == OP_SQRT) return sqrt_pos<T>(rho > (T)0 ? rho : (T)kZero);
-  if (op == OP_POWB) return pow_beta_ct<T>(rho < (T)kZero ? (T)kZero : rho, beta);
+  if (op == OP_POWB) return pow_beta_ct<T>(rho < (T)kZero ? (T)kZero : rho, b56, beta);
   return rho;
 }
 
@@ -66,7 +78,8 @@ struct CtRowsFwd {
   int64_t fstride;
   int nrows, ld2, nf;
   int op[GB_MAX_FIELDS];
-  double beta, scale;
+  int b56;            // beta == 5/6
+  Sc beta, half;      // half = scale / 2
   const void* tw;
 };
 
@@ -89,19 +102,21 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_fwd(CtRows
     R[idx] = row < a.nrows ? __ldg(in + row * N + idx % N) : (T)0;
   }
   __syncthreads();
+  const bool b56 = a.b56 != 0;
+  const T beta = sc<T>(a.beta);
   for (int idx = tid; idx < nl * N; idx += blockDim.x) {
     const int line = idx / N, j = idx % N;
     const int f = line / RP, l2 = line % RP;
     const int op = a.op[f];
     const int64_t ra = base + 2 * l2;
-    const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], a.beta) : (T)0;
-    const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], a.beta) : (T)0;
+    const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], b56, beta) : (T)0;
+    const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], b56, beta) : (T)0;
     A[sw<T, NP>(line, j)] = cpx<T>{x0, x1};
   }
   __syncthreads();
   cpx<T>* res = fft<-1, T, N>(A, B, tw, l, lane, true);
   cpx<T>* out = reinterpret_cast<cpx<T>*>(a.out);
-  const T half = (T)(0.5 * a.scale);
+  const T half = sc<T>(a.half);
   for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
     const int line = idx / NH, k = idx % NH;
     const int f = line / RP, l2 = line % RP;
@@ -123,8 +138,10 @@ struct CtRowsInv {
   const void* tw;
   void* out;
   int64_t ostride;
-  double scale;
+  Sc scale;
   EvalDesc ev;
+  Sc tf_v, tf_e, vw_y, two_alpha, inv_two_alpha, wt_beta;  // evaluation constants
+  int b56;
   const void* rho;
   const void* vloc;
   void* pot;
@@ -171,7 +188,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_store(
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
   cpx<T>* res = ct_rows_inv_lines<T, N>(a, base, tw, A, B);
   T* out = reinterpret_cast<T*>(a.out);
-  const T s = (T)a.scale;
+  const T s = sc<T>(a.scale);
   for (int idx = tid; idx < a.nf * 2 * RP * N; idx += blockDim.x) {
     const int f = idx / (2 * RP * N), r = idx % (2 * RP * N);
     const int rr = r / N, j = r % N;
@@ -211,7 +228,10 @@ __device__ __forceinline__ void pz_lda_ct(T rho, T& eps, T& pot, bool want_e) {
   }
 }
 
-template <typename T, int N>
+// WANT_E is a template parameter so the potential-only instantiation holds no
+// FP64 accumulation at all (if-converted, never-taken FP64 code still
+// occupies the FP64 pipe).
+template <typename T, int N, bool WANT_E>
 __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(CtRowsInv a) {
   constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -229,10 +249,14 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
   const T* rhop = reinterpret_cast<const T*>(a.rho);
   const T* vlocp = reinterpret_cast<const T*>(a.vloc);
   T* potp = reinterpret_cast<T*>(a.pot);
-  const bool want_e = a.calc_e != 0;
-  const T ctf = (T)2.87123400018819181594;               // (3/10)(3 pi^2)^(2/3)
-  const T alpha = (T)ev.wt_alpha;
-  const bool b56 = fabs(ev.wt_beta - 5.0 / 6.0) < 1e-15;
+  constexpr bool want_e = WANT_E;
+  const T tf_v = sc<T>(a.tf_v);             // (5/3) C_TF x
+  const T tf_e = sc<T>(a.tf_e);             // C_TF x
+  const T vw_y = sc<T>(a.vw_y);
+  const T two_alpha = sc<T>(a.two_alpha);
+  const T inv_two_alpha = sc<T>(a.inv_two_alpha);
+  const T wt_beta = sc<T>(a.wt_beta);
+  const bool b56 = a.b56 != 0;
   double es[6] = {0, 0, 0, 0, 0, 0};
   for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
     const int rr = idx / N, j = idx % N;
@@ -251,12 +275,12 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
       T r23;                                              // cbrt(rho^2)
       if (pos) r23 = rho * z3;
       else r23 = cbrt(rho * rho);
-      pot += (T)(5.0 / 3.0) * ctf * r23 * (T)ev.tf_x;
+      pot += tf_v * r23;
       if (want_e) {
         T r53;                                            // cbrt(rho^5)
         if (pos) r53 = rho * rho * z3;
         else { T r5 = rho * rho; r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho; r53 = cbrt(r5); }
-        es[0] += (double)(r53 * ctf) * ev.tf_x;
+        es[0] += (double)(r53 * tf_e);
       }
     }
     if (ev.vw) {
@@ -265,8 +289,8 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
       // 1 / max(sqrt(rho_m), 1e-30), rho_m = rho if rho > 0 else 1e-30
       const T inv_sq = pos ? z2 : (rho > (T)0 ? (T)1 / fmax(sqrt(rho), (T)kZero) : (T)1e15);
       const T v = (T)0.5 * w * inv_sq;
-      pot += v * (T)ev.vw_y;
-      if (want_e && rho > (T)0) es[1] += (double)(rho * v) * ev.vw_y;
+      pot += v * vw_y;
+      if (want_e && rho > (T)0) es[1] += (double)(rho * v * vw_y);
     }
     if (ev.wt) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_wt * RP + pr, j)];
@@ -277,11 +301,11 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
         else { const T rc = (T)kZero; rb_over_rc = sqrt(rc) * cbrt(rc) / rc; }
       } else {
         const T rc = rho < (T)kZero ? (T)kZero : rho;
-        rb_over_rc = pow(rc, (T)ev.wt_beta) / rc;
+        rb_over_rc = pow(rc, wt_beta) / rc;
       }
-      const T v = (T)2 * alpha * rb_over_rc * kc;
+      const T v = two_alpha * rb_over_rc * kc;
       pot += v;
-      if (want_e) es[2] += (double)(v * rho / ((T)2 * alpha));
+      if (want_e) es[2] += (double)(v * rho * inv_two_alpha);
     }
     if (ev.xc) {
       T eps, vx;
@@ -302,7 +326,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
     }
     potp[gidx] = pot;
   }
-  if (!want_e) return;
+  if constexpr (!WANT_E) return;
   __shared__ double red[32][6];
   const int lane32 = tid & 31, warp = tid >> 5;
 #pragma unroll
@@ -326,10 +350,28 @@ struct CtCols {
   int64_t fstride, stride, ostride;
   int ncols;
   const void* tw;
-  double scale;
+  Sc scale;
+  Sc coef[GB_MAX_FIELDS];
+  float bgf[9];        // reciprocal lattice rows in FP32 (FP32 convolution)
   GInfo gi;
   KerDesc kd;
 };
+
+// General kernel value (Nyquist partner averaging; FP64 geometry), kept out
+// of line so the FP32 fast loop is not if-converted into it.
+template <typename T>
+__device__ __noinline__ T kernel_value_slow(const GInfo& g, int type, const void* arr, int i0, int i1, int k2) {
+  return gbk::kernel_value<T>(g, type, arr, i0, i1, k2);
+}
+
+// FP32 |G|^2 along an axis-0 column: gg(m0) = (qa m0 + qb) m0 + qd with
+// qa = |b0|^2, qb = 2 b0.u, qd = |u|^2, u = m1 b1 + m2 b2 (one column).
+__device__ __forceinline__ void col_quadratic(const float* bg, float m1, float m2, float& qa, float& qb, float& qd) {
+  const float ux = m1 * bg[3] + m2 * bg[6], uy = m1 * bg[4] + m2 * bg[7], uz = m1 * bg[5] + m2 * bg[8];
+  qa = bg[0] * bg[0] + bg[1] * bg[1] + bg[2] * bg[2];
+  qb = 2.0f * (bg[0] * ux + bg[1] * uy + bg[2] * uz);
+  qd = ux * ux + uy * uy + uz * uz;
+}
 
 template <typename T, int N, int DIR, bool CONV>
 __global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB) k_ct_cols(CtCols a) {
@@ -356,20 +398,63 @@ __global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB) k_ct_cols(C
   } else {
     res = fft<-1, T, N>(A, B, tw, l, lane, true);
     const int type = a.kd.type[f];
-    const T coef = (T)a.kd.coef[f];
+    const T coef = sc<T>(a.coef[f]);
     const void* arr = a.kd.arr[f];
-    for (int idx = tid; idx < N * TB; idx += blockDim.x) {
-      const int c = idx % TB, j = idx / TB;
-      if (c >= nc) continue;
-      const T kv = gbk::kernel_value<T>(a.gi, type, arr, j, outer, c0 + c) * coef;
-      const int p = sw<T, NP>(c, j);
-      res[p] = c_scale(res[p], kv);
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (type == KER_HARTREE || type == KER_G2) {
+        // axis-0 line: i0 = j varies, i1 = outer, k2 = c0 + c.  |G|^2 from a
+        // per-column quadratic in m0 (no per-element conversions); points on
+        // a Nyquist plane take the partner-averaged general path.
+        __shared__ float s_m0[N];
+        __shared__ float s_qa[TB], s_qb[TB], s_qd[TB];
+        __shared__ int s_sym[TB];
+        const GInfo& g = a.gi;
+        for (int j = tid; j < N; j += blockDim.x) s_m0[j] = (float)gbk::ffreq(j, N);
+        if (tid < TB) {
+          const int k2 = c0 + tid;
+          const float m1 = (float)gbk::ffreq(outer, g.n1);
+          const float m2 = (float)(g.full ? gbk::ffreq(k2, g.n2) : k2);
+          col_quadratic(a.bgf, m1, m2, s_qa[tid], s_qb[tid], s_qd[tid]);
+          const bool plane = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
+          const bool nyq = ((g.n1 & 1) == 0 && 2 * outer == g.n1) || (g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2);
+          s_sym[tid] = plane ? (nyq ? 2 : 1) : 0;   // 2: every point, 1: only i0 = n0/2
+        }
+        __syncthreads();
+        const bool hart = type == KER_HARTREE;
+        const T fourpi_c = (T)(4.0f * 3.14159265358979323846f) * coef;
+        for (int idx = tid; idx < N * TB; idx += blockDim.x) {
+          const int c = idx % TB, j = idx / TB;
+          if (c >= nc) continue;
+          const int sy = s_sym[c];
+          T kv;
+          if (sy == 2 || (sy == 1 && (N & 1) == 0 && 2 * j == N)) {
+            kv = kernel_value_slow<T>(g, type, arr, j, outer, c0 + c) * coef;
+          } else {
+            const float m0 = s_m0[j];
+            const float gg = (s_qa[c] * m0 + s_qb[c]) * m0 + s_qd[c];
+            kv = hart ? (gg > 0.0f ? fourpi_c / gg : 0.0f) : gg * coef;
+          }
+          const int p = sw<T, NP>(c, j);
+          res[p] = c_scale(res[p], kv);
+        }
+        done = true;
+      }
+    }
+    if (!done) {
+      for (int idx = tid; idx < N * TB; idx += blockDim.x) {
+        const int c = idx % TB, j = idx / TB;
+        if (c >= nc) continue;
+        const T kv = gbk::kernel_value<T>(a.gi, type, arr, j, outer, c0 + c) * coef;
+        const int p = sw<T, NP>(c, j);
+        res[p] = c_scale(res[p], kv);
+      }
     }
     __syncthreads();
     cpx<T>* other = (res == A) ? B : A;
     res = fft<1, T, N>(res, other, tw, l, lane, true);
   }
-  const T s = (T)a.scale;
+  const T s = sc<T>(a.scale);
   for (int idx = tid; idx < N * TB; idx += blockDim.x) {
     const int c = idx % TB, j = idx / TB;
     if (c < nc) base[(int64_t)j * a.stride + c] = c_scale(res[sw<T, NP>(c, j)], s);
@@ -402,7 +487,10 @@ int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, in
     a.in = in; a.out = spec; a.fstride = fstride;
     a.nrows = p->n[0] * p->n[1]; a.ld2 = ld2; a.nf = nf;
     for (int f = 0; f < GB_MAX_FIELDS; ++f) a.op[f] = f < nf ? ops[f] : OP_RHO;
-    a.beta = beta; a.scale = scale; a.tw = p->tw[2];
+    a.b56 = fabs(beta - 5.0 / 6.0) < 1e-15;
+    a.beta.set(beta);
+    a.half.set(0.5 * scale);
+    a.tw = p->tw[2];
     const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP) + sizeof(T) * 2 * RP * N;
     if ((rc = ct_smem(k_ct_rows_fwd<T, N>, sm))) return;
     const int nblk = (a.nrows + 2 * RP - 1) / (2 * RP);
@@ -425,15 +513,28 @@ int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int
     CtRowsInv a;
     memset(&a, 0, sizeof(a));
     a.in = spec; a.fstride = fstride; a.nrows = p->n[0] * p->n[1]; a.ld2 = ld2; a.nf = nf; a.tw = p->tw[2];
-    a.out = out; a.ostride = ostride; a.scale = scale;
+    a.out = out; a.ostride = ostride; a.scale.set(scale);
     const int nblk = (a.nrows + 2 * RP - 1) / (2 * RP);
     if (nblk_out) *nblk_out = nblk;
     if (ev) {
       a.ev = *ev; a.rho = rho; a.vloc = vloc; a.pot = pot; a.calc_e = calc_e; a.partials = partials;
+      const double ctf = 2.87123400018819181594;    // (3/10)(3 pi^2)^(2/3)
+      a.tf_v.set(5.0 / 3.0 * ctf * ev->tf_x);
+      a.tf_e.set(ctf * ev->tf_x);
+      a.vw_y.set(ev->vw_y);
+      a.two_alpha.set(2.0 * ev->wt_alpha);
+      a.inv_two_alpha.set(ev->wt_alpha != 0.0 ? 1.0 / (2.0 * ev->wt_alpha) : 0.0);
+      a.wt_beta.set(ev->wt_beta);
+      a.b56 = fabs(ev->wt_beta - 5.0 / 6.0) < 1e-15;
       const int nfl = nf > 0 ? nf : 1;
       const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nfl * RP * NP);
-      if ((rc = ct_smem(k_ct_rows_inv_eval<T, N>, sm))) return;
-      k_ct_rows_inv_eval<T, N><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+      if (calc_e) {
+        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, true>, sm))) return;
+        k_ct_rows_inv_eval<T, N, true><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+      } else {
+        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, false>, sm))) return;
+        k_ct_rows_inv_eval<T, N, false><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+      }
     } else {
       const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP);
       if ((rc = ct_smem(k_ct_rows_inv_store<T, N>, sm))) return;
@@ -458,9 +559,13 @@ int ct_cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int
     a.data = spec; a.fstride = fstride;
     a.stride = axis == 1 ? ld2 : (int64_t)p->n[1] * ld2;
     a.ostride = axis == 1 ? (int64_t)p->n[1] * ld2 : ld2;
-    a.ncols = p->n2h; a.tw = p->tw[axis]; a.scale = scale;
+    a.ncols = p->n2h; a.tw = p->tw[axis]; a.scale.set(scale);
     a.gi = p->gi;
-    if (kd) a.kd = *kd;
+    for (int i = 0; i < 9; ++i) a.bgf[i] = (float)p->bg[i];
+    if (kd) {
+      a.kd = *kd;
+      for (int f = 0; f < GB_MAX_FIELDS; ++f) a.coef[f].set(kd->coef[f]);
+    }
     const size_t sm = sizeof(cpx<T>) * (N + 2 * TB * NP);
     if ((rc = ct_smem(k_ct_cols<T, N, DIR, CONV>, sm))) return;
     dim3 grid((p->n2h + TB - 1) / TB, p->n[axis == 1 ? 0 : 1], nf);

@@ -48,6 +48,23 @@ def rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def rank_seed(rank):
+    """Each rank solves its own snapshot (weak scaling): seed = rank."""
+    return int(rank)
+
+
+def max_over_ranks(x, world, device="cuda"):
+    """Step time of the whole job: the maximum over ranks (one all-reduce,
+    outside the timed region; the only collective of the benchmark)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi samples of the SM clock and throttle reasons during a region."""
@@ -314,8 +331,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import __graft_entry__
     __graft_entry__.build()
-    seed = rank
-    st, grid, total, rho0 = build_system(seed)
+    st, grid, total, rho0 = build_system(rank_seed(rank))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     n_evals_ref, e_golden = golden_evals()
     # FP64 reference energy for this snapshot (plain GPU path; rank 0 also
@@ -333,12 +349,7 @@ def main():
     if rank == 0 and e_golden is not None:
         e_ref = e_golden
     err = None if e_ref is None else max(abs(e - e_ref) for e in energies) * HA_EV / st.nat
-    t_step = statistics.mean(times)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(statistics.mean(times), world)
     t_eval, b_eval = eval_roofline(total, rho0)
     peak, peak_kind = measured_peaks()
     achieved = b_eval / t_eval / 1e9

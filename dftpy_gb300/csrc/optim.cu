@@ -485,6 +485,19 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       fval = s.host[S_EN + GB_E_TOTAL];
       gval = 2.0 * s.host[S_A] * dV;
       accepted = true;
+      // energy change below the evaluation's resolution: the sufficient-
+      // decrease test cannot be decided, the derivative (computed from the
+      // potential, not from energy differences) still can -- accept a step
+      // that has reduced |dE/dtheta| enough.
+      if (o.eres > 0.0 && fabs(fval - energy) <= o.eres * fmax(1.0, fabs(energy)) &&
+          fabs(gval) <= o.c2 * fabs(2.0 * d0 * dV)) {
+        task = DCS_CONV;
+        if (s.verbose)
+          fprintf(stderr, "[gbofdft tn] it %d ls %d stp %.6e accepted at energy resolution (df %.3e g %.3e)\n", it,
+                  nls, stp, fval - energy, gval);
+        ++nls;
+        break;
+      }
       if (s.verbose)
         fprintf(stderr, "[gbofdft tn] it %d ls %d stp %.6e f %.12f df %.3e g %.6e task %d\n", it, nls, stp, fval,
                 fval - energy, gval, task);
@@ -555,6 +568,7 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->ncheck = 2;
   o->eps = 0.0;
   o->pred_stop = 0.0;
+  o->eres = 0.0;
   return GBOFDFT_OK;
 }
 

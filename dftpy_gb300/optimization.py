@@ -47,6 +47,12 @@ DEFAULTS = {
     "refine_maxls": 10,
     "refine": "split",
     "refine_pred_stop": None,
+    # relative energy resolution of the evaluations, for the line-search
+    # acceptance on the derivative (mixed precision only): the PZ81 LDA is
+    # discontinuous at r_s = 1, which makes E(theta) jump by ~1e-10 |E| over
+    # tiny steps in FP64; FP32 fields add their own rounding
+    "refine_eres": 3e-10,
+    "fp32_eres": 1e-7,
 }
 
 
@@ -81,7 +87,7 @@ class Optimization:
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
-    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0):
+    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -96,6 +102,7 @@ class Optimization:
         opts.ncheck = int(o["ncheck"])
         opts.eps = float(eps)
         opts.pred_stop = float(pred_stop)
+        opts.eres = float(eres)
         spec = self.EnergyEvaluator.spec(rho)
         f = spec.ctypes()
         nb = ctypes.c_int64()
@@ -153,7 +160,8 @@ class Optimization:
             # search stops resolving progress
             nat = self._natoms()
             e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
-            r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"])
+            r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"],
+                                   pred_stop=0.1 * e32, eres=o["fp32_eres"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
             # the FP32 stage conserves the electron number only to single
@@ -165,9 +173,10 @@ class Optimization:
             if o["refine"] == "split":
                 ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.1 * o["econv"]
                 r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
-                                   hess_rho=r32, pred_stop=ps)
+                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"])
             elif o["refine"] == "fp64":
-                r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"])
+                r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
+                                   eres=o["refine_eres"])
             else:
                 raise ValueError("refine must be 'split' or 'fp64', got %r" % (o["refine"],))
             self.stats["stages"].append(dict(precision="fp64", **out))

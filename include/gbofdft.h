@@ -309,6 +309,10 @@ typedef struct gbofdft_tn_options {
   double pred_stop; /* > 0: stop converged when the quadratic-model energy
                        decrease of the next Newton step, |dE/dtheta| theta0 / 2,
                        is below it (no reference counterpart); 0: off */
+  double eres;      /* > 0: relative energy resolution of the evaluation; a
+                       line-search trial whose energy change is below
+                       eres max(1, |E|) is accepted when |dE/dtheta| <= c2 |dE/dtheta(0)|
+                       (no reference counterpart); 0: off (the reference's test) */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {

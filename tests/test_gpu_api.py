@@ -218,11 +218,14 @@ def test_tn_al256_mixed_split_refine(api, golden):
     products; energy within 1e-5 eV/atom and forces within 1e-5 Ha/Bohr of the
     reference's FP64 solve."""
     a = golden("al256")
+    t = golden("al256_tight")      # the reference's solve converged to econv 1e-10
     st = systems.config_al256(0)
     opt, rho, total = _solve(api, st, "WT", 1e-7, precision="mixed")
     E = total.Energy(rho)
     assert abs(E - float(a["E_final"])) < 1e-5 / 27.211386 * st.nat
-    assert np.abs(total.get_forces(rho) - a["forces"]).max() < 1e-5
+    F = total.get_forces(rho)
+    assert np.abs(F - a["forces"]).max() < 1e-5
+    assert np.abs(F - t["forces"]).max() < 1e-5
 
 
 @pytest.mark.parametrize("interp", ["linear", "hermite"])

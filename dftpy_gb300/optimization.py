@@ -53,6 +53,10 @@ DEFAULTS = {
     # tiny steps in FP64; FP32 fields add their own rounding
     "refine_eres": 3e-10,
     "fp32_eres": 1e-7,
+    # energy-change checks per stage of "mixed": a stage ends after one
+    # accepted step below its threshold (its next direction would be
+    # discarded by the model-decrease stop)
+    "stage_ncheck": 1,
 }
 
 
@@ -87,7 +91,7 @@ class Optimization:
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
-    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0):
+    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -99,7 +103,7 @@ class Optimization:
         opts.maxiter = int(maxiter)
         opts.maxls = int(o["maxls"] if maxls is None else maxls)
         opts.c1, opts.c2, opts.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
-        opts.ncheck = int(o["ncheck"])
+        opts.ncheck = int(o["ncheck"] if ncheck is None else ncheck)
         opts.eps = float(eps)
         opts.pred_stop = float(pred_stop)
         opts.eres = float(eres)
@@ -161,7 +165,7 @@ class Optimization:
             nat = self._natoms()
             e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"],
-                                   pred_stop=0.1 * e32, eres=o["fp32_eres"])
+                                   pred_stop=0.1 * e32, eres=o["fp32_eres"], ncheck=o["stage_ncheck"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
             # the FP32 stage conserves the electron number only to single
@@ -173,7 +177,7 @@ class Optimization:
             if o["refine"] == "split":
                 ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.1 * o["econv"]
                 r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
-                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"])
+                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["stage_ncheck"])
             elif o["refine"] == "fp64":
                 r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
                                    eres=o["refine_eres"])

@@ -172,6 +172,7 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   p->max_partials = (nrows + 2 * p->pairs - 1) / (2 * p->pairs) + 1;
   if (e == cudaSuccess) e = cudaMalloc(&p->partials, sizeof(double) * GB_NE * p->max_partials);
   if (e == cudaSuccess) e = cudaMalloc(&p->scratch, sizeof(double) * 4096);
+  if (e == cudaSuccess) e = cudaMemset(p->scratch, 0, sizeof(double) * 4096);  // the counter slot starts at 0
   if (e != cudaSuccess) {
     gbofdft_plan_destroy(p);
     return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: workspace: %s", cudaGetErrorString(e));
@@ -282,3 +283,5 @@ int gbofdft_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, doub
 }
 
 }  // extern "C"
+
+unsigned* gb_plan_counter(gbofdft_plan* p) { return reinterpret_cast<unsigned*>(p->scratch + 4095); }

@@ -29,6 +29,7 @@ constexpr int kMaxVals = 4;
 enum {
   S_A = 0, S_B = 1, S_C = 2, S_D = 3,   // generic reduction outputs
   S_PAP = 4, S_R1 = 8,                  // TN inner loop
+  S_ALPHA = 12,                         // CG step r0 / pAp in the loop precision (0 if pAp < 0)
   S_EN = 16,                            // energies (GB_NE)
   S_COUNT = 64
 };
@@ -42,15 +43,32 @@ struct Ws {
 
 enum { F_PHI = 0, F_RHO, F_POT, F_RES0, F_P, F_CGR, F_CGP, F_AP, F_DIR, F_BEST, F_PHI1, F_POT1, F_TMP, F_NF };
 
-template <int NV>
-__device__ __forceinline__ void reduce_finalize(KSum (&acc)[NV], double* partials, double* out, unsigned* counter) {
+struct NoPost {
+  __device__ void operator()() const {}
+};
+
+// Grid reduction epilogue: per-CTA partials, then the last CTA to arrive sums
+// them in a fixed order into out[0..NV) and runs post() (scalars derived from
+// the sums, computed once instead of per element).
+template <typename ACC>
+__device__ __forceinline__ ACC warp_sum_acc(ACC v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// acc: per-thread sums in the field precision ACC; the warp sums are formed in
+// ACC (a few dozen elements each) and everything above them in FP64.
+template <int NV, typename ACC, typename P = NoPost>
+__device__ __forceinline__ void reduce_finalize(const ACC (&acc)[NV], double* partials, double* out,
+                                                unsigned* counter, P post = P()) {
   __shared__ double red[kRedThreads / 32][NV];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double v = warp_sum(acc[k].value());
-    if (lane == 0) red[warp][k] = v;
+    const ACC v = warp_sum_acc(acc[k]);
+    if (lane == 0) red[warp][k] = (double)v;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -85,15 +103,16 @@ __device__ __forceinline__ void reduce_finalize(KSum (&acc)[NV], double* partial
       out[k] = s.value();
     }
     *counter = 0u;
+    post();
   }
 }
 
 // f(i, ACC* contributions[NV]) for i in [0, n).  Each thread accumulates its
 // elements in the field precision ACC (a handful per thread); the per-thread
 // sums are combined in FP64 (compensated at the CTA and grid level).
-template <int NV, typename ACC, typename F>
+template <int NV, typename ACC, typename F, typename P = NoPost>
 __global__ void __launch_bounds__(kRedThreads) k_map_reduce(int64_t n, F f, double* partials, double* out,
-                                                           unsigned* counter) {
+                                                           unsigned* counter, P post = P()) {
   constexpr int NA = NV > 0 ? NV : 1;
   ACC acc[NA];
 #pragma unroll
@@ -104,20 +123,15 @@ __global__ void __launch_bounds__(kRedThreads) k_map_reduce(int64_t n, F f, doub
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] += c[k];
   }
-  if constexpr (NV > 0) {
-    KSum ks[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) { ks[k].init(); ks[k].add((double)acc[k]); }
-    reduce_finalize<NV>(ks, partials, out, counter);
-  }
+  if constexpr (NV > 0) reduce_finalize<NV, ACC>(acc, partials, out, counter, post);
 }
 
-template <int NV, typename ACC, typename F>
-int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st) {
+template <int NV, typename ACC, typename F, typename P = NoPost>
+int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st, P post = P()) {
   int nb = (int)((n + kRedThreads * 4 - 1) / (kRedThreads * 4));
   if (nb > kRedBlocks) nb = kRedBlocks;
   if (nb < 1) nb = 1;
-  k_map_reduce<NV, ACC><<<nb, kRedThreads, 0, st>>>(n, f, w.partials, w.sc + slot, w.counter);
+  k_map_reduce<NV, ACC><<<nb, kRedThreads, 0, st>>>(n, f, w.partials, w.sc + slot, w.counter, post);
   GB_CHECK_LAUNCH();
   return 0;
 }
@@ -254,18 +268,25 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     if ((rc = gbofdft_eval(plan, rho1, fn, pot1, nullptr, GBOFDFT_CALC_V, st))) return rc;
     TH* ap = d.ap;
     const TH inv_e = (TH)(1.0 / epsi);
+    double* scw = w.sc;
+    const double r0c = r0Norm;
+    // alpha = r0 / pAp, once, by the last CTA of the pAp reduction
+    auto alpha_post = [=] __device__() {
+      const double pap = scw[S_PAP];
+      TH* al = reinterpret_cast<TH*>(scw + S_ALPHA);
+      al[0] = pap < 0.0 ? (TH)0 : (TH)(r0c / pap);
+      al[1] = pap < 0.0 ? (TH)1 : (TH)0;   // negative curvature: no update
+    };
     rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
       const TH a = ((pot1[i] - muH) * phi1[i] - rb[i]) * inv_e;
       ap[i] = a;
       c[0] = cgp[i] * a;
-    }, S_PAP, st);
+    }, S_PAP, st, alpha_post);
     if (rc) return rc;
-    const double* scd = w.sc;
-    const double r0c = r0Norm;
+    const TH* alp = reinterpret_cast<const TH*>(w.sc + S_ALPHA);
     rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
-      const double pap = scd[S_PAP];
-      if (pap < 0.0) { c[0] = (TH)0; return; }
-      const TH alpha = (TH)(r0c / pap);
+      if (alp[1] != (TH)0) { c[0] = (TH)0; return; }
+      const TH alpha = alp[0];
       dir[i] += alpha * cgp[i];
       const TH r = cgr[i] - alpha * ap[i];
       cgr[i] = r;

@@ -299,29 +299,38 @@ __global__ void __launch_bounds__(256) k_rows_inv_eval(RowsInvArgs a) {
 
 // Sum per-CTA partials in a fixed order; slot GB_E_TOTAL gets the sum of
 // the components (times dV) plus the constant ion-ion term.
+// One CTA per energy component (the FP64 sums spread over 6 SMs); the last
+// CTA to finish adds the components into the total.  counter: zero on entry,
+// left zero.
 __global__ void __launch_bounds__(256) k_energy_final(const double* __restrict__ partials, int64_t nblk,
-                                                      double dV, double e_ion, double* __restrict__ e) {
-  __shared__ double red[8][6];
+                                                      double dV, double e_ion, double* __restrict__ e,
+                                                      unsigned* counter) {
+  __shared__ double red[8];
+  __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = 0; c < 6; ++c) {
-    KSum s;
-    s.init();
-    for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) s.add(partials[b * GB_NE + c]);
-    double v = warp_sum(s.value());
-    if (lane == 0) red[warp][c] = v;
-  }
+  const int c = blockIdx.x;
+  KSum s;
+  s.init();
+  for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) s.add(partials[b * GB_NE + c]);
+  const double v = warp_sum(s.value());
+  if (lane == 0) red[warp] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
+    KSum t;
+    t.init();
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t.add(red[w]);
+    e[c] = t.value() * dV;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
     double tot = 0.0;
-    for (int c = 0; c < 6; ++c) {
-      KSum s;
-      s.init();
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s.add(red[w][c]);
-      e[c] = s.value() * dV;
-      tot += e[c];
-    }
+    for (int k = 0; k < 6; ++k) tot += __ldcg(e + k);
     e[GB_E_EXTRA] = 0.0;
     e[GB_E_TOTAL] = tot + e_ion;
+    *counter = 0u;
   }
 }
 
@@ -542,7 +551,7 @@ static int rows_inv_eval_t(gbofdft_plan* p, const void* spec, int64_t fstride, i
   k_rows_inv_eval<T><<<(unsigned)nblk, 256, sm, st>>>(a);
   GB_CHECK_LAUNCH();
   if (calc_e) {
-    k_energy_final<<<1, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies);
+    k_energy_final<<<6, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies, gb_plan_counter(p));
     GB_CHECK_LAUNCH();
   }
   return 0;
@@ -559,7 +568,7 @@ int gb_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, int nf,
                                             p->partials, &nblk, st);
     if (rc == 0 && calc_e) {
       if (nblk > p->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
-      k_energy_final<<<1, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies);
+      k_energy_final<<<6, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies, gb_plan_counter(p));
       GB_CHECK_LAUNCH();
     }
     if (rc != 1) return rc;

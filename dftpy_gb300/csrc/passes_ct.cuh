@@ -257,7 +257,9 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
   const T inv_two_alpha = sc<T>(a.inv_two_alpha);
   const T wt_beta = sc<T>(a.wt_beta);
   const bool b56 = a.b56 != 0;
-  double es[6] = {0, 0, 0, 0, 0, 0};
+  // per-thread energy sums in the field precision (a handful of elements per
+  // thread); combined in FP64 across threads and CTAs
+  T es[6] = {0, 0, 0, 0, 0, 0};
   for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
     const int rr = idx / N, j = idx % N;
     const int64_t row = base + rr;
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
         T r53;                                            // cbrt(rho^5)
         if (pos) r53 = rho * rho * z3;
         else { T r5 = rho * rho; r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho; r53 = cbrt(r5); }
-        es[0] += (double)(r53 * tf_e);
+        es[0] += r53 * tf_e;
       }
     }
     if (ev.vw) {
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
       const T inv_sq = pos ? z2 : (rho > (T)0 ? (T)1 / fmax(sqrt(rho), (T)kZero) : (T)1e15);
       const T v = (T)0.5 * w * inv_sq;
       pot += v * vw_y;
-      if (want_e && rho > (T)0) es[1] += (double)(rho * v * vw_y);
+      if (want_e && rho > (T)0) es[1] += rho * v * vw_y;
     }
     if (ev.wt) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_wt * RP + pr, j)];
@@ -305,24 +307,24 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
       }
       const T v = two_alpha * rb_over_rc * kc;
       pot += v;
-      if (want_e) es[2] += (double)(v * rho * inv_two_alpha);
+      if (want_e) es[2] += v * rho * inv_two_alpha;
     }
     if (ev.xc) {
       T eps, vx;
       pz_lda_ct<T>(rho, eps, vx, want_e);
       pot += vx;
-      if (want_e) es[3] += (double)(eps * rho);
+      if (want_e) es[3] += eps * rho;
     }
     if (ev.hartree) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_h * RP + pr, j)];
       const T vh = odd ? zz.y : zz.x;
       pot += vh;
-      if (want_e) es[4] += 0.5 * (double)vh * (double)rho;
+      if (want_e) es[4] += (T)0.5 * vh * rho;
     }
     if (ev.pp) {
       const T vl = __ldg(vlocp + gidx);
       pot += vl;
-      if (want_e) es[5] += (double)vl * (double)rho;
+      if (want_e) es[5] += vl * rho;
     }
     potp[gidx] = pot;
   }
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(C
   const int lane32 = tid & 31, warp = tid >> 5;
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
-    const double v = warp_sum(es[c]);
+    const double v = warp_sum((double)es[c]);
     if (lane32 == 0) red[warp][c] = v;
   }
   __syncthreads();

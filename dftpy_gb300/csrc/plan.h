@@ -33,6 +33,9 @@ struct gbofdft_plan {
 };
 
 size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
+// zero-initialised grid-reduction ticket in the plan's scratch (last double;
+// scratch[0..4094] are free for per-CTA partial sums)
+unsigned* gb_plan_counter(gbofdft_plan* p);
 
 // ---- pass launchers (passes.cu) -------------------------------------------
 enum { OP_RHO = 0, OP_SQRT = 1, OP_POWB = 2 };           // forward prologues

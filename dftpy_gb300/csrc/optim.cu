@@ -196,7 +196,7 @@ struct DirFields {
 // The direction is left in F_P (precision T).
 template <typename T, typename TH>
 static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional* fn, const DirFields<TH>& d,
-                        double mu, double eps_fixed, double eps_rel, int maxfun) {
+                        double mu, double eps_fixed, double eps_rel, int maxfun, double cg_rtol) {
   const int64_t N = s.p->N;
   cudaStream_t st = s.st;
   const Ws& w = s.w;
@@ -242,7 +242,7 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
   const double r0_first = r0Norm;
   int jend = 0;
   const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
-  const double rConv = r0Norm * 0.1;
+  const double rConv = r0Norm * cg_rtol;
   double rmin = 1e10;          // min(rLists) with rLists = [1e10]
   double prev_min = 1e10;
   bool use_best = false;
@@ -413,7 +413,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
         float** hf = reinterpret_cast<float**>(s.hf);
         d.phi = hf[H_PHI]; d.rb = hf[H_RB]; d.cgr = hf[H_CGR]; d.cgp = hf[H_CGP]; d.ap = hf[H_AP];
         d.dir = hf[H_DIR]; d.best = hf[H_BEST]; d.phi1 = hf[H_PHI1]; d.rho1 = hf[H_TMP]; d.pot1 = hf[H_POT1];
-        if ((rc = tn_direction<T, float>(s, s.hp, s.hfn, d, mu, eps_fixed, eps_rel, o.maxfun))) return rc;
+        if ((rc = tn_direction<T, float>(s, s.hp, s.hfn, d, mu, eps_fixed, eps_rel, o.maxfun, o.cg_rtol))) return rc;
         done_dir = true;
       }
     }
@@ -422,7 +422,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       d.phi = F<T>(s, F_PHI); d.rb = F<T>(s, F_RES0); d.cgr = F<T>(s, F_CGR); d.cgp = F<T>(s, F_CGP);
       d.ap = F<T>(s, F_AP); d.dir = F<T>(s, F_DIR); d.best = F<T>(s, F_BEST); d.phi1 = F<T>(s, F_PHI1);
       d.rho1 = F<T>(s, F_TMP); d.pot1 = F<T>(s, F_POT1);
-      if ((rc = tn_direction<T, T>(s, s.p, s.fn, d, mu, eps_fixed, eps_rel, o.maxfun))) return rc;
+      if ((rc = tn_direction<T, T>(s, s.p, s.fn, d, mu, eps_fixed, eps_rel, o.maxfun, o.cg_rtol))) return rc;
     }
     // ---- OrthogonalNormalization (optimization.py:204-225) -----------------
     double theta0 = 0.0, d0 = 0.0;
@@ -470,7 +470,8 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     // quadratic-model decrease of a Newton step along p: |g| theta0 / 2 with
     // g = dE/dtheta at 0.  Below pred_stop the step cannot change the energy
     // by more than the requested resolution: stop converged.
-    if (o.pred_stop > 0.0 && fabs(d0 * dV) * theta0 < o.pred_stop) {
+    const double pred = fabs(d0 * dV) * theta0;
+    if (o.pred_stop > 0.0 && pred < o.pred_stop) {
       converged = 0;
       break;
     }
@@ -536,6 +537,13 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     void* t1 = s.w.f[F_POT]; s.w.f[F_POT] = s.w.f[F_POT1]; s.w.f[F_POT1] = t1;
     if ((rc = mu_residual(mu, energy, resN))) return rc;
     push_hist(energy);
+    // a Newton step whose inner CG reduced the residual to cg_rtol leaves a
+    // model decrease of about cg_rtol x this step's for the next one: below
+    // pred_stop, stop without computing that direction
+    if (o.pred_stop > 0.0 && o.pred_next && pred * o.cg_rtol < o.pred_stop) {
+      converged = 0;
+      break;
+    }
     // check_converge (optimization.py:522-535)
     if (nhist - 1 >= o.ncheck) {
       bool ok = true;
@@ -590,6 +598,8 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->eps = 0.0;
   o->pred_stop = 0.0;
   o->eres = 0.0;
+  o->cg_rtol = 0.1;
+  o->pred_next = 0;
   return GBOFDFT_OK;
 }
 
@@ -625,6 +635,7 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
     GB_REQUIRE(((uintptr_t)hworkspace & 255) == 0, "optimize_tn_split: Hessian workspace must be 256-byte aligned");
   }
   GB_REQUIRE(o->pred_stop >= 0.0, "optimize_tn: pred_stop must be >= 0");
+  GB_REQUIRE(o->cg_rtol > 0.0 && o->cg_rtol < 1.0, "optimize_tn: cg_rtol must be in (0, 1)");
   int64_t need = 0;
   gbofdft_tn_workspace_bytes(p, &need);
   GB_REQUIRE(workspace_bytes >= need, "optimize_tn: workspace %lld bytes < %lld", (long long)workspace_bytes,

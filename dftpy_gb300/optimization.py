@@ -13,7 +13,8 @@ density to the requested ``econv``).  Reductions are FP64 in every mode.
 In the FP64 refinement of "mixed", ``refine="split"`` (default) evaluates
 the Hessian-vector products of the inner CG loop in FP32
 (``gbofdft_optimize_tn_split``) and stops once the model decrease of the next
-Newton step is below ``refine_pred_stop`` (default econv / 10);
+Newton step is below ``refine_pred_stop`` (default econv / 100: the model
+decrease measures the density error, and forces need it that small);
 ``refine="fp64"`` runs the plain FP64 TN to ``econv``.
 """
 import ctypes
@@ -57,6 +58,14 @@ DEFAULTS = {
     # accepted step below its threshold (its next direction would be
     # discarded by the model-decrease stop)
     "stage_ncheck": 1,
+    # the refinement stops on the Newton model decrease (refine_pred_stop),
+    # which measures the density error; energy changes at FP64 resolution
+    # are noisy (see refine_eres), so their check is effectively off
+    "refine_ncheck": 50,
+    # inner CG tolerance (r.r < cg_rtol r0.r0) of the FP32 stage and of the
+    # refinement of "mixed"; the reference's TN uses 0.1
+    "fp32_cg_rtol": 0.1,
+    "refine_cg_rtol": 0.1,
 }
 
 
@@ -91,7 +100,8 @@ class Optimization:
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
-    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None):
+    def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None,
+             cg_rtol=0.1, pred_next=False):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -107,6 +117,8 @@ class Optimization:
         opts.eps = float(eps)
         opts.pred_stop = float(pred_stop)
         opts.eres = float(eres)
+        opts.cg_rtol = float(cg_rtol)
+        opts.pred_next = int(bool(pred_next))
         spec = self.EnergyEvaluator.spec(rho)
         f = spec.ctypes()
         nb = ctypes.c_int64()
@@ -165,7 +177,8 @@ class Optimization:
             nat = self._natoms()
             e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"],
-                                   pred_stop=0.1 * e32, eres=o["fp32_eres"], ncheck=o["stage_ncheck"])
+                                   pred_stop=0.1 * e32, eres=o["fp32_eres"], ncheck=o["stage_ncheck"],
+                                   cg_rtol=o["fp32_cg_rtol"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
             # the FP32 stage conserves the electron number only to single
@@ -175,9 +188,10 @@ class Optimization:
             n_out = float(r64.as_subclass(torch.Tensor).sum())
             r64 = r64 * (n_in / n_out)
             if o["refine"] == "split":
-                ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.1 * o["econv"]
+                ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.01 * o["econv"]
                 r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
-                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["stage_ncheck"])
+                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["refine_ncheck"],
+                                   cg_rtol=o["refine_cg_rtol"], pred_next=True)
             elif o["refine"] == "fp64":
                 r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
                                    eres=o["refine_eres"])

@@ -313,6 +313,10 @@ typedef struct gbofdft_tn_options {
                        line-search trial whose energy change is below
                        eres max(1, |E|) is accepted when |dE/dtheta| <= c2 |dE/dtheta(0)|
                        (no reference counterpart); 0: off (the reference's test) */
+  double cg_rtol;   /* inner CG stops when r.r < cg_rtol r0.r0 (the reference: 0.1) */
+  int pred_next;    /* with pred_stop > 0: also stop after a step whose model
+                       decrease times cg_rtol is below pred_stop (no reference
+                       counterpart); 0: off */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {

@@ -27,29 +27,73 @@ constexpr double kZero = 1e-30;
 
 __device__ __forceinline__ int ffreq_l(int i, int n) { return (i <= (n - 1) / 2) ? i : i - n; }
 
-// uniform-grid cubic spline table: coefficients c[j] (4 doubles) on
-// [j deta, (j+1) deta]; eta >= etamax returns the end value
+// uniform-grid cubic spline table: coefficients c[j] (4 values) on
+// [j deta, (j+1) deta]; eta >= etamax returns the end value.  A is the
+// arithmetic type: double for FP64 plans, float (with an FP32 copy of the
+// coefficients) for FP32 plans, so FP32 evaluations run no FP64 per element.
+template <typename A>
 struct UTable {
-  const double* c;
+  const A* c;
   int neta;
-  double deta, etamax, endval;
+  A deta, inv_deta, etamax, endval;
 };
 
-__device__ __forceinline__ double utab_eval(const UTable& t, double eta) {
+template <typename A>
+__device__ __forceinline__ A utab_eval(const UTable<A>& t, A eta) {
   if (!(eta < t.etamax)) return t.endval;
-  int j = (int)(eta / t.deta);
+  int j;
+  if constexpr (sizeof(A) == 8) j = (int)(eta / t.deta);
+  else j = (int)(eta * t.inv_deta);
   if (j > t.neta - 2) j = t.neta - 2;
   if (j < 0) j = 0;
-  const double u = eta - j * t.deta;
-  const double* cc = t.c + 4 * (size_t)j;
+  const A u = eta - j * t.deta;
+  const A* cc = t.c + 4 * (size_t)j;
   return __ldg(cc) + u * (__ldg(cc + 1) + u * (__ldg(cc + 2) + u * __ldg(cc + 3)));
+}
+
+// reciprocal lattice rows in the arithmetic type
+template <typename A>
+struct BG {
+  A b[9];
+};
+
+template <typename A>
+__device__ __forceinline__ A gg_a(const BG<A>& bg, int m0, int m1, int m2) {
+  const A f0 = (A)m0, f1 = (A)m1, f2 = (A)m2;
+  const A gx = f0 * bg.b[0] + f1 * bg.b[3] + f2 * bg.b[6];
+  const A gy = f0 * bg.b[1] + f1 * bg.b[4] + f2 * bg.b[7];
+  const A gz = f0 * bg.b[2] + f1 * bg.b[5] + f2 * bg.b[8];
+  return gx * gx + gy * gy + gz * gz;
+}
+
+// K(|G| / kf) in the Nyquist-partner-averaged form of gbk::sym_kernel, with
+// the geometry in the arithmetic type A
+template <typename A>
+__device__ __forceinline__ A lwt_kval(const GInfo& g, const BG<A>& bg, const UTable<A>& t, A inv_kf, int i0, int i1,
+                                      int k2) {
+  if constexpr (sizeof(A) == 8) {
+    return gbk::sym_kernel<double>(g, i0, i1, k2, [&](double gg) { return utab_eval(t, sqrt(gg) * inv_kf); });
+  } else {
+    const int m0 = ffreq_l(i0, g.n0), m1 = ffreq_l(i1, g.n1), m2 = g.full ? ffreq_l(k2, g.n2) : k2;
+    A k = utab_eval(t, sqrt(gg_a(bg, m0, m1, m2)) * inv_kf);
+    const bool nyq = ((g.n0 & 1) == 0 && 2 * i0 == g.n0) || ((g.n1 & 1) == 0 && 2 * i1 == g.n1) ||
+                     (g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2);
+    const bool plane = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
+    if (nyq && plane) {
+      const int p0 = ffreq_l((g.n0 - i0) % g.n0, g.n0), p1 = ffreq_l((g.n1 - i1) % g.n1, g.n1);
+      const int p2 = g.full ? ffreq_l((g.n2 - k2) % g.n2, g.n2) : k2;
+      k = (k + utab_eval(t, sqrt(gg_a(bg, p0, p1, p2)) * inv_kf)) * (A)0.5;
+    }
+    return k;
+  }
 }
 
 // dst[f] = coef_f * K_f(q / kf) * src   (f = 0: kernel table, f = 1: derivative table)
 template <typename T>
-__global__ void k_lwt_kmul(GInfo g, const cpx<T>* __restrict__ src, int64_t sld, cpx<T>* __restrict__ dst,
-                           int64_t dfs, int nf, UTable tk, UTable td, double kf, double scale) {
+__global__ void k_lwt_kmul(GInfo g, BG<T> bg, const cpx<T>* __restrict__ src, int64_t sld, cpx<T>* __restrict__ dst,
+                           int64_t dfs, int nf, UTable<T> tk, UTable<T> td, double kf, double scale) {
   const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  const T inv_kf = (T)(1.0 / kf), kfT = (T)kf, scT = (T)scale;
   for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
        id += (int64_t)gridDim.x * blockDim.x) {
     const int k2 = (int)(id % g.n2h);
@@ -58,12 +102,11 @@ __global__ void k_lwt_kmul(GInfo g, const cpx<T>* __restrict__ src, int64_t sld,
     const int64_t row = (int64_t)i0 * g.n1 + i1;
     const cpx<T> s = src[row * sld + k2];
     for (int f = 0; f < nf; ++f) {
-      const UTable& t = f == 0 ? tk : td;
-      double kv = 0.0;
-      if (!(i0 == 0 && i1 == 0 && k2 == 0))
-        kv = gbk::sym_kernel<double>(g, i0, i1, k2, [&](double gg) { return utab_eval(t, sqrt(gg) / kf); });
-      if (f == 1) kv /= kf;
-      const T c = (T)(kv * scale);
+      const UTable<T>& t = f == 0 ? tk : td;
+      T kv = (T)0;
+      if (!(i0 == 0 && i1 == 0 && k2 == 0)) kv = lwt_kval<T>(g, bg, t, inv_kf, i0, i1, k2);
+      if (f == 1) kv /= kfT;
+      const T c = kv * scT;
       dst[f * dfs + row * g.ld2 + k2] = cpx<T>{s.x * c, s.y * c};
     }
   }
@@ -71,35 +114,54 @@ __global__ void k_lwt_kmul(GInfo g, const cpx<T>* __restrict__ src, int64_t sld,
 
 // acc (+)= K(q/kf) U + [D(q/kf)/kf Ud]     (half spectra, layout ld2)
 template <typename T>
-__global__ void k_lwt_acc(GInfo g, const cpx<T>* __restrict__ U, int64_t ufs, int nf, UTable tk, UTable td,
-                          double kf, double scale, cpx<T>* __restrict__ acc, int first) {
+__global__ void k_lwt_acc(GInfo g, BG<T> bg, const cpx<T>* __restrict__ U, int64_t ufs, int nf, UTable<T> tk,
+                          UTable<T> td, double kf, double scale, cpx<T>* __restrict__ acc, int first) {
   const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  const T inv_kf = (T)(1.0 / kf), kfT = (T)kf, scT = (T)scale;
   for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
        id += (int64_t)gridDim.x * blockDim.x) {
     const int k2 = (int)(id % g.n2h);
     const int64_t r = id / g.n2h;
     const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
     const int64_t o = ((int64_t)i0 * g.n1 + i1) * g.ld2 + k2;
-    double ax = 0.0, ay = 0.0;
+    T ax = (T)0, ay = (T)0;
     if (!(i0 == 0 && i1 == 0 && k2 == 0)) {
       for (int f = 0; f < nf; ++f) {
-        const UTable& t = f == 0 ? tk : td;
-        double kv = gbk::sym_kernel<double>(g, i0, i1, k2, [&](double gg) { return utab_eval(t, sqrt(gg) / kf); });
-        if (f == 1) kv /= kf;
+        const UTable<T>& t = f == 0 ? tk : td;
+        T kv = lwt_kval<T>(g, bg, t, inv_kf, i0, i1, k2);
+        if (f == 1) kv /= kfT;
         const cpx<T> u = U[f * ufs + o];
-        ax += kv * scale * (double)u.x;
-        ay += kv * scale * (double)u.y;
+        ax += kv * scT * u.x;
+        ay += kv * scT * u.y;
       }
     }
-    if (first) acc[o] = cpx<T>{(T)ax, (T)ay};
-    else acc[o] = cpx<T>{(T)((double)acc[o].x + ax), (T)((double)acc[o].y + ay)};
+    if (first) acc[o] = cpx<T>{ax, ay};
+    else acc[o] = cpx<T>{acc[o].x + ax, acc[o].y + ay};
   }
 }
 
 __device__ __forceinline__ double kf_of(double rho) { return 2.0 * cbrt(3.0 * 9.86960440108935861883 * rho); }
+__device__ __forceinline__ float kf_of(float rho) { return 2.0f * cbrtf(29.6088132032680758f * rho); }
+
+// once per evaluation: kf(r) = 2 (3 pi^2 rho)^(1/3) clamped at kfmax, and
+// rho^alpha (rho clamped at 1e-30)
+template <typename T>
+__global__ void k_lwt_pre(int64_t n, const T* __restrict__ rho, double kfmax, double alpha, T* __restrict__ kfo,
+                          T* __restrict__ rao) {
+  const T kfm = (T)kfmax, al = (T)alpha;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T r = rho[i];
+    T kf = kf_of(r);
+    if (kf > kfm) kf = kfm;
+    const T rc = r > (T)0 ? r : (T)kZero;
+    kfo[i] = kf;
+    rao[i] = pow(rc, al);
+  }
+}
 
 struct IntervalArgs {
   const void* rho;
+  const void *kf, *ra;      // k_lwt_pre fields
   const void *p0, *p1, *m0, *m1;
   void *pot1, *pot3;
   void *w0, *w1, *wd0, *wd1;   // weight fields of knots i and i+1 (wd: derivative kernels, hermite)
@@ -113,46 +175,49 @@ struct IntervalArgs {
 // the first knot.
 template <typename T>
 __global__ void k_lwt_interval(IntervalArgs a) {
-  const T* rho = reinterpret_cast<const T*>(a.rho);
+  const T *kfp = reinterpret_cast<const T*>(a.kf), *rap = reinterpret_cast<const T*>(a.ra);
   const T *p0 = reinterpret_cast<const T*>(a.p0), *p1 = reinterpret_cast<const T*>(a.p1);
   const T *m0 = reinterpret_cast<const T*>(a.m0), *m1 = reinterpret_cast<const T*>(a.m1);
   T *pot1 = reinterpret_cast<T*>(a.pot1), *pot3 = reinterpret_cast<T*>(a.pot3);
   T *w0 = reinterpret_cast<T*>(a.w0), *w1 = reinterpret_cast<T*>(a.w1);
   T *wd0 = reinterpret_cast<T*>(a.wd0), *wd1 = reinterpret_cast<T*>(a.wd1);
-  const double dk = a.kr - a.kl;
+  const T kl = (T)a.kl, kr_e = (T)(a.kr + 1e-18), kl_e = (T)(a.kl + 1e-18);
+  const T dk = (T)(a.kr - a.kl), inv_kl = (T)(1.0 / a.kl);
+  const T one = (T)1, two = (T)2, three = (T)3;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double r = (double)rho[i];
-    double kf = kf_of(r);
-    if (kf > a.kfmax) kf = a.kfmax;
-    const double rc = r > 0.0 ? r : kZero;
-    const double rA = pow(rc, a.alpha);
-    if (a.first && kf < a.kl + 1e-18) {
-      const double t = (kf - a.kl) / a.kl;
-      pot1[i] = (T)((double)p0[i] * t);
-      if (a.kdd > 1) w0[i] += (T)(rA * t);
+    const T kf = kfp[i];
+    const T rA = rap[i];
+    if (a.first && kf < kl_e) {
+      T t;
+      if constexpr (sizeof(T) == 8) t = (kf - kl) / kl;
+      else t = (kf - kl) * inv_kl;
+      pot1[i] = p0[i] * t;
+      if (a.kdd > 1) w0[i] += rA * t;
     }
-    if (!(kf > a.kl && kf < a.kr + 1e-18)) continue;
-    const double t = (kf - a.kl) / dk;
+    if (!(kf > kl && kf < kr_e)) continue;
+    const T t = (kf - kl) / dk;
     if (!a.hermite) {
-      const double t0 = 1.0 - t;
-      pot1[i] = (T)((double)p0[i] * t0 + (double)p1[i] * t);
+      const T t0 = one - t;
+      pot1[i] = p0[i] * t0 + p1[i] * t;
       if (a.kdd > 1) {
-        w0[i] += (T)(rA * t0);
-        w1[i] += (T)(rA * t);
-        if (a.kdd == 3) pot3[i] = (T)((double)m0[i] * t0 + (double)m1[i] * t);
+        w0[i] += rA * t0;
+        w1[i] += rA * t;
+        if (a.kdd == 3) pot3[i] = m0[i] * t0 + m1[i] * t;
       }
     } else {
-      const double t2 = t * t, t3 = t2 * t;
-      const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = t3 - 2.0 * t2 + t, h01 = 1.0 - h00, h11 = t3 - t2;
-      pot1[i] = (T)(h00 * p0[i] + h01 * p1[i] + dk * (h10 * m0[i] + h11 * m1[i]));
+      const T t2 = t * t, t3 = t2 * t;
+      const T h00 = two * t3 - three * t2 + one, h10 = t3 - two * t2 + t, h01 = one - h00, h11 = t3 - t2;
+      pot1[i] = h00 * p0[i] + h01 * p1[i] + dk * (h10 * m0[i] + h11 * m1[i]);
       if (a.kdd > 1) {
-        w0[i] += (T)(rA * h00);
-        w1[i] += (T)(rA * h01);
-        wd0[i] += (T)(rA * dk * h10);
-        wd1[i] += (T)(rA * dk * h11);
+        w0[i] += rA * h00;
+        w1[i] += rA * h01;
+        wd0[i] += rA * dk * h10;
+        wd1[i] += rA * dk * h11;
         if (a.kdd == 3) {
-          const double h00D = 6.0 * t2 - 6 * t, h10D = 3.0 * t2 - 4 * t + 1.0, h01D = -h00D, h11D = 3.0 * t2 - 2 * t;
-          pot3[i] = (T)((h00D * p0[i] + h01D * p1[i]) / dk + h10D * m0[i] + h11D * m1[i]);
+          const T six = (T)6, four = (T)4;
+          const T h00D = six * t2 - six * t, h10D = three * t2 - four * t + one, h01D = -h00D,
+                  h11D = three * t2 - two * t;
+          pot3[i] = (h00D * p0[i] + h01D * p1[i]) / dk + h10D * m0[i] + h11D * m1[i];
         }
       }
     }
@@ -161,33 +226,38 @@ __global__ void k_lwt_interval(IntervalArgs a) {
 
 // final assembly (lwt.py:305-341): low-density weight, energy, potential
 template <typename T>
-__global__ void k_lwt_final(int64_t n, const T* __restrict__ rho, const T* __restrict__ pot1,
-                            const T* __restrict__ pot2, const T* __restrict__ pot3, double alpha, double beta,
-                            double kfmax, double rhov, double ld, int vcalc, int have_pot2, T* __restrict__ pot,
-                            double* __restrict__ partial) {
-  KSum es;
-  es.init();
+__global__ void k_lwt_final(int64_t n, const T* __restrict__ rho, const T* __restrict__ kfp,
+                            const T* __restrict__ rap, const T* __restrict__ pot1, const T* __restrict__ pot2,
+                            const T* __restrict__ pot3, double alpha, double beta, double rhov, double ld, int vcalc,
+                            int have_pot2, T* __restrict__ pot, double* __restrict__ partial) {
+  const T al = (T)alpha, be = (T)beta, ldT = (T)ld, inv_rhov_ld = (T)(1.0 / pow(rhov, ld));
+  const T third = (T)(1.0 / 3.0);
+  T es = (T)0;   // per-thread energy sum in the field precision, FP64 above
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double r = (double)rho[i];
-    double fac = 1.0;
-    if (r < 1e-6) fac = pow(fabs(r), ld) / pow(rhov, ld);
-    if (r < 0.0) fac = 0.0;
-    const double rc = r > 0.0 ? r : kZero;
-    const double rA = pow(rc, alpha);
-    const double p1 = (double)pot1[i] * fac;
-    es.add(rA * p1);
+    const T r = rho[i];
+    T fac = (T)1;
+    if (r < (T)1e-6) {
+      if constexpr (sizeof(T) == 8) fac = pow(fabs(r), ld) / pow(rhov, ld);
+      else fac = pow(fabs(r), ldT) * inv_rhov_ld;
+    }
+    if (r < (T)0) fac = (T)0;
+    const T rc = r > (T)0 ? r : (T)kZero;
+    const T rA = rap[i];
+    const T p1 = pot1[i] * fac;
+    es += rA * p1;
     if (vcalc) {
-      double kf = kf_of(r);
-      if (kf > kfmax) kf = kfmax;
-      const double p2 = (have_pot2 ? (double)pot2[i] : (double)pot1[i]) * fac;
-      const double p3 = (double)pot3[i] * fac;
-      const double rB = alpha == beta ? rA : pow(rc, beta);
-      const double v = p1 * alpha * (rA / rc) + p2 * beta * (rB / rc) + p3 * (kf / 3.0) * (rA / rc);
-      pot[i] = (T)((double)pot[i] + v);
+      const T kf = kfp[i];
+      const T p2 = (have_pot2 ? pot2[i] : pot1[i]) * fac;
+      const T p3 = pot3[i] * fac;
+      const T rB = alpha == beta ? rA : pow(rc, be);
+      T v;
+      if constexpr (sizeof(T) == 8) v = p1 * al * (rA / rc) + p2 * be * (rB / rc) + p3 * (kf / 3.0) * (rA / rc);
+      else v = p1 * al * (rA / rc) + p2 * be * (rB / rc) + p3 * (kf * third) * (rA / rc);
+      pot[i] = pot[i] + v;
     }
   }
   __shared__ double red[32];
-  double v = warp_sum(es.value());
+  double v = warp_sum((double)es);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -219,12 +289,13 @@ __global__ void k_lwt_energy(const double* __restrict__ partial, int nb, double 
 
 template <typename T>
 __global__ void k_minmax(int64_t n, const T* __restrict__ x, double* __restrict__ part) {
-  double mn = 1e300, mx = -1e300;
+  T mnT = x[0], mxT = x[0];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = (double)x[i];
-    mn = fmin(mn, v);
-    mx = fmax(mx, v);
+    const T v = x[i];
+    mnT = v < mnT ? v : mnT;
+    mxT = v > mxT ? v : mxT;
   }
+  double mn = (double)mnT, mx = (double)mxT;
   for (int o = 16; o > 0; o >>= 1) {
     mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -283,9 +354,12 @@ int blocks_for(int64_t n) {
 
 size_t r256(size_t x) { return (x + 255) / 256 * 256; }
 
+constexpr int kMaxNetaF32 = 200001;   // FP32 table copies: coefficients of at most this many points
+
 struct LwtBufs {
-  void *p[2], *m[2], *w[2], *wd[2], *pot1, *pot2, *pot3;
+  void *p[2], *m[2], *w[2], *wd[2], *pot1, *pot2, *pot3, *kf, *ra;
   void *S, *T, *U, *G;   // spectra: rho^beta, knot work (2), weights (2), pot2 accumulator
+  float *ktab_f, *dtab_f; // FP32 copies of the kernel tables (FP32 plans)
   double* part;
 };
 
@@ -297,8 +371,10 @@ LwtBufs lwt_layout(const gbofdft_plan* p, void* work) {
   const size_t fb = lwt_field_bytes(p), sb = lwt_spec_bytes(p);
   LwtBufs L;
   void** fields[] = {&L.p[0], &L.p[1], &L.m[0], &L.m[1], &L.w[0], &L.w[1], &L.wd[0], &L.wd[1],
-                     &L.pot1, &L.pot2, &L.pot3};
-  for (int i = 0; i < 11; ++i) { *fields[i] = b; b += fb; }
+                     &L.pot1, &L.pot2, &L.pot3, &L.kf, &L.ra};
+  for (int i = 0; i < 13; ++i) { *fields[i] = b; b += fb; }
+  L.ktab_f = reinterpret_cast<float*>(b); b += r256(sizeof(float) * 4 * (size_t)kMaxNetaF32);
+  L.dtab_f = reinterpret_cast<float*>(b); b += r256(sizeof(float) * 4 * (size_t)kMaxNetaF32);
   L.S = b; b += sb;
   L.T = b; b += 2 * sb;
   L.U = b; b += 2 * sb;
@@ -307,14 +383,30 @@ LwtBufs lwt_layout(const gbofdft_plan* p, void* work) {
   return L;
 }
 
-UTable utab(const gbofdft_lwt* d, int deriv) {
-  UTable t;
-  t.c = deriv ? d->dtab_c : d->ktab_c;
+template <typename T>
+UTable<T> utab(const gbofdft_lwt* d, int deriv, const float* fcopy) {
+  UTable<T> t;
+  if constexpr (sizeof(T) == 8) t.c = deriv ? d->dtab_c : d->ktab_c;
+  else t.c = fcopy;
   t.neta = d->neta;
-  t.deta = d->etamax / (d->neta - 1);
-  t.etamax = d->etamax;
-  t.endval = deriv ? d->dtab_end : d->ktab_end;
+  const double deta = d->etamax / (d->neta - 1);
+  t.deta = (T)deta;
+  t.inv_deta = (T)(1.0 / deta);
+  t.etamax = (T)d->etamax;
+  t.endval = (T)(deriv ? d->dtab_end : d->ktab_end);
   return t;
+}
+
+__global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+template <typename T>
+BG<T> bg_of(const gbofdft_plan* p) {
+  BG<T> b;
+  for (int i = 0; i < 9; ++i) b.b[i] = (T)p->bg[i];
+  return b;
 }
 
 // forward 3D transform of a real field (scale 1) into spectrum layout ld2
@@ -385,7 +477,18 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   const int hermite = d->interp == 1;
   const int mcalc = kdd > 1 || hermite;
   const int nkf = mcalc ? 2 : 1;
-  const UTable tk = utab(d, 0), td = utab(d, 1);
+  if constexpr (sizeof(T) == 4) {
+    GB_REQUIRE(d->neta <= kMaxNetaF32, "lwt: FP32 plans take at most %d table points (neta %d)", kMaxNetaF32,
+               d->neta);
+    const int64_t nc = 4 * (int64_t)(d->neta - 1);
+    k_to_float<<<blocks_for(nc), 256, 0, st>>>(nc, d->ktab_c, L.ktab_f);
+    k_to_float<<<blocks_for(nc), 256, 0, st>>>(nc, d->dtab_c, L.dtab_f);
+    GB_CHECK_LAUNCH();
+  }
+  const UTable<T> tk = utab<T>(d, 0, L.ktab_f), td = utab<T>(d, 1, L.dtab_f);
+  const BG<T> bg = bg_of<T>(p);
+  k_lwt_pre<T><<<nb, 256, 0, st>>>(N, rhoT, kfmax, d->alpha, reinterpret_cast<T*>(L.kf), reinterpret_cast<T*>(L.ra));
+  GB_CHECK_LAUNCH();
   const double invN = 1.0 / (double)N;
   const size_t fb = lwt_field_bytes(p), sb = lwt_spec_bytes(p);
   const int64_t sfs = (int64_t)(sb / (2 * gb_elem(p)));  // complex elements per spectrum slot
@@ -400,7 +503,8 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   int cur = 0;
   for (int k = 0; k < nsp; ++k) {
     // p_k (and m_k) from the shared spectrum
-    k_lwt_kmul<T><<<nb, 256, 0, st>>>(p->gi, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs, nkf, tk, td, kfl[k], invN);
+    k_lwt_kmul<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs, nkf, tk, td, kfl[k],
+                                       invN);
     GB_CHECK_LAUNCH();
     // pm slots: p[cur], m[cur] must be adjacent for one inverse with nf = 2:
     // inverse into p[cur] then copy to m[cur] when needed (p and m are separate fields)
@@ -411,7 +515,7 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
     if (k >= 1) {
       const int prv = cur ^ 1;
       IntervalArgs a;
-      a.rho = rho; a.p0 = L.p[prv]; a.p1 = L.p[cur]; a.m0 = L.m[prv]; a.m1 = L.m[cur];
+      a.rho = rho; a.kf = L.kf; a.ra = L.ra; a.p0 = L.p[prv]; a.p1 = L.p[cur]; a.m0 = L.m[prv]; a.m1 = L.m[cur];
       a.pot1 = L.pot1; a.pot3 = L.pot3;
       a.w0 = L.w[prv]; a.w1 = L.w[cur]; a.wd0 = L.wd[prv]; a.wd1 = L.wd[cur];
       a.kl = kfl[k - 1]; a.kr = kfl[k]; a.kfmax = kfmax; a.alpha = d->alpha;
@@ -427,7 +531,7 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
         // weights of knot k-1 are complete: pot2G += K_{k-1} fft(w) (+ D_{k-1} fft(wd))
         if ((rc = fwd3d(p, L.w[prv], L.U, OP_RHO, 1.0, st))) return rc;
         if (hermite && (rc = fwd3d(p, L.wd[prv], (char*)L.U + sb, OP_RHO, 1.0, st))) return rc;
-        k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[k - 1], invN,
+        k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[k - 1], invN,
                                           (cpx<T>*)L.G, k == 1);
         GB_CHECK_LAUNCH();
       }
@@ -438,14 +542,15 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   if (kdd > 1) {
     if ((rc = fwd3d(p, L.w[last], L.U, OP_RHO, 1.0, st))) return rc;
     if (hermite && (rc = fwd3d(p, L.wd[last], (char*)L.U + sb, OP_RHO, 1.0, st))) return rc;
-    k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[nsp - 1], invN,
+    k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[nsp - 1], invN,
                                       (cpx<T>*)L.G, 0);
     GB_CHECK_LAUNCH();
     if (calc_v && (rc = inv3d(p, L.G, sfs, 1, L.pot2, 0, st))) return rc;
   }
   const double ld = fmax(0.1, d->ldw > 0 ? d->ldw : 1.0 / 6.0);
-  k_lwt_final<T><<<nb, 256, 0, st>>>(N, rhoT, (const T*)L.pot1, (const T*)L.pot2, (const T*)L.pot3, d->alpha,
-                                      d->beta, kfmax, rmax, ld, calc_v, kdd > 1, reinterpret_cast<T*>(pot), L.part);
+  k_lwt_final<T><<<nb, 256, 0, st>>>(N, rhoT, (const T*)L.kf, (const T*)L.ra, (const T*)L.pot1, (const T*)L.pot2,
+                                      (const T*)L.pot3, d->alpha, d->beta, rmax, ld, calc_v, kdd > 1,
+                                      reinterpret_cast<T*>(pot), L.part);
   GB_CHECK_LAUNCH();
   if (calc_e && energies) {
     k_lwt_energy<<<1, 256, 0, st>>>(L.part, nb, p->dV, energies);
@@ -475,7 +580,8 @@ extern "C" {
 
 int gbofdft_lwt_workspace_bytes(const gbofdft_plan* p, int64_t* bytes) {
   GB_REQUIRE(p && bytes, "lwt_workspace_bytes: null argument");
-  *bytes = (int64_t)(11 * lwt_field_bytes(p) + 6 * lwt_spec_bytes(p) + r256(sizeof(double) * 8192));
+  *bytes = (int64_t)(13 * lwt_field_bytes(p) + 6 * lwt_spec_bytes(p) + 2 * r256(sizeof(float) * 4 * kMaxNetaF32) +
+                     r256(sizeof(double) * 8192));
   return GBOFDFT_OK;
 }
 

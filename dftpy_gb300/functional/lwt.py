@@ -75,16 +75,21 @@ class LWTTerm:
         self._tabs = True
 
     def prepare(self, rho):
-        """Tables and a workspace for rho's grid and dtype; returns the descriptor."""
+        """Tables and a workspace for rho's grid and dtype; returns that
+        (grid, dtype)'s descriptor.  Each descriptor owns its workspace, so an
+        FP64 and an FP32 evaluation of the same term can interleave (the
+        mixed-precision refinement does); each carries its own automatic k_F
+        bounds, seeded from the first descriptor's at creation."""
         self._tables()
         key = (id(rho.grid), rho.dtype)
         if key not in self._work:
             plan = rho.grid.plan(rho.dtype)
             nb = ctypes.c_int64()
             _lib.check(_lib.load().gbofdft_lwt_workspace_bytes(plan.handle, ctypes.byref(nb)))
-            self._work[key] = (torch.empty(int(nb.value) // 8 + 64, dtype=torch.float64, device="cuda"),
-                               int(nb.value))
-        buf, nb = self._work[key]
-        self.d.work = _lib.aligned_ptr(buf, 256)
-        self.d.work_bytes = nb
-        return self.d
+            buf = torch.empty(int(nb.value) // 8 + 64, dtype=torch.float64, device="cuda")
+            d = _lib.Lwt()
+            ctypes.pointer(d)[0] = self.d          # copy the options, tables and k_F state
+            d.work = _lib.aligned_ptr(buf, 256)
+            d.work_bytes = int(nb.value)
+            self._work[key] = (buf, d)
+        return self._work[key][1]

@@ -250,7 +250,7 @@ def test_lmgp_reference_fixture(api, golden, interp, prec):
     assert np.abs(v - vs).max() <= vtol * np.abs(vs).max()
     if interp == "linear" and prec == 1:
         assert abs(out.energy - 2.9145872498710492) < 1e-10
-        assert ke._lwt.d.nknots == 15
+        assert ke._lwt.prepare(rho).nknots == 15
 
 
 def test_tn_al4_lmgp_matches_oracle(api):
@@ -347,3 +347,39 @@ def test_tn_from_atomic_guess(api, golden):
     rho = opt.optimize_rho(guess_rho=rho0)
     assert opt.converged == 0
     assert abs(total.Energy(rho) - float(a["E_final"])) < 1e-6 * st.nat
+
+
+def test_config5_lmgp_translation_invariance(api):
+    """4000 Al, 360^3, LMGP + LDA + Hartree + PP (PME) at full size, through a
+    size-independent property: moving every atom by one grid step along a
+    lattice vector and rolling the density by one point gives the same energy
+    (1e-11 relative) and the rolled potential (1e-10 of max|V|); the FP32
+    evaluation agrees with the FP64 one to 1e-6 relative."""
+    torch = api["torch"]
+    F = api["functional"]
+    from dftpy_gb300.density import DensityGenerator
+    st = systems.config_al4000(0)
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    r, a = {"Al": None}, {"Al": None}
+    r["Al"], a["Al"] = systems.atomic_density_table(3.0, systems.ATOMIC_SIGMA["Al"])
+
+    def energy_potential(positions, rho=None, shift=0, dtype=torch.float64):
+        ions = api["ions"].Ions(st.symbols, positions=positions, cell=st.lattice)
+        ps = F.LocalPseudo(grid=grid, ions=ions, PP_list=_pp(api, st.symbols), PME=True)
+        total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="LMGP"),
+                                  XCFunctional=F.Functional(type="XC", name="LDA"),
+                                  HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+        if rho is None:
+            rho = DensityGenerator(r=r, arho=a).guess_rho(ps.ions, grid=grid)
+        x = torch.roll(rho.as_subclass(torch.Tensor), shifts=shift, dims=0).to(dtype).contiguous()
+        out = total(api["field"].DirectField(grid, data=x), calcType={"E", "V"})
+        return rho, float(out.energy), out.potential.as_subclass(torch.Tensor)
+
+    step = st.lattice[0] / st.nr[0]
+    rho, e0, v0 = energy_potential(st.positions)
+    _, e1, v1 = energy_potential(st.positions + step, rho=rho, shift=1)
+    assert abs(e1 - e0) <= 1e-11 * abs(e0), (e0, e1)
+    vmax = float(v0.abs().max())
+    assert float((torch.roll(v0, shifts=1, dims=0) - v1).abs().max()) <= 1e-10 * vmax
+    _, e32, _ = energy_potential(st.positions, rho=rho, dtype=torch.float32)
+    assert abs(e32 - e0) <= 1e-6 * abs(e0), (e0, e32)

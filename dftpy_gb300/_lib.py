@@ -59,7 +59,7 @@ class TnOptions(ctypes.Structure):
                 ("maxls", ctypes.c_int), ("c1", ctypes.c_double), ("c2", ctypes.c_double),
                 ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double),
                 ("pred_stop", ctypes.c_double), ("eres", ctypes.c_double), ("cg_rtol", ctypes.c_double),
-                ("pred_next", ctypes.c_int)]
+                ("pred_next", ctypes.c_int), ("precond", ctypes.c_int)]
 
 
 class TnResult(ctypes.Structure):

@@ -30,18 +30,21 @@ enum {
   S_A = 0, S_B = 1, S_C = 2, S_D = 3,   // generic reduction outputs
   S_PAP = 4, S_R1 = 8,                  // TN inner loop
   S_ALPHA = 12,                         // CG step r0 / pAp in the loop precision (0 if pAp < 0)
+  S_RZ = 14, S_RZN = 15,                // preconditioned CG: r.z (current, new)
+  S_BETA = 24,                          // preconditioned CG: beta in the loop precision
   S_EN = 16,                            // energies (GB_NE)
   S_COUNT = 64
 };
 
 struct Ws {
-  void* f[14];
+  void* f[16];
   double* partials;  // kRedBlocks * kMaxVals
   double* sc;        // S_COUNT
   unsigned* counter;
 };
 
-enum { F_PHI = 0, F_RHO, F_POT, F_RES0, F_P, F_CGR, F_CGP, F_AP, F_DIR, F_BEST, F_PHI1, F_POT1, F_TMP, F_NF };
+enum { F_PHI = 0, F_RHO, F_POT, F_RES0, F_P, F_CGR, F_CGP, F_AP, F_DIR, F_BEST, F_PHI1, F_POT1, F_TMP,
+       F_Z, F_PC, F_NF };   // F_Z, F_PC: preconditioned residual and preconditioner (half spectrum)
 
 struct NoPost {
   __device__ void operator()() const {}
@@ -139,7 +142,7 @@ int launch_mr(const Ws& w, int64_t n, F f, int slot, cudaStream_t st, P post = P
 }  // namespace
 
 // Fields of the Hessian-precision inner loop (split mode only)
-enum { H_PHI = 0, H_RB, H_POT, H_CGR, H_CGP, H_AP, H_DIR, H_BEST, H_PHI1, H_POT1, H_TMP, H_NF };
+enum { H_PHI = 0, H_RB, H_POT, H_CGR, H_CGP, H_AP, H_DIR, H_BEST, H_PHI1, H_POT1, H_TMP, H_Z, H_PC, H_NF };
 
 struct TnState {
   gbofdft_plan* p;
@@ -188,6 +191,8 @@ static T* F(TnState& s, int i) { return reinterpret_cast<T*>(s.w.f[i]); }
 template <typename TH>
 struct DirFields {
   TH *phi, *rb, *cgr, *cgp, *ap, *dir, *best, *phi1, *rho1, *pot1;
+  TH* z;          // preconditioned residual (PCG only)
+  const TH* pc;   // preconditioner on the half spectrum; nullptr: plain CG (the reference's)
 };
 
 // TN direction (optimization.py:91-147) with Hessian products
@@ -237,11 +242,27 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     }, S_A, st);
     if (rc) return rc;
   }
+  const bool pcg = d.pc != nullptr;
+  double* scw0 = w.sc;
+  if (pcg) {
+    // z = P r, p = z, rz = r.z
+    if ((rc = gbofdft_convolve(plan, cgr, d.z, GBOFDFT_KER_ARRAY, d.pc, 1.0, st))) return rc;
+    TH* zz = d.z;
+    rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+      const TH zi = zz[i];
+      cgp[i] = zi;
+      c[0] = cgr[i] * zi;
+    }, S_RZ, st);
+    if (rc) return rc;
+  }
   if ((rc = ts_sync(s))) return rc;
-  double r0Norm = s.host[S_A];
+  const double rz0 = s.host[S_RZ];
+  // stopping tests on r.r (the reference's), or on r.z with the preconditioner
+  double r0Norm = pcg ? rz0 : s.host[S_A];
   const double r0_first = r0Norm;
   int jend = 0;
-  const double epsi = eps_rel > 0 && r0Norm > 0 ? eps_rel * sqrt(s.host[S_B] / r0Norm) : eps_fixed;
+  const double rr0 = s.host[S_A];
+  const double epsi = eps_rel > 0 && rr0 > 0 ? eps_rel * sqrt(s.host[S_B] / rr0) : eps_fixed;
   const double rConv = r0Norm * cg_rtol;
   double rmin = 1e10;          // min(rLists) with rLists = [1e10]
   double prev_min = 1e10;
@@ -255,13 +276,25 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     TH* rho1 = d.rho1;
     const TH eT = (TH)epsi, bT = (TH)beta;
     const bool first = (j == 0);
-    rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) {
-      TH pv = cgp[i];
-      if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
-      const TH p1 = phi[i] + eT * pv;
-      phi1[i] = p1;
-      rho1[i] = p1 * p1;
-    }, S_A, st);
+    if (!pcg) {
+      rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+        TH pv = cgp[i];
+        if (!first) { pv = cgr[i] + bT * pv; cgp[i] = pv; }
+        const TH p1 = phi[i] + eT * pv;
+        phi1[i] = p1;
+        rho1[i] = p1 * p1;
+      }, S_A, st);
+    } else {
+      const TH* zz = d.z;
+      const TH* bd = reinterpret_cast<const TH*>(w.sc + S_BETA);
+      rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) {
+        TH pv = cgp[i];
+        if (!first) { pv = zz[i] + *bd * pv; cgp[i] = pv; }
+        const TH p1 = phi[i] + eT * pv;
+        phi1[i] = p1;
+        rho1[i] = p1 * p1;
+      }, S_A, st);
+    }
     if (rc) return rc;
     TH* pot1 = d.pot1;
     if (split) ++s.n_hv; else ++s.n_v;
@@ -271,10 +304,12 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     double* scw = w.sc;
     const double r0c = r0Norm;
     // alpha = r0 / pAp, once, by the last CTA of the pAp reduction
+    const bool pcgc = pcg;
     auto alpha_post = [=] __device__() {
       const double pap = scw[S_PAP];
+      const double num = pcgc ? scw[S_RZ] : r0c;
       TH* al = reinterpret_cast<TH*>(scw + S_ALPHA);
-      al[0] = pap < 0.0 ? (TH)0 : (TH)(r0c / pap);
+      al[0] = pap < 0.0 ? (TH)0 : (TH)(num / pap);
       al[1] = pap < 0.0 ? (TH)1 : (TH)0;   // negative curvature: no update
     };
     rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) {
@@ -293,18 +328,31 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
       c[0] = r * r;
     }, S_R1, st);
     if (rc) return rc;
+    if (pcg) {
+      // z = P r; beta = r.z / previous r.z (device scalars)
+      if ((rc = gbofdft_convolve(plan, cgr, d.z, GBOFDFT_KER_ARRAY, d.pc, 1.0, st))) return rc;
+      TH* zz = d.z;
+      auto beta_post = [=] __device__() {
+        const double rzn = scw0[S_RZN], rzo = scw0[S_RZ];
+        *reinterpret_cast<TH*>(scw0 + S_BETA) = rzo != 0.0 ? (TH)(rzn / rzo) : (TH)0;
+        scw0[S_RZ] = rzn;
+      };
+      rc = launch_mr<1, TH>(w, N, [=] __device__(int64_t i, TH* c) { c[0] = cgr[i] * zz[i]; }, S_RZN, st,
+                            beta_post);
+      if (rc) return rc;
+    }
     if ((rc = ts_sync(s))) return rc;
     const double pAp = s.host[S_PAP];
     if (pAp < 0.0) {
       if (j == 0) {
-        // direction = r0Norm / pAp * p
-        const TH sc = (TH)(r0Norm / pAp);
+        // direction = r0Norm / pAp * p  (r.z / pAp with the preconditioner)
+        const TH sc = (TH)((pcg ? rz0 : r0Norm) / pAp);
         rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) { dir[i] = sc * cgp[i]; }, S_A, st);
         if (rc) return rc;
       }
       break;
     }
-    const double r1Norm = s.host[S_R1];
+    const double r1Norm = pcg ? s.host[S_RZ] : s.host[S_R1];
     if (r1Norm < rmin) {
       GB_CUDA(cudaMemcpyAsync(d.best, dir, sizeof(TH) * N, cudaMemcpyDeviceToDevice, st));
       have_best = true;
@@ -348,6 +396,12 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     if (rc) return rc;
     if ((rc = ts_sync(s))) return rc;
     const T fac = (T)sqrt(s.host[S_A] / s.host[S_B]);
+    if (o.precond) {
+      // preconditioner of the uniform gas at the mean density
+      const double rho0 = s.host[S_A] / (double)N;
+      if ((rc = gb_build_precond(s.p, rho0, s.w.f[F_PC], st))) return rc;
+      if (s.hp && (rc = gb_build_precond(s.hp, rho0, s.hf[H_PC], st))) return rc;
+    }
     T* rho = F<T>(s, F_RHO);
     rc = launch_mr<0, T>(w, N, [=] __device__(int64_t i, T* c) {
       const T ph = phi[i] * fac;
@@ -413,6 +467,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
         float** hf = reinterpret_cast<float**>(s.hf);
         d.phi = hf[H_PHI]; d.rb = hf[H_RB]; d.cgr = hf[H_CGR]; d.cgp = hf[H_CGP]; d.ap = hf[H_AP];
         d.dir = hf[H_DIR]; d.best = hf[H_BEST]; d.phi1 = hf[H_PHI1]; d.rho1 = hf[H_TMP]; d.pot1 = hf[H_POT1];
+        d.z = hf[H_Z]; d.pc = o.precond ? hf[H_PC] : nullptr;
         if ((rc = tn_direction<T, float>(s, s.hp, s.hfn, d, mu, eps_fixed, eps_rel, o.maxfun, o.cg_rtol))) return rc;
         done_dir = true;
       }
@@ -422,6 +477,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       d.phi = F<T>(s, F_PHI); d.rb = F<T>(s, F_RES0); d.cgr = F<T>(s, F_CGR); d.cgp = F<T>(s, F_CGP);
       d.ap = F<T>(s, F_AP); d.dir = F<T>(s, F_DIR); d.best = F<T>(s, F_BEST); d.phi1 = F<T>(s, F_PHI1);
       d.rho1 = F<T>(s, F_TMP); d.pot1 = F<T>(s, F_POT1);
+      d.z = F<T>(s, F_Z); d.pc = o.precond ? F<T>(s, F_PC) : nullptr;
       if ((rc = tn_direction<T, T>(s, s.p, s.fn, d, mu, eps_fixed, eps_rel, o.maxfun, o.cg_rtol))) return rc;
     }
     // ---- OrthogonalNormalization (optimization.py:204-225) -----------------
@@ -475,6 +531,9 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       converged = 0;
       break;
     }
+    // Newton step whose model decrease is below the energy resolution: the
+    // line search cannot judge it from energies; take it as it is.
+    const bool newton_only = o.eres > 0.0 && pred < o.eres * fmax(1.0, fabs(energy));
     // ---- line search over the rotation angle (ValueAndDerivative) ----------
     Dcsrch ls;
     dcs_init(ls, o.c1, o.c2, o.xtol, 0.0, 3.14159265358979323846);
@@ -482,9 +541,12 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     double stp = theta, fval = energy, gval = 2.0 * d0 * dV;
     bool accepted = false;
     int nls;
+    if (newton_only) stp = theta0;
     for (nls = 0; nls < o.maxls; ++nls) {
-      task = dcs_step(ls, stp, fval, gval, task);
-      if (task != DCS_FG) break;
+      if (!newton_only) {
+        task = dcs_step(ls, stp, fval, gval, task);
+        if (task != DCS_FG) break;
+      }
       T* phi = F<T>(s, F_PHI);
       T* p = F<T>(s, F_P);
       T* phi1 = F<T>(s, F_PHI1);
@@ -507,6 +569,14 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
       fval = s.host[S_EN + GB_E_TOTAL];
       gval = 2.0 * s.host[S_A] * dV;
       accepted = true;
+      if (newton_only) {
+        task = DCS_CONV;
+        if (s.verbose)
+          fprintf(stderr, "[gbofdft tn] it %d Newton step %.6e below the energy resolution (pred %.3e, df %.3e)\n",
+                  it, stp, pred, fval - energy);
+        ++nls;
+        break;
+      }
       // energy change below the evaluation's resolution: the sufficient-
       // decrease test cannot be decided, the derivative (computed from the
       // potential, not from energy differences) still can -- accept a step
@@ -600,6 +670,7 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->eres = 0.0;
   o->cg_rtol = 0.1;
   o->pred_next = 0;
+  o->precond = 0;
   return GBOFDFT_OK;
 }
 

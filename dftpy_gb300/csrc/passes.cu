@@ -449,6 +449,27 @@ __global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __r
   }
 }
 
+// Truncated-Newton preconditioner for the phi-space Hessian of a near-uniform
+// density rho0 (diagonal in G): 1 / ((2/3) k_F^2 / F_Lindhard(|G| / 2k_F) + 8 pi rho0 / G^2),
+// the inverse of the kinetic (Lindhard) plus Hartree curvature of the
+// uniform electron gas; 0 at G = 0.
+template <typename T>
+__global__ void k_precond(GInfo g, double rho0, T* __restrict__ out) {
+  const double kf = cbrt(3.0 * kPi * kPi * rho0);
+  const double ckin = 2.0 / 3.0 * kf * kf, tkf = 2.0 * kf, ch = 8.0 * kPi * rho0;
+  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int k2 = (int)(id % g.n2h);
+    const int64_t r = id / g.n2h;
+    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+    const double v = sym_kernel<double>(g, i0, i1, k2, [&](double gg) {
+      return gg > 0.0 ? 1.0 / (ckin * lindhard_inv(sqrt(gg) / tkf, 0.0, 0.0) + ch / gg) : 0.0;
+    });
+    out[id] = (T)v;
+  }
+}
+
 template <typename T> size_t rows_smem(int n2, int nl) { return sizeof(cpx<T>) * ((size_t)n2 + 2 * (size_t)nl * n2); }
 template <typename T> size_t cols_smem(int n, int tb) { return sizeof(cpx<T>) * ((size_t)n + 2 * (size_t)n * tb); }
 
@@ -646,6 +667,16 @@ int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, 
   }
   return p->prec == GBOFDFT_F64 ? cols_conv_t<double>(p, spec, fstride, ld2, nf, kd, scale, st)
                                 : cols_conv_t<float>(p, spec, fstride, ld2, nf, kd, scale, st);
+}
+
+int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
+  GB_REQUIRE(rho0 > 0.0, "preconditioner: rho0 must be positive (got %g)", rho0);
+  const int64_t total = p->NG;
+  const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
+  if (p->prec == GBOFDFT_F64) k_precond<double><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<double*>(out));
+  else k_precond<float><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<float*>(out));
+  GB_CHECK_LAUNCH();
+  return 0;
 }
 
 int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, double beta, void* out,

@@ -66,6 +66,8 @@ DEFAULTS = {
     # refinement of "mixed"; the reference's TN uses 0.1
     "fp32_cg_rtol": 0.1,
     "refine_cg_rtol": 0.1,
+    # preconditioned inner CG in the stages of "mixed" (uniform-gas Hessian)
+    "mixed_precond": True,
 }
 
 
@@ -101,7 +103,7 @@ class Optimization:
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
     def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None,
-             cg_rtol=0.1, pred_next=False):
+             cg_rtol=0.1, pred_next=False, precond=False):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -119,6 +121,7 @@ class Optimization:
         opts.eres = float(eres)
         opts.cg_rtol = float(cg_rtol)
         opts.pred_next = int(bool(pred_next))
+        opts.precond = int(bool(precond))
         spec = self.EnergyEvaluator.spec(rho)
         f = spec.ctypes()
         nb = ctypes.c_int64()
@@ -178,7 +181,7 @@ class Optimization:
             e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"],
                                    pred_stop=0.1 * e32, eres=o["fp32_eres"], ncheck=o["stage_ncheck"],
-                                   cg_rtol=o["fp32_cg_rtol"])
+                                   cg_rtol=o["fp32_cg_rtol"], precond=o["mixed_precond"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
             eps = o["eps"] if o["eps"] is not None else 1e-9
             # the FP32 stage conserves the electron number only to single
@@ -191,7 +194,7 @@ class Optimization:
                 ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.01 * o["econv"]
                 r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
                                    hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["refine_ncheck"],
-                                   cg_rtol=o["refine_cg_rtol"], pred_next=True)
+                                   cg_rtol=o["refine_cg_rtol"], pred_next=True, precond=o["mixed_precond"])
             elif o["refine"] == "fp64":
                 r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
                                    eres=o["refine_eres"])

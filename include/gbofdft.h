@@ -317,6 +317,10 @@ typedef struct gbofdft_tn_options {
   int pred_next;    /* with pred_stop > 0: also stop after a step whose model
                        decrease times cg_rtol is below pred_stop (no reference
                        counterpart); 0: off */
+  int precond;      /* 1: preconditioned inner CG with the inverse phi-space
+                       Hessian of the uniform electron gas at the mean density
+                       (Lindhard kinetic + Hartree curvature, applied by FFT);
+                       no reference counterpart.  0: the reference's plain CG */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {

@@ -125,11 +125,13 @@ _SIGS = [
 EXPORTED = [s[0] for s in _SIGS]
 
 
-def load(path=LIBPATH):
-    """Load the library and bind the signatures (no GPU needed to load)."""
+def load(path=None):
+    """Load the library and bind the signatures (no GPU needed to load).
+    ``GBOFDFT_LIBRARY`` names another build of the library to load instead."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("GBOFDFT_LIBRARY") or LIBPATH
     if not os.path.exists(path):
         raise GbofdftError("%s is missing: build it with `python -m dftpy_gb300.build`" % path)
     L = ctypes.CDLL(path)

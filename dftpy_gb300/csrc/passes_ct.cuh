@@ -29,14 +29,36 @@ __host__ inline bool ct_dispatch(int n, F&& f) {
   }
 }
 
+// Launch-shape parameters (overridable at build time for tuning sweeps)
+#ifndef GB_CT_RP_F32
+#define GB_CT_RP_F32 4
+#endif
+#ifndef GB_CT_TB_F32
+#define GB_CT_TB_F32 16
+#endif
+#ifndef GB_CT_ROWS_MINB
+#define GB_CT_ROWS_MINB 1
+#endif
+#ifndef GB_CT_COLS_MINB
+#define GB_CT_COLS_MINB 1
+#endif
+#ifndef GB_CT_CONV_MINB
+#define GB_CT_CONV_MINB 5   // FP32 convolution pass, N <= 128: >= 5 CTAs/SM (measured best at 128^3; no spills)
+#endif
+
 template <typename T> struct RowsCfg;            // row pairs per CTA (per field)
-template <> struct RowsCfg<float> { static constexpr int RP = 4; };
+template <> struct RowsCfg<float> { static constexpr int RP = GB_CT_RP_F32; };
 template <> struct RowsCfg<double> { static constexpr int RP = 4; };
 // threads of a row-pass CTA: TPL per line, one line per (field, row pair)
 template <typename T, int N> constexpr int rows_threads_max() { return Tpl<N>::value * RowsCfg<T>::RP * GB_MAX_FIELDS; }
 template <typename T, int N> struct ColsCfg {     // columns per tile
-  static constexpr int TB = (sizeof(T) == 4 && N <= 256) ? 16 : 8;
+  static constexpr int TB = (sizeof(T) == 4 && N <= 256) ? GB_CT_TB_F32 : 8;
 };
+// minimum resident CTAs per SM for the column passes (caps registers)
+template <typename T, int N, bool CONV> constexpr int cols_minb() {
+  if constexpr (CONV) return (sizeof(T) == 4 && N <= 128) ? GB_CT_CONV_MINB : 1;
+  else return GB_CT_COLS_MINB;
+}
 
 // A scalar kernel parameter in both precisions, converted on the host: the
 // FP32 kernels then run without double->float conversions, which execute on
@@ -84,7 +106,7 @@ struct CtRowsFwd {
 };
 
 template <typename T, int N>
-__global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_fwd(CtRowsFwd a) {
+__global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_ct_rows_fwd(CtRowsFwd a) {
   constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nl = a.nf * RP;
@@ -232,7 +254,7 @@ __device__ __forceinline__ void pz_lda_ct(T rho, T& eps, T& pot, bool want_e) {
 // FP64 accumulation at all (if-converted, never-taken FP64 code still
 // occupies the FP64 pipe).
 template <typename T, int N, bool WANT_E>
-__global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_eval(CtRowsInv a) {
+__global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_ct_rows_inv_eval(CtRowsInv a) {
   constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nl = (a.nf > 0 ? a.nf : 1) * RP;
@@ -376,7 +398,8 @@ __device__ __forceinline__ void col_quadratic(const float* bg, float m1, float m
 }
 
 template <typename T, int N, int DIR, bool CONV>
-__global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB) k_ct_cols(CtCols a) {
+__global__ void __launch_bounds__(Tpl<N>::value * ColsCfg<T, N>::TB, (cols_minb<T, N, CONV>()))
+k_ct_cols(CtCols a) {
   constexpr int TB = ColsCfg<T, N>::TB, TPL = Tpl<N>::value, NP = Pad<T, N>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);

@@ -65,7 +65,7 @@ DEFAULTS = {
     # inner CG tolerance (r.r < cg_rtol r0.r0) of the FP32 stage and of the
     # refinement of "mixed"; the reference's TN uses 0.1
     "fp32_cg_rtol": 0.1,
-    "refine_cg_rtol": 0.1,
+    "refine_cg_rtol": 0.01,
     # preconditioned inner CG in the stages of "mixed" (uniform-gas Hessian)
     "mixed_precond": True,
 }

@@ -686,6 +686,198 @@ def ewald_forces(grid, positions, charges, pme=True, precision=1e-8, order=10):
 
 
 # ----------------------------------------------------------------------------
+# Stress (3 x 3, Ha/Bohr^3)
+# ----------------------------------------------------------------------------
+def _invq(grid):
+    q = grid.q.copy()
+    z = q == 0
+    q[z] = 1.0
+    out = 1.0 / q
+    out[z] = 0.0
+    return out
+
+
+def _sym(s):
+    for i in range(3):
+        for j in range(i):
+            s[i, j] = s[j, i]
+    return s
+
+
+def lindhard_derivative(eta, mu):
+    """``LindhardDerivative`` (``kedf/kernel.py:197-211``)."""
+    eta = np.asarray(eta, float)
+    out = np.zeros_like(eta)
+    atol = 1.0e-10
+    c0 = (eta > atol) & (np.abs(eta - 1.0) > atol)
+    c1 = eta < atol
+    c2 = np.abs(eta - 1.0) < atol
+    e = eta[c0]
+    t = np.log(np.abs((1.0 + e) / (1.0 - e)))
+    out[c0] = (0.5 / e - 0.25 * (e ** 2 + 1.0) / e ** 2 * t) / (0.5 + 0.25 * (1 - e ** 2) / e * t) ** 2 \
+        + 6.0 * e * mu
+    out[c1] = -2.0 * eta[c1] * (1.0 / 3.0 - 3.0 * mu)
+    out[c2] = -48
+    return out * eta
+
+
+def stress_tf(energy, grid):
+    """``ThomasFermiStress`` (``kedf/tf.py:52-62``)."""
+    return np.eye(3) * (-2.0 / 3.0 * energy / grid.volume)
+
+
+def stress_vw(rho, grid, y=1.0):
+    """``vonWeizsackerStress`` (``kedf/vw.py:97-112``)."""
+    g = grid.g
+    rhoG = fft(rho, grid)
+    d = [ifft(1j * g[i] * rhoG, grid) for i in range(3)]
+    s = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(i, 3):
+            s[i, j] = -0.25 / grid.volume * grid.dV * np.einsum("ijk->", d[i] * d[j] / rho) * y
+    return _sym(s)
+
+
+def stress_wt(rho, grid, energy, y=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0):
+    """``WTStress`` (``kedf/wt.py:75-105``)."""
+    rho0 = rho.mean()
+    g, invgg, q, mask = grid.g, grid.invgg, grid.q, grid.mask
+    tkf = float(2.0 * (3.0 * rho0 * np.pi ** 2) ** (1.0 / 3.0))
+    A = fft(rho ** alpha, grid) / grid.volume
+    B = np.conj(fft(rho ** beta, grid)) / grid.volume
+    dd = lindhard_derivative(q / tkf, y) * A * B
+    s = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(i, 3):
+            fac = 1.0 / 3.0 if i == j else 0.0
+            s[i, j] = np.sum((g[i][mask] * g[j][mask] * invgg[mask] - fac) * dd[mask]).real
+    s = _sym(s) * (np.pi ** 2 / (alpha * beta * rho0 ** (alpha + beta - 2) * tkf / 2.0))
+    return s - np.eye(3) * (2.0 / 3.0 * energy / grid.volume)
+
+
+def stress_lda(rho, grid, energy, pot):
+    """``LDAStress`` (``xc/semilocal_xc.py:308-322``)."""
+    return np.eye(3) * ((energy - np.einsum("ijk,ijk->", pot, rho) * grid.dV) / grid.volume)
+
+
+def stress_hartree(rho, grid, energy):
+    """``HartreeFunctionalStress`` (``hartree.py:68-90``)."""
+    g, invgg, mask = grid.g, grid.invgg, grid.mask
+    rhoG = fft(rho, grid)
+    r2 = (rhoG * np.conj(rhoG) * invgg * invgg).real
+    s = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(i, 3):
+            s[i, j] = np.sum(g[i][mask] * g[j][mask] * r2[mask]) * 8.0 * np.pi / grid.volume ** 2
+    return _sym(s) - np.eye(3) * energy / grid.volume
+
+
+def _vline_deriv(q, table):
+    """``_PP_Derivative_One`` (``pseudo/__init__.py:406-412``): d/dq of the
+    spline of vp[1:] on gp[1:] (its first piece extrapolated below gp[1]),
+    0 from gp[-1] on."""
+    gp, vp = (np.asarray(t, float) for t in table)
+    sp = spline_notaknot(gp[1:], vp[1:])
+    out = np.zeros_like(q)
+    m = q < gp.max()
+    out[m] = spline_eval_deriv(sp, q[m])
+    return out
+
+
+def stress_pp_pme(rho, grid, positions, symbols, tables, energy, order=10):
+    """``LocalPseudo._StressPME`` (``pseudo/__init__.py:525-562``)."""
+    g, mask, q = grid.g, grid.mask, grid.q
+    invq = _invq(grid)
+    rhoGB = np.conj(fft(rho, grid)) * bspline_barray(grid, order)
+    spos = np.linalg.solve(grid.lattice.T, np.asarray(positions).T).T % 1.0
+    s = np.zeros((3, 3))
+    for key in sorted(set(symbols)):
+        idx = [i for i, x in enumerate(symbols) if x == key]
+        Q = pme_qarray(grid, spos[idx], np.ones(len(idx)), order)
+        v = rhoGB * _vline_deriv(q, tables[key]) * fft(Q, grid)
+        for i in range(3):
+            for j in range(i, 3):
+                s[i, j] -= np.sum(g[i][mask] * g[j][mask] * v[mask] * invq[mask]).real / grid.volume ** 2
+    s *= 2.0 * grid.nnr
+    s = _sym(s) - np.eye(3) * energy
+    return s / grid.volume
+
+
+def stress_pp_exact(rho, grid, positions, symbols, tables, energy):
+    """``LocalPseudo._Stress`` (``pseudo/__init__.py:431-455``)."""
+    g, mask, q = grid.g, grid.mask, grid.q
+    invq = _invq(grid)
+    v = np.zeros(grid.nrG, dtype=np.complex128)
+    for key in sorted(set(symbols)):
+        dv = _vline_deriv(q, tables[key])
+        for i, x in enumerate(symbols):
+            if x == key:
+                v += dv * np.conj(np.exp(-1j * np.einsum("lijk,l->ijk", g, positions[i])))
+    rv = fft(rho, grid) * v * invq
+    s = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(i, 3):
+            s[i, j] = -np.sum(g[i][mask] * g[j][mask] * rv[mask]).real / grid.volume * 2.0
+    s = _sym(s) - np.eye(3) * energy
+    return s / grid.volume
+
+
+def ewald_stress(grid, positions, charges, pme=True, precision=1e-8, order=10):
+    """``ewald.stress`` (``ewald.py:523-538``): ``Stress_real`` (``:609-662``) +
+    ``Stress_rec_PME`` (``:915-963``) or ``Stress_rec`` (``:719-760``)."""
+    from scipy.special import erfc, erfcinv
+    pos = np.asarray(positions, float)
+    charges = np.asarray(charges, float)
+    eta = ewald_eta(grid, charges, precision)
+    rmax = erfcinv(precision / 3.0) / np.sqrt(eta)
+    R = _images(grid, rmax)
+    se = np.sqrt(eta)
+    st = np.zeros(6)
+    for ia in range(len(charges)):
+        d = pos[ia][None, None, :] - (pos[None, :, :] - R[:, None, :])
+        dist = np.sqrt((d * d).sum(axis=-1))
+        m = (dist < rmax) & (dist > 0.001)
+        rij, rr = d[m], dist[m]
+        qq = np.broadcast_to(charges[None, :], dist.shape)[m]
+        w = qq * (2 * se / np.sqrt(np.pi) * np.exp(-eta * rr ** 2) + erfc(se * rr) / rr)
+        k = 0
+        for i in range(3):
+            for j in range(i, 3):
+                st[k] += charges[ia] * np.sum(w * rij[:, i] * rij[:, j] / rr ** 2)
+                k += 1
+    st *= -0.5 / grid.volume
+    s = np.zeros((3, 3))
+    k = 0
+    for i in range(3):
+        for j in range(i, 3):
+            s[i, j] = st[k]
+            k += 1
+    g, gg, invgg, mask = grid.g, grid.gg, grid.invgg, grid.mask
+    if pme:
+        spos = np.linalg.solve(grid.lattice.T, pos.T).T % 1.0
+        strf = fft(pme_qarray(grid, spos, charges, order), grid) * bspline_barray(grid, order)
+        scale = 2.0 * 2.0 * np.pi / grid.volume ** 2 / grid.dV ** 2
+    else:
+        strf = np.zeros(grid.nrG, dtype=complex)
+        for i in range(len(charges)):
+            strf += np.exp(-1j * np.einsum("lijk,l->ijk", g, pos[i])) * charges[i]
+        scale = 4.0 * np.pi / grid.volume ** 2
+    s2 = (np.conj(strf) * strf).real
+    w = s2[mask] * np.exp(-gg[mask] / (4.0 * eta)) * invgg[mask]
+    k = 0
+    for i in range(3):
+        for j in range(i, 3):
+            f = g[i][mask] * g[j][mask] * 2.0 * invgg[mask] * (1 + gg[mask] / (4.0 * eta))
+            if i == j:
+                f = f - 1.0
+            s[i, j] += np.sum(w * f) * scale
+            k += 1
+    s_g0 = charges.sum() ** 2 * 4.0 * np.pi * (1.0 / (4.0 * eta * grid.volume ** 2) / 2.0)
+    s += np.eye(3) * s_g0
+    return _sym(s)
+
+
+# ----------------------------------------------------------------------------
 # Total functional
 # ----------------------------------------------------------------------------
 class OFDFT:
@@ -736,6 +928,21 @@ class OFDFT:
             return None, pot
         e = sum(comps[k][0] for k in comps) + self.ewald["energy"]
         return float(e), pot
+
+    def stress(self, rho, split=False):
+        """``TotalFunctional.get_stress`` (``total_functional.py:176-209``)."""
+        g = self.grid
+        comps = self.components(rho, True)
+        out = {"KEDF-TF": stress_tf(comps["TF"][0], g), "KEDF-VW": stress_vw(rho, g, self.y)}
+        if self.wt is not None:
+            out["KEDF-NL"] = stress_wt(rho, g, comps["WT"][0], 1.0, self.wt.alpha, self.wt.beta)
+        out["XC"] = stress_lda(rho, g, comps["XC"][0], comps["XC"][1])
+        out["HARTREE"] = stress_hartree(rho, g, comps["HARTREE"][0])
+        f = stress_pp_pme if self.pme else stress_pp_exact
+        out["PSEUDO"] = f(rho, g, self.positions, self.symbols, self.tables, comps["PSEUDO"][0])
+        out["II"] = ewald_stress(g, self.positions, self.charges, pme=self.pme)
+        out["TOTAL"] = sum(out.values())
+        return out if split else out["TOTAL"]
 
     def forces(self, rho):
         """``TotalFunctional.get_forces`` (``total_functional.py:148-174``), PME."""

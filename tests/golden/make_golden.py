@@ -22,6 +22,8 @@ guess.npz    superposed atomic densities (``get_3d_value_recipe``, PME and
              on the skewed ``Al_fde_rho.pp`` grid (full=True).
 al256_tight.npz  the same 256-atom solve at econv 1e-10 Ha (converged
              energy and forces).
+stress.npz   stress tensors of every term (WT+LDA+Hartree+PP+Ewald, PME and
+             exact) on the skewed test density, and the 4-Al total.
 dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
              (``LineSearchDcsrch2``) on analytic 1-D functions.
 """
@@ -279,6 +281,35 @@ def gen_al256_tight():
     np.savez_compressed(HERE / "al256_tight.npz", **{k: out[k] for k in keep})
 
 
+def gen_stress():
+    """Stress tensors of every term (reference ``TotalFunctional.get_stress``,
+    ``total_functional.py:176-209``) on the reference's test density (skewed
+    cell, full grid) and on the converged 4-Al density."""
+    out = {}
+    ions, rho, _ = io.read_all(refenv.REF_DATA / "Al_fde_rho.pp")
+    grid = rho.grid
+    al = {"Al": AnalyticPP(*systems.SPECIES["Al"])}
+    for pme in (True, False):
+        tag = "pme" if pme else "exact"
+        ps = LocalPseudo(grid=grid, ions=ions, PP_list=al, PME=pme)
+        total = TotalFunctional(KineticEnergyFunctional=Functional(type="KEDF", name="WT"),
+                                XCFunctional=Functional(type="XC", name="LDA"),
+                                HARTREE=Functional(type="HARTREE"), PSEUDO=ps)
+        total(rho, calcType={"E", "V"})    # energies of this density (Hartree caches its own per class)
+        st = total.get_stress(rho, split=True)
+        for k, v in st.items():
+            out["fde_%s_%s" % (tag, k)] = np.asarray(v)
+    a = np.load(HERE / "al4.npz")
+    st4 = systems.config_al4(seed=0)
+    grid, ions, pseudo, total, funcs = build_total(st4, "TFVW")
+    rho4 = DirectField(grid=grid, data=a["rho"])
+    total(rho4, calcType={"E", "V"})
+    for k, v in total.get_stress(rho4, split=True).items():
+        out["al4_" + k] = np.asarray(v)
+    np.savez_compressed(HERE / "stress.npz", **out)
+    print({k: float(np.abs(v).max()) for k, v in out.items()})
+
+
 def gen_dcsrch():
     """Trial-step sequences of the reference line search on 1-D test functions."""
     cases = {
@@ -310,7 +341,7 @@ def gen_dcsrch():
     print("dcsrch: %d cases" % len(cases))
 
 
-GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight}
+GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

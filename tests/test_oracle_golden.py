@@ -161,3 +161,40 @@ def test_density_guess_recipe(golden, case, pme):
     tag = case + ("_pme" if pme else "_exact")
     np.testing.assert_allclose(rho.ravel()[d[case + "_idx"]], d[tag + "_s"], rtol=0, atol=1e-12)
     np.testing.assert_allclose([rho.sum(), (rho * rho).sum()], d[tag + "_c"][:2], rtol=1e-12)
+
+
+@pytest.mark.parametrize("pme", [True, False])
+def test_stress_components_fde(golden, pme):
+    """Every stress term on the reference's skewed test density (full grid)."""
+    d = golden("fde")
+    S = golden("stress")
+    g = O.Grid(d["lattice"], tuple(int(x) for x in d["nr"]), full=True)
+    rho = d["rho"]
+    sym = ["Al"] * len(d["positions"])
+    tab = {"Al": systems.analytic_pp_table(*systems.SPECIES["Al"])}
+    tag = "fde_%s_" % ("pme" if pme else "exact")
+    e_tf, _ = O.tf(rho, g)
+    np.testing.assert_allclose(O.stress_tf(e_tf, g), S[tag + "KEDF-TF"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(O.stress_vw(rho, g), S[tag + "KEDF-VW"], rtol=0, atol=1e-14)
+    e_wt, _ = O.WTNL()(rho, g)
+    np.testing.assert_allclose(O.stress_wt(rho, g, e_wt), S[tag + "KEDF-NL"], rtol=0, atol=1e-14)
+    e_xc, v_xc = O.lda(rho, g)
+    np.testing.assert_allclose(O.stress_lda(rho, g, e_xc, v_xc), S[tag + "XC"], rtol=0, atol=1e-14)
+    e_h, _ = O.hartree(rho, g)
+    np.testing.assert_allclose(O.stress_hartree(rho, g, e_h), S[tag + "HARTREE"], rtol=0, atol=1e-14)
+    v = O.local_pp(g, d["positions"], sym, tab, pme=pme)
+    e_pp = float(np.einsum("ijk,ijk->", v, rho) * g.dV)
+    f = O.stress_pp_pme if pme else O.stress_pp_exact
+    np.testing.assert_allclose(f(rho, g, d["positions"], sym, tab, e_pp), S[tag + "PSEUDO"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(O.ewald_stress(g, d["positions"], d["charges"], pme=pme), S[tag + "II"],
+                               rtol=0, atol=1e-12)
+
+
+def test_stress_total_al4(golden):
+    a = golden("al4")
+    S = golden("stress")
+    st = systems.config_al4(0)
+    ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
+    out = ev.stress(a["rho"], split=True)
+    for k in ("KEDF-TF", "KEDF-VW", "XC", "HARTREE", "PSEUDO", "II", "TOTAL"):
+        np.testing.assert_allclose(out[k], S["al4_" + k], rtol=0, atol=1e-12, err_msg=k)

@@ -109,6 +109,15 @@ _SIGS = [
     ("gbofdft_ewald_forces", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P,
                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int64, _P,
                                             _P]),
+    ("gbofdft_stress_workspace_bytes", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_stress_functional", ctypes.c_int, [_P, _P, ctypes.POINTER(Functional), ctypes.POINTER(ctypes.c_double),
+                                                 _P, ctypes.c_int64, _P, _P]),
+    ("gbofdft_pp_stress", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P,
+                                         ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, ctypes.c_int64, _P,
+                                         _P]),
+    ("gbofdft_ewald_stress", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P,
+                                            ctypes.c_int64, _P, _P]),
     ("gbofdft_tn_options_default", ctypes.c_int, [ctypes.POINTER(TnOptions)]),
     ("gbofdft_tn_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_tn_hess_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
@@ -194,6 +203,12 @@ def aligned_ptr(t, align=256):
 def setup_workspace_bytes(plan, nat):
     n = ctypes.c_int64()
     check(load().gbofdft_setup_workspace_bytes(plan.handle, int(nat), ctypes.byref(n)), "setup_workspace_bytes")
+    return int(n.value)
+
+
+def stress_workspace_bytes(plan, nat):
+    n = ctypes.c_int64()
+    check(load().gbofdft_stress_workspace_bytes(plan.handle, int(nat), ctypes.byref(n)), "stress_workspace_bytes")
     return int(n.value)
 
 

@@ -93,6 +93,13 @@ class KEDF(AbstractFunctional):
             sp.lwt = self._lwt.prepare(rho)
         return sp
 
+    def stress(self, density, split=False, **kwargs):
+        """Stress of the KEDF parts (``KEDF.stress``, ``kedf/__init__.py:186-229``):
+        a dict by part ("TF", "VW", "NL") with ``split``, else their sum."""
+        from .stress import functional_stress
+        out = functional_stress(density, self.spec(density))
+        return out if split else sum(out.values())
+
     def compute(self, density, calcType={"E", "V"}, split=False, **kwargs):
         en, pot = evaluate(density, self.spec(density), calcType)
         out = FunctionalOutput(name="KEDF")

@@ -148,6 +148,29 @@ class LocalPseudo(AbstractFunctional):
         self._vG = vG
         self._vreal[torch.float64] = vR
 
+    def stress(self, rho, energy=None):
+        """Local-pseudopotential stress, 3x3 (``stress``, ``:248-258``: ``_StressPME``
+        with PME, ``_Stress`` without).  ``energy``: E_PSEUDO at rho (computed
+        when not given)."""
+        if rho is None:
+            raise AttributeError("Must specify rho")
+        if not isinstance(rho, DirectField):
+            raise TypeError("rho must be DirectField")
+        if energy is None:
+            energy = self.compute(rho, calcType={"E"}).energy
+        keys, spos, species, tabs, bm = self._device_setup()
+        plan = self.grid.plan(rho.dtype)
+        nat = self.ions.nat
+        nb = _lib.stress_workspace_bytes(plan, nat)
+        work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
+        out = torch.empty(9, dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().gbofdft_pp_stress(
+            plan.handle, _lib.ptr(rho.as_subclass(torch.Tensor).contiguous()), len(keys), tabs, nat,
+            _lib.ptr(spos), _lib.ptr(species), int(self.PME), self.BsplineOrder,
+            _lib.ptr(bm) if bm is not None else None, float(energy), _lib.aligned_ptr(work, 256), nb,
+            _lib.ptr(out), _lib.stream_ptr()), "pp_stress")
+        return out.cpu().numpy().reshape(3, 3)
+
     def forces(self, rho):
         """Forces of the local pseudopotential on the ions, nat x 3 numpy array
         (``forces``, ``:260-271``: ``_ForcePME`` with PME, ``_Force`` without).
@@ -300,6 +323,25 @@ class ewald:
                 _lib.stream_ptr()), "ewald")
             self._parts = [float(x) for x in out.cpu().numpy()]
         return self._parts
+
+    @property
+    def stress(self):
+        """Ion-ion stress, 3x3 (``stress``, ``ewald.py:523-538``): ``Stress_real``
+        plus ``Stress_rec_PME`` or ``Stress_rec``, in FP64."""
+        if getattr(self, "_stress", None) is None:
+            plan = self.grid.plan(torch.float64)
+            rmax, images, pos, spos, q, bm = self._device_setup()
+            nat = self.ions.nat
+            nb = _lib.stress_workspace_bytes(plan, nat)
+            work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
+            out = torch.empty(9, dtype=torch.float64, device="cuda")
+            _lib.check(_lib.load().gbofdft_ewald_stress(
+                plan.handle, nat, _lib.ptr(pos), _lib.ptr(spos), _lib.ptr(q), float(self.eta), float(rmax),
+                _lib.ptr(images), int(images.shape[0]), int(self.PME), int(self.order),
+                _lib.ptr(bm) if bm is not None else None, float(self.ions.get_ncharges()),
+                _lib.aligned_ptr(work, 256), nb, _lib.ptr(out), _lib.stream_ptr()), "ewald_stress")
+            self._stress = out.cpu().numpy().reshape(3, 3)
+        return self._stress
 
     @property
     def forces(self):

@@ -127,3 +127,32 @@ class TotalFunctional(AbstractFunctional):
                 forces["II"] = f
             forces["TOTAL"] = forces["TOTAL"] + f
         return forces if split else forces["TOTAL"]
+
+    def get_stress(self, rho, split=False, **kwargs):
+        """Stress tensor, 3x3 (Ha/Bohr^3) (``get_stress``, ``total_functional.py:176-209``):
+        the KEDF parts under "KEDF-TF", "KEDF-VW", "KEDF-NL", then "XC",
+        "HARTREE", "PSEUDO", the Ewald part under "II" and the sum under
+        "TOTAL" with ``split=True``.  The density terms come from one energy
+        evaluation and one ``gbofdft_stress_functional`` call."""
+        from .stress import functional_stress
+        stress = {"TOTAL": np.zeros((3, 3))}
+        own = [f for f in self.funcDict.values() if isinstance(f, _FUSABLE)]
+        if own:
+            sp = Spec()
+            for f in own:
+                sp = sp.merge(f.spec(rho))
+            en, _ = evaluate(rho, sp, {"E"})
+            parts = functional_stress(rho, sp, en)
+            for k, v in parts.items():
+                stress[("KEDF-" + k) if k in ("TF", "VW", "NL") else k] = v
+            for f in own:
+                if isinstance(f, LocalPseudo):
+                    stress["PSEUDO"] = f.stress(rho, energy=float(en[_lib.E_PSEUDO]))
+        for key, f in self.funcDict.items():
+            if not isinstance(f, _FUSABLE):
+                stress[getattr(f, "type", key)] = f.stress(rho)
+        ew = self.ewald
+        if ew is not None:
+            stress["II"] = ew.stress
+        stress["TOTAL"] = sum(v for k, v in stress.items() if k != "TOTAL")
+        return stress if split else stress["TOTAL"]

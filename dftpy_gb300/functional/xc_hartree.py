@@ -27,6 +27,11 @@ class XC(AbstractFunctional):
         sp.xc = 1
         return sp
 
+    def stress(self, density, **kwargs):
+        """``XC.stress`` -> ``LDAStress`` (``xc/__init__.py:83-88``, ``semilocal_xc.py:308-322``)."""
+        from .stress import functional_stress
+        return functional_stress(density, self.spec(density))["XC"]
+
     def compute(self, density, calcType={"E", "V"}, **kwargs):
         en, pot = evaluate(density, self.spec(density), calcType)
         out = FunctionalOutput(name="XC")
@@ -54,6 +59,11 @@ class Hartree(AbstractFunctional):
         sp = Spec()
         sp.hartree = True
         return sp
+
+    def stress(self, density, **kwargs):
+        """``Hartree.stress`` (``hartree.py:51-90``)."""
+        from .stress import functional_stress
+        return functional_stress(density, self.spec(density))["HARTREE"]
 
     def compute(self, density, calcType={"E", "V"}, **kwargs):
         en, pot = evaluate(density, self.spec(density), calcType)

@@ -293,6 +293,49 @@ int gbofdft_ewald_forces(gbofdft_plan* plan, int nat, const double* pos_dev, con
                          int pme, int order, const double* bm_dev, void* work, int64_t work_bytes,
                          double* forces_dev, void* stream);
 
+/* ---- stress --------------------------------------------------------------- */
+
+/* Device workspace bytes for the stress entry points with nat atoms (0: functional terms only). */
+int gbofdft_stress_workspace_bytes(const gbofdft_plan* plan, int nat, int64_t* bytes);
+
+/*
+ * Stress tensors (Ha/Bohr^3, row-major 3x3) of the density-functional terms
+ * of f at rho: out_dev[0..44] = TF, vW, WT nonlocal, LDA, Hartree (9 doubles
+ * each; zero for disabled terms).  energies: host copy of the energies
+ * gbofdft_eval wrote for this rho (slots GBOFDFT_E_*).  Synchronises the
+ * stream once when WT is enabled (the mean density).  Replaces
+ * ThomasFermiStress, vonWeizsackerStress, WTStress, LDAStress and
+ * HartreeFunctionalStress (src/dftpy/functional/kedf/tf.py:52-62,
+ * kedf/vw.py:97-112, kedf/wt.py:75-105, xc/semilocal_xc.py:308-322,
+ * hartree.py:68-90) as TotalFunctional.get_stress calls them
+ * (total_functional.py:176-209).
+ */
+int gbofdft_stress_functional(gbofdft_plan* plan, const void* rho, const gbofdft_functional* f,
+                              const double energies[GBOFDFT_NE], void* workspace, int64_t workspace_bytes,
+                              double* out_dev, void* stream);
+
+/*
+ * Local-pseudopotential stress (out_dev: 9 doubles), PME or exact structure
+ * factor; e_pp the local-PP energy at rho; other arguments as gbofdft_vloc.
+ * Replaces LocalPseudo.stress -> _StressPME / _Stress
+ * (src/dftpy/functional/pseudo/__init__.py:248-258, 431-455, 525-562).
+ */
+int gbofdft_pp_stress(gbofdft_plan* plan, const void* rho, int nspec, const gbofdft_vtable* tables, int nat,
+                      const double* spos_dev, const int* species_dev, int pme, int order, const double* bm_dev,
+                      double e_pp, void* workspace, int64_t workspace_bytes, double* out_dev, void* stream);
+
+/*
+ * Ewald stress (out_dev: 9 doubles): real-space part plus the PME or exact
+ * reciprocal part and its G = 0 term (charge_sum = sum of the ionic charges);
+ * eta, rmax and the images as for gbofdft_ewald.
+ * Replaces ewald.stress, Stress_real, Stress_rec, Stress_rec_PME
+ * (src/dftpy/ewald.py:523-538, 609-662, 719-760, 915-963).
+ */
+int gbofdft_ewald_stress(gbofdft_plan* plan, int nat, const double* pos_dev, const double* spos_dev,
+                         const double* charges_dev, double eta, double rmax, const double* images_dev, int nimg,
+                         int pme, int order, const double* bm_dev, double charge_sum, void* workspace,
+                         int64_t workspace_bytes, double* out_dev, void* stream);
+
 /* ---- direct density optimisation (truncated Newton) ---------------------- */
 
 /* Options of Optimization(optimization_method="TN") (optimization.py:64-77). */

@@ -383,3 +383,45 @@ def test_config5_lmgp_translation_invariance(api):
     assert float((torch.roll(v0, shifts=1, dims=0) - v1).abs().max()) <= 1e-10 * vmax
     _, e32, _ = energy_potential(st.positions, rho=rho, dtype=torch.float32)
     assert abs(e32 - e0) <= 1e-6 * abs(e0), (e0, e32)
+
+
+@pytest.mark.parametrize("pme", [True, False])
+def test_stress_fde_matches_reference(api, golden, pme):
+    """Every stress term (WT + LDA + Hartree + PP + Ewald) on the reference's
+    skewed test density (full grid), FP64: within 1e-11 Ha/Bohr^3 of the
+    reference's tensors (values ~1e-3)."""
+    F = api["functional"]
+    d = golden("fde")
+    S = golden("stress")
+    grid = api["grid"].DirectGrid(d["lattice"], tuple(int(x) for x in d["nr"]), full=True)
+    ions = api["ions"].Ions(["Al", "Al"], positions=d["positions"], cell=d["lattice"])
+    ps = F.LocalPseudo(grid=grid, ions=ions, PP_list=_pp(api, ["Al"]), PME=pme)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="WT"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho = api["field"].DirectField(grid, data=np.ascontiguousarray(d["rho"]))
+    out = total.get_stress(rho, split=True)
+    tag = "fde_%s_" % ("pme" if pme else "exact")
+    for k in ("KEDF-TF", "KEDF-VW", "KEDF-NL", "XC", "HARTREE", "PSEUDO", "II", "TOTAL"):
+        np.testing.assert_allclose(out[k], S[tag + k], rtol=0, atol=1e-11, err_msg=k)
+
+
+def test_stress_al4_total_and_fp32(api, golden):
+    """4-Al converged density (TFVW): the total stress against the reference
+    (1e-11); the FP32 path to 1e-7 Ha/Bohr^3."""
+    torch = api["torch"]
+    F = api["functional"]
+    a = golden("al4")
+    S = golden("stress")
+    st = systems.config_al4(0)
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = F.LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="TFVW"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho = api["field"].DirectField(grid, data=np.ascontiguousarray(a["rho"]))
+    out = total.get_stress(rho, split=True)
+    for k in ("KEDF-TF", "KEDF-VW", "XC", "HARTREE", "PSEUDO", "II", "TOTAL"):
+        np.testing.assert_allclose(out[k], S["al4_" + k], rtol=0, atol=1e-11, err_msg=k)
+    s32 = total.get_stress(rho.to(torch.float32))
+    assert np.abs(s32 - S["al4_TOTAL"]).max() < 1e-7

@@ -6,6 +6,7 @@ the host builds the per-species 1-D spline tables, the PME b(m) factors and
 the Ewald scalars (eta, cutoff, lattice images, correction term).
 """
 import math
+import os
 
 import numpy as np
 import torch
@@ -51,14 +52,16 @@ class AnalyticPP:
 
 
 def _read_pp(obj):
+    """(gp, vp, zval) of a PP_list entry: a file path (recpot, psp8/psp6,
+    UPF v2; ``ReadPseudo._init_pp``, ``pseudo/__init__.py:726-779``) or a
+    ``BasePseudo``-like object; real-space tables are transformed to |G|
+    (``_real2recip``) on the host."""
+    from ..pseudo_files import read_pp, reciprocal_atomic_density, reciprocal_table
     if isinstance(obj, (str, bytes)) or hasattr(obj, "__fspath__"):
-        raise NotImplementedError("pseudopotential files (%s) are not read by this build; pass an object with "
-                                  "radial_grid / local_potential / zval in reciprocal space" % (obj,))
-    if getattr(obj, "direct", False):
-        raise NotImplementedError("real-space pseudopotential tables are not part of this path")
-    gp = np.asarray(obj.radial_grid, dtype=float)
-    vp = np.asarray(obj.local_potential, dtype=float)
-    return gp, vp, float(obj.zval)
+        obj = read_pp(os.fsdecode(obj))
+    gp, vp, z = reciprocal_table(obj)
+    atom = reciprocal_atomic_density(obj) if hasattr(obj, "atomic_density") else None
+    return gp, vp, z, atom
 
 
 class _VTable:
@@ -101,6 +104,10 @@ class LocalPseudo(AbstractFunctional):
         self.PP_list = dict(PP_list)
         self._pp = {k: _read_pp(v) for k, v in self.PP_list.items()}
         self.zval = {k: v[2] for k, v in self._pp.items()}
+        # reciprocal-space atomic densities of the species whose files have
+        # one (read by DensityGenerator(pseudo=...), density.py:114-134)
+        self._atomic_density_grid = {k: v[3][0] for k, v in self._pp.items() if v[3] is not None}
+        self._atomic_density = {k: v[3][1] for k, v in self._pp.items() if v[3] is not None}
         self.ions = Ions.from_any(ions)
         for key in self.ions.symbols_uniq:
             if key not in self._pp:

@@ -24,6 +24,9 @@ al256_tight.npz  the same 256-atom solve at econv 1e-10 Ha (converged
              energy and forces).
 stress.npz   stress tensors of every term (WT+LDA+Hartree+PP+Ewald, PME and
              exact) on the skewed test density, and the 4-Al total.
+pseudo_files.npz  reciprocal tables of the reference's example pseudopotential
+             files as its ReadPseudo builds them (needs the ``xmltodict``
+             stand-in in ``_shims`` for UPF).
 dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
              (``LineSearchDcsrch2``) on analytic 1-D functions.
 """
@@ -310,6 +313,29 @@ def gen_stress():
     print({k: float(np.abs(v).max()) for k, v in out.items()})
 
 
+def gen_pseudo_files():
+    """Reciprocal-space tables the reference's ReadPseudo builds from its own
+    example pseudopotential files (recpot, psp8, UPF v2; ``_init_pp``,
+    ``pseudo/__init__.py:726-779``), sampled."""
+    from dftpy.functional.pseudo import ReadPseudo
+    out = {}
+    for f in ("al.lda.recpot", "Al_lda.oe01.recpot", "al.lda.psp", "al.lda.upf", "Mg_OEPP_PZ.UPF"):
+        key = "Al" if f.lower().startswith("al") else "Mg"
+        rp = ReadPseudo({key: str(refenv.REF_DATA / f)})
+        tag = f.replace(".", "_")
+        gp, vp = rp._gp[key], rp._vp[key]
+        out[tag + "_zval"] = float(rp._zval[key])
+        out[tag + "_n"] = gp.size
+        idx = np.unique(np.linspace(0, gp.size - 1, 400).astype(int))
+        out[tag + "_idx"] = idx
+        out[tag + "_gp"] = gp[idx]
+        out[tag + "_vp"] = vp[idx]
+        if rp._atomic_density.get(key) is not None:
+            out[tag + "_rho_gp"] = rp._atomic_density_grid[key][idx]
+            out[tag + "_rho"] = rp._atomic_density[key][idx]
+    np.savez_compressed(HERE / "pseudo_files.npz", **out)
+
+
 def gen_dcsrch():
     """Trial-step sequences of the reference line search on 1-D test functions."""
     cases = {
@@ -341,7 +367,7 @@ def gen_dcsrch():
     print("dcsrch: %d cases" % len(cases))
 
 
-GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress}
+GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

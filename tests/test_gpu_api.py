@@ -425,3 +425,24 @@ def test_stress_al4_total_and_fp32(api, golden):
         np.testing.assert_allclose(out[k], S["al4_" + k], rtol=0, atol=1e-11, err_msg=k)
     s32 = total.get_stress(rho.to(torch.float32))
     assert np.abs(s32 - S["al4_TOTAL"]).max() < 1e-7
+
+
+def test_local_pseudo_from_recpot_file(api, tmp_path):
+    """A pseudopotential given as a recpot file path: the device v_loc equals
+    the oracle's for the table the file holds (FP64, 1e-10 of max|v|)."""
+    from dftpy_gb300 import pseudo_files as P
+    st = systems.config_al4(0)
+    gp = np.linspace(0.0, 30.0, 6001)
+    vp = np.empty_like(gp)
+    vp[1:] = -4.0 * np.pi * 3.0 * np.exp(-(gp[1:] * 1.0) ** 2 / 4.0) / gp[1:] ** 2
+    vp[0] = np.pi * 3.0
+    path = str(tmp_path / "al.recpot")
+    P.write_recpot(path, gp, vp)
+    pp = P.read_pp(path)
+    assert pp.zval == 3.0
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = api["functional"].LocalPseudo(grid=grid, ions=_ions(api, st), PP_list={"Al": path}, PME=True)
+    g = O.Grid(st.lattice, st.nr)
+    ref = O.local_pp(g, st.positions, st.symbols, {"Al": (pp.radial_grid, pp.local_potential)}, pme=True)
+    v = ps.vreal.to_numpy()
+    assert np.abs(v - ref).max() <= 1e-10 * np.abs(ref).max()

@@ -123,6 +123,20 @@ class LocalPseudo(AbstractFunctional):
         species = torch.tensor([keys.index(s) for s in self.ions.symbols], dtype=torch.int32, device="cuda")
         return keys, spos, species
 
+    def restart(self, grid=None, ions=None, full=False, duplicate=False):
+        """Drop the cached v_loc, device inputs and Ewald sum and take new ions
+        and/or grid (``restart``, ``pseudo/__init__.py:152-175``): the next use
+        recomputes them for the new positions."""
+        if ions is not None:
+            self.ions = Ions.from_any(ions)
+            self.ions.set_charges(self.zval)
+        if grid is not None:
+            self.grid = grid
+        self._vreal = {}
+        self._vG = None
+        self._dev = None
+        self.ewald = None
+
     def _device_setup(self):
         """Device copies of the positions, species, v(|G|) tables and PME b(m)."""
         if getattr(self, "_dev", None) is None:

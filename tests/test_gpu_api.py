@@ -446,3 +446,57 @@ def test_local_pseudo_from_recpot_file(api, tmp_path):
     ref = O.local_pp(g, st.positions, st.symbols, {"Al": (pp.radial_grid, pp.local_potential)}, pme=True)
     v = ps.vreal.to_numpy()
     assert np.abs(v - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+class _Atoms:
+    """The few ``ase.Atoms`` members the calculator reads (Angstrom)."""
+
+    def __init__(self, symbols, positions, cell):
+        self.symbols = list(symbols)
+        self.positions = np.array(positions, float)
+        self.cell = np.array(cell, float)
+
+    def get_positions(self):
+        return self.positions.copy()
+
+    def get_chemical_symbols(self):
+        return list(self.symbols)
+
+
+def test_ase_calculator_forces_are_energy_gradient(api):
+    """DFTpyCalculator (evaluator path) on 4 Al: forces equal the central
+    difference of the optimised energy (eV/A), and the second ionic step,
+    starting from the first step's density, takes fewer evaluations than the
+    first one from the uniform density."""
+    from dftpy_gb300.api4ase import DFTpyCalculator
+    from dftpy_gb300.pseudo_files import BOHR_ANG
+    F = api["functional"]
+    st = systems.config_al4(0)
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = F.LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="TFVW"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho0 = api["field"].DirectField(grid)
+    rho0[:] = st.nelec / st.volume
+    opt = api["opt"].Optimization(EnergyEvaluator=total, optimization_method="TN",
+                                  optimization_options={"econv": 1e-10, "maxfun": 50, "maxiter": 200})
+    calc = DFTpyCalculator(evaluator=total, optimizer=opt, rho=rho0)
+    atoms = _Atoms(st.symbols, st.positions * BOHR_ANG, st.lattice * BOHR_ANG)
+    calc.get_potential_energy(atoms)
+    n_first = sum(s["n_eval_ev"] + s["n_eval_v"] for s in opt.stats["stages"])
+    f = calc.get_forces(atoms)
+    assert f.shape == (4, 3)
+    h = 0.004
+    e = []
+    for sgn in (1, -1):
+        a = _Atoms(st.symbols, st.positions * BOHR_ANG, st.lattice * BOHR_ANG)
+        a.positions[0, 0] += sgn * h
+        e.append(calc.get_potential_energy(a))
+        if sgn == 1:
+            n_second = sum(s["n_eval_ev"] + s["n_eval_v"] for s in opt.stats["stages"])
+    fd = -(e[0] - e[1]) / (2 * h)
+    assert abs(fd - f[0, 0]) < 2e-3 + 1e-2 * abs(f[0, 0]), (fd, f[0, 0])
+    assert n_second < n_first
+    s = calc.get_stress(atoms)
+    assert s.shape == (6,)

@@ -220,6 +220,36 @@ class Optimization:
         self._functional = None
         return r
 
+    def optimize_rho_multistep(self, guess_rho, multistep=2, nr_final=None):
+        """Coarse-to-fine optimisation (the multi-step branch of
+        ``OptimizeDensityConf``, ``interface.py:160-200``): optimise on the
+        guess's grid, then ``multistep - 1`` times double the grid (the last
+        step goes to ``nr_final`` when given), interpolate the density's
+        spectrum onto it (``field2distrib``), rescale it to the electron
+        count, move the local pseudopotential to the new grid and optimise
+        again.  Returns the density on the finest grid."""
+        from .grid import DirectGrid
+        from .utils import field2distrib
+        if multistep < 1:
+            raise ValueError("multistep must be >= 1")
+        charge_total = float(np.sum(guess_rho.integral()))
+        rho = self.optimize_rho(guess_rho=guess_rho)
+        nr = np.array(guess_rho.grid.nrR, dtype=int)
+        for istep in range(2, multistep + 1):
+            if istep == multistep and nr_final is not None:
+                nr = np.array(nr_final, dtype=int)
+            else:
+                nr = nr * 2
+            grid2 = DirectGrid(lattice=rho.grid.lattice, nr=nr, full=rho.grid.full)
+            rho_ini = DirectField(grid2, rank=rho.rank, dtype=rho.dtype)
+            field2distrib(rho, rho_ini, root=0)
+            rho_ini = rho_ini * (charge_total / float(np.sum(rho_ini.integral())))
+            for f in self.EnergyEvaluator.funcDict.values():
+                if getattr(f, "type", None) == "PSEUDO":
+                    f.restart(full=False, ions=f.ions, grid=grid2)
+            rho = self.optimize_rho(guess_rho=rho_ini)
+        return rho
+
     def _natoms(self):
         for f in self.EnergyEvaluator.funcDict.values():
             if getattr(f, "type", None) == "PSEUDO":

@@ -20,7 +20,7 @@ import numpy as np
 # Hartree (eV) and Bohr (A) from the CODATA 2014 constants, derived as ase's
 # units module does (the reference converts recpot files with them)
 _C, _MU0 = 299792458.0, 4.0e-7 * np.pi
-_EPS0 = 1.0 / (_MU0 * _C * _C)
+_EPS0 = 1.0 / _MU0 / _C ** 2
 _HBAR = 6.626070040e-34 / (2.0 * np.pi)
 _E, _ME = 1.6021766208e-19, 9.10938356e-31
 BOHR_ANG = 4.0e10 * np.pi * _EPS0 * _HBAR ** 2 / _ME / _E ** 2

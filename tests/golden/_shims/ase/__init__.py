@@ -13,6 +13,13 @@ import numpy as np
 from . import units  # noqa: F401
 from .cell import Cell
 
+# element symbols indexed by atomic number (0 is a placeholder)
+_SYMBOLS = (
+    "X H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
+    "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb "
+    "Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn Fr Ra Ac Th Pa U Np Pu Am Cm Bk Cf Es Fm Md No Lr Rf "
+    "Db Sg Bh Hs Mt Ds Rg Cn Nh Fl Mc Lv Ts Og").split()
+
 
 class _Symbols(list):
     def __eq__(self, other):
@@ -35,6 +42,8 @@ class Atoms:
         self.cell = Cell(np.zeros((3, 3)) if cell is None else cell)
         if isinstance(symbols, str):
             symbols = [symbols]
+        if symbols is None and numbers is not None:
+            symbols = [_SYMBOLS[int(z)] for z in numbers]
         self._symbols = _Symbols(symbols or [])
         n = len(self._symbols)
         self.arrays = {}
@@ -68,6 +77,10 @@ class Atoms:
     @property
     def symbols(self):
         return self._symbols
+
+    @property
+    def numbers(self):
+        return np.array([_SYMBOLS.index(s) for s in self._symbols], dtype=int)
 
     def get_chemical_symbols(self):
         return list(self._symbols)

@@ -9,7 +9,7 @@ import math
 
 _c = 299792458.0                 # speed of light, m/s
 _mu0 = 4.0e-7 * math.pi          # vacuum permeability
-_eps0 = 1.0 / (_mu0 * _c * _c)   # vacuum permittivity
+_eps0 = 1.0 / _mu0 / _c ** 2     # vacuum permittivity (evaluated in ase's order)
 _hplanck = 6.626070040e-34       # Planck constant, J s
 _hbar = _hplanck / (2.0 * math.pi)
 _e = 1.6021766208e-19            # elementary charge, C

@@ -336,6 +336,106 @@ def gen_pseudo_files():
     np.savez_compressed(HERE / "pseudo_files.npz", **out)
 
 
+def gen_formats():
+    """Density files: what the reference's readers return for its example
+    files (``formats/qepp.py``, ``xsf.py``; checksums and samples), and the
+    files its writers make (qepp, xsf, snpy) for a small seeded field, kept
+    byte for byte under ``formats/`` with the arrays they were made from."""
+    from dftpy.field import DirectField
+    from dftpy.formats import io, qepp, snpy, xsf
+    from dftpy.grid import DirectGrid
+    from dftpy.ions import Ions
+    from numpy.lib import format as npyf
+    if not hasattr(npyf, "_check_version"):
+        # the reference's npy module calls this private numpy helper (gone in
+        # numpy 2.x); it only validates the format version
+        def _check_version(version):
+            if version not in [(1, 0), (2, 0), (3, 0), None]:
+                raise ValueError("we only support format version (1,0), (2,0), and (3,0), not %s" % (version,))
+        npyf._check_version = _check_version
+    out = {}
+    for f in ("Al_fde_rho.pp", "GaAs_random.xsf", "al_random.xsf", "ti.xsf"):
+        tag = f.replace(".", "_")
+        for dt in ("density", "potential"):
+            ions, field, info = io.read_all(str(refenv.REF_DATA / f), data_type=dt)
+            v = np.asarray(field)
+            key = tag + ("" if dt == "density" else "_pot")
+            out[key + "_shape"] = np.array(v.shape)
+            out[key + "_sum"] = float(v.sum())
+            out[key + "_sumsq"] = float((v * v).sum())
+            idx = sample_index(v.size, seed=7)[:300]
+            out[key + "_idx"] = idx
+            out[key + "_samples"] = v.ravel()[idx]
+        out[tag + "_lattice"] = np.asarray(field.grid.lattice)
+        out[tag + "_full"] = bool(field.grid.full)
+        out[tag + "_cell"] = np.asarray(ions.cell)
+        out[tag + "_pos"] = np.asarray(ions.positions)
+        out[tag + "_symbols"] = np.array(list(ions.get_chemical_symbols()))
+        if info is not None:
+            for k, val in info.items():
+                out[tag + "_info_" + k] = np.asarray(val)
+    # writers on a small seeded field
+    rng = np.random.default_rng(2024)
+    cell = np.array([[7.1, 0.0, 0.0], [0.3, 6.6, 0.0], [0.2, -0.4, 8.3]])
+    pos = rng.random((3, 3)) @ cell
+    nr = np.array([6, 5, 4])
+    grid = DirectGrid(lattice=cell, nr=nr, full=False)
+    rho = DirectField(grid=grid, griddata_3d=0.01 + rng.random(tuple(nr)))
+    ions = Ions(symbols=["Ga", "As", "Ga"], positions=pos, cell=cell)
+    ions.set_charges({"Ga": 3.0, "As": 5.0})
+    d = HERE / "formats"
+    d.mkdir(exist_ok=True)
+    qepp.write_qepp(str(d / "small_density.pp"), ions=ions, data=rho)
+    qepp.write_qepp(str(d / "small_potential.pp"), ions=ions, data=rho, data_type="potential")
+    xsf.write_xsf(str(d / "small_density.xsf"), ions=ions, data=rho)
+    xsf.write_xsf(str(d / "small_potential.xsf"), ions=ions, data=rho, data_type="potential")
+    rho2 = DirectField(grid=grid, rank=2, griddata_3d=np.stack([np.asarray(rho), 2.0 * np.asarray(rho)]))
+    xsf.write_xsf(str(d / "small_spin.xsf"), ions=ions, data=rho2)
+    snpy.write(str(d / "small.snpy"), ions=ions, data=rho)
+    out["small_cell"] = cell
+    out["small_pos"] = pos
+    out["small_rho"] = np.asarray(rho)
+    out["small_symbols"] = np.array(ions.get_chemical_symbols())
+    for f in ("small_density.pp", "small_potential.pp", "small_density.xsf", "small_potential.xsf", "small_spin.xsf",
+              "small.snpy"):
+        dt = "potential" if "potential" in f else "density"
+        i2, fld, _ = io.read_all(str(d / f), data_type=dt)
+        tag = f.replace(".", "_")
+        out[tag + "_read"] = np.asarray(fld)
+        out[tag + "_read_lattice"] = np.asarray(fld.grid.lattice)
+        out[tag + "_read_pos"] = np.asarray(i2.positions)
+        out[tag + "_read_cell"] = np.asarray(i2.cell)
+    np.savez_compressed(HERE / "formats.npz", **out)
+
+
+def gen_gridmap():
+    """Spectral interpolation between grids (``grid_map_data``,
+    ``field2distrib``, ``utils/utils.py:80-129, 218-287``) for half and full
+    spectra, coarse to fine and fine to coarse, odd and even sizes."""
+    from dftpy.field import DirectField
+    from dftpy.grid import DirectGrid
+    from dftpy.utils.utils import field2distrib, grid_map_data
+    rng = np.random.default_rng(77)
+    cell = np.array([[6.2, 0.0, 0.0], [0.4, 5.9, 0.0], [-0.3, 0.2, 7.1]])
+    out = {"cell": cell}
+    cases = [("up", (8, 6, 5), (12, 10, 9)), ("up_even", (8, 6, 6), (16, 12, 12)), ("down", (12, 10, 9), (8, 6, 5)),
+             ("down_even", (16, 12, 12), (10, 8, 6))]
+    for full in (False, True):
+        for name, nr1, nr2 in cases:
+            tag = name + ("_full" if full else "_half")
+            g1 = DirectGrid(lattice=cell, nr=nr1, full=full)
+            x = rng.random(nr1) + 0.5
+            f1 = DirectField(grid=g1, griddata_3d=x)
+            y = grid_map_data(f1, nr=np.array(nr2))
+            out[tag + "_in"] = x
+            out[tag + "_out"] = np.asarray(y)
+            g2 = DirectGrid(lattice=cell, nr=nr2, full=full)
+            o2 = DirectField(grid=g2)
+            field2distrib(f1, o2, root=0, tol=0.8)
+            out[tag + "_distrib"] = np.asarray(o2)
+    np.savez_compressed(HERE / "gridmap.npz", **out)
+
+
 def gen_dcsrch():
     """Trial-step sequences of the reference line search on 1-D test functions."""
     cases = {
@@ -367,7 +467,7 @@ def gen_dcsrch():
     print("dcsrch: %d cases" % len(cases))
 
 
-GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files}
+GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files, "formats": gen_formats, "gridmap": gen_gridmap}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

@@ -500,3 +500,46 @@ def test_ase_calculator_forces_are_energy_gradient(api):
     assert n_second < n_first
     s = calc.get_stress(atoms)
     assert s.shape == (6,)
+
+
+@pytest.mark.parametrize("full", [False, True])
+@pytest.mark.parametrize("case", ["up", "up_even", "down", "down_even"])
+def test_grid_map_matches_reference(api, golden, case, full):
+    """Spectral interpolation between grids against the reference's
+    grid_map_data / field2distrib (half and full spectra, both directions)."""
+    from dftpy_gb300.utils import field2distrib, grid_map_data
+    d = golden("gridmap")
+    tag = case + ("_full" if full else "_half")
+    x, ref = d[tag + "_in"], d[tag + "_out"]
+    g1 = api["grid"].DirectGrid(d["cell"], x.shape, full=full)
+    f1 = api["field"].DirectField(g1, data=x)
+    y = grid_map_data(f1, nr=np.array(ref.shape))
+    assert tuple(y.shape) == ref.shape and y.grid.full == full
+    np.testing.assert_allclose(y.to_numpy(), ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    o2 = api["field"].DirectField(api["grid"].DirectGrid(d["cell"], ref.shape, full=full))
+    field2distrib(f1, o2, tol=0.8)
+    np.testing.assert_allclose(o2.to_numpy(), d[tag + "_distrib"], rtol=0, atol=1e-13 * np.abs(ref).max())
+
+
+def test_multistep_al4_reaches_fine_grid_minimum(api, golden):
+    """Coarse (16^3) then fine (32^3) TN solve ends at the reference's 32^3
+    minimum: same energy and density as the direct fine-grid solve."""
+    a = golden("al4")
+    st = systems.config_al4(0)
+    F = api["functional"]
+    grid = api["grid"].DirectGrid(st.lattice, (16, 16, 16), full=False)
+    ps = F.LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="TFVW"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho0 = api["field"].DirectField(grid)
+    rho0[:] = st.nelec / st.volume
+    opt = api["opt"].Optimization(EnergyEvaluator=total, optimization_method="TN",
+                                  optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100})
+    rho = opt.optimize_rho_multistep(rho0, multistep=2, nr_final=tuple(st.nr))
+    assert tuple(rho.grid.nrR) == tuple(st.nr) and ps.grid is rho.grid
+    assert opt.converged == 0
+    assert abs(rho.integral() - st.nelec) < 1e-9
+    E = total.Energy(rho)
+    assert abs(E - float(a["E_final"])) < 1e-7
+    assert np.abs(rho.to_numpy() - a["rho"]).max() < 1e-4

@@ -55,7 +55,10 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc, "-c", src, "-o", obj] + ARCH + NVFLAGS
+        # GBOFDFT_NVCC_DEFINES: extra -D tuning macros (launch shapes, radix
+        # schedules) for sweeps; the defaults are the tuned values
+        extra = os.environ.get("GBOFDFT_NVCC_DEFINES", "").split()
+        cmd = [cc, "-c", src, "-o", obj] + ARCH + NVFLAGS + [d for d in extra if d.startswith("-D")]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,6 +1,7 @@
 // C ABI entry points: plans, FFTs, the fused functional evaluation.
 #include <math.h>
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -92,6 +93,7 @@ int gbofdft_plan_destroy(gbofdft_plan* p) {
   if (p->spec) cudaFree(p->spec);
   if (p->partials) cudaFree(p->partials);
   if (p->scratch) cudaFree(p->scratch);
+  if (p->wt_pm) cudaFree(p->wt_pm);
   delete p;
   return GBOFDFT_OK;
 }
@@ -180,6 +182,10 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   memcpy(p->gi.bg, p->bg, sizeof(p->bg));
   p->gi.n0 = nr[0]; p->gi.n1 = nr[1]; p->gi.n2 = nr[2]; p->gi.n2h = p->n2h; p->gi.ld2 = p->ld2;
   p->gi.full = p->full;
+  // FP32 grids whose (n0, n1) plane fits in shared memory evaluate through
+  // the plane pipeline (GBOFDFT_PLANE=0 selects the column passes instead)
+  const char* pe = getenv("GBOFDFT_PLANE");
+  p->plane = precision == GBOFDFT_F32 && !(pe && pe[0] == '0') && gb_plane_supported_f32(nr[0], nr[1], nr[2]);
   *out = p;
   return GBOFDFT_OK;
 }
@@ -262,7 +268,16 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
     ++nf;
   }
   const int64_t fs = p->NGld;
-  int rc = 0;
+  int rc = gb_eval_plane(p, rho, nf, ops, f->wt_beta, kd, ev, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies,
+                         st);
+  if (rc == 0) {
+    if (f->lwt)
+      rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0,
+                       (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
+    return rc;
+  }
+  if (rc != 1) return rc;
+  rc = 0;
   if (nf > 0) {
     rc = gb_rows_fwd(p, rho, p->spec, fs, p->ld2, nf, ops, f->wt_beta, 1.0, st);
     if (!rc) rc = gb_cols(p, p->spec, fs, p->ld2, nf, 1, -1, 1.0, st);

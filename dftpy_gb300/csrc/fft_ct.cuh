@@ -53,6 +53,40 @@ template <> struct Plan<360> { using S = Sched<8, 5, 3, 3>; static constexpr int
 
 template <int N> struct Tpl { static constexpr int value = N / Plan<N>::R0; };
 
+// 16-point DFT as 4 x 4: four stride-4 DFT4s, twiddles W16^(m k1), then a
+// DFT4 across them (X[k1 + 4 k2]); W16 = exp(DIR 2 pi i / 16).
+template <int DIR, typename T>
+__device__ __forceinline__ void dft16(cpx<T>* u) {
+  const T c = (T)0.92387953251128675613;   // cos(pi / 8)
+  const T s = (T)0.38268343236508977173;   // sin(pi / 8)
+  const T h = (T)GB_R2;
+  const T d = DIR < 0 ? (T)-1 : (T)1;
+  const cpx<T> w1 = {c, d * s}, w2 = {h, d * h}, w3 = {s, d * c}, w6 = {-h, d * h}, w9 = {-c, -d * s};
+  cpx<T> q[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[m][j] = u[m + 4 * j];
+    dft4<DIR, T>(q[m]);
+  }
+  q[1][1] = c_mul(q[1][1], w1);
+  q[1][2] = c_mul(q[1][2], w2);
+  q[1][3] = c_mul(q[1][3], w3);
+  q[2][1] = c_mul(q[2][1], w2);
+  q[2][2] = c_rot<DIR>(q[2][2]);
+  q[2][3] = c_mul(q[2][3], w6);
+  q[3][1] = c_mul(q[3][1], w3);
+  q[3][2] = c_mul(q[3][2], w6);
+  q[3][3] = c_mul(q[3][3], w9);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    cpx<T> e[4] = {q[0][k1], q[1][k1], q[2][k1], q[3][k1]};
+    dft4<DIR, T>(e);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) u[k1 + 4 * k2] = e[k2];
+  }
+}
+
 template <int DIR, typename T, int R>
 __device__ __forceinline__ void dft(cpx<T>* u) {
   if constexpr (R == 2) dft2<DIR, T>(u);
@@ -60,6 +94,7 @@ __device__ __forceinline__ void dft(cpx<T>* u) {
   else if constexpr (R == 4) dft4<DIR, T>(u);
   else if constexpr (R == 5) dft5<DIR, T>(u);
   else if constexpr (R == 8) dft8<DIR, T>(u);
+  else if constexpr (R == 16) dft16<DIR, T>(u);
   else static_assert(R == 2, "radix not implemented");
 }
 

@@ -435,7 +435,10 @@ __device__ double lindhard_inv(double eta, double lbda, double mu) {
 }
 
 template <typename T>
-__global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __restrict__ out) {
+// out: half-spectrum layout; out_pm (optional): the same values plane-major,
+// (k2 * n0 + i0) * n1 + i1
+__global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __restrict__ out,
+                            T* __restrict__ out_pm) {
   const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
   for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
        id += (int64_t)gridDim.x * blockDim.x) {
@@ -446,6 +449,7 @@ __global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __r
       return lindhard_inv(sqrt(gg) / tkf, x, 1.0) * factor;
     });
     out[id] = (T)v;
+    if (out_pm) out_pm[(int64_t)k2 * g.n0 * g.n1 + r] = (T)v;
   }
 }
 
@@ -669,6 +673,30 @@ int gb_cols_conv(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, 
                                 : cols_conv_t<float>(p, spec, fstride, ld2, nf, kd, scale, st);
 }
 
+int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, double beta, const KerDesc& kd,
+                  const EvalDesc& ev, const void* vloc, void* pot, int calc_e, double* energies, cudaStream_t st) {
+  if (!p->plane || p->prec != GBOFDFT_F32 || nf <= 0 || !gb_use_ct()) return 1;
+  const float* pm_arr[GB_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
+  for (int f = 0; f < nf; ++f) {
+    if (kd.type[f] != KER_ARRAY) continue;
+    if (!p->wt_pm || kd.arr[f] != p->wt_pm_src) return 1;
+    pm_arr[f] = p->wt_pm;
+  }
+  const int64_t fs = p->NG;
+  int rc = gb_ct_rows_fwd_pm_f32(p, rho, p->spec, fs, nf, ops, beta, st);
+  if (!rc) rc = gb_plane_conv_f32(p, p->spec, fs, nf, &kd, pm_arr, 1.0 / (double)p->N, st);
+  if (rc) return rc == 1 ? gb_set_error(GBOFDFT_ERR_STATE, "plane pipeline: size without specialisation") : rc;
+  int64_t nblk = 0;
+  rc = gb_ct_rows_inv_eval_pm_f32(p, p->spec, fs, nf, &ev, rho, vloc, pot, calc_e, p->partials, &nblk, st);
+  if (rc) return rc == 1 ? gb_set_error(GBOFDFT_ERR_STATE, "plane pipeline: size without specialisation") : rc;
+  if (calc_e) {
+    if (nblk > p->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
+    k_energy_final<<<6, 256, 0, st>>>(p->partials, nblk, p->dV, ev.e_ion, energies, gb_plan_counter(p));
+    GB_CHECK_LAUNCH();
+  }
+  return 0;
+}
+
 int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
   GB_REQUIRE(rho0 > 0.0, "preconditioner: rho0 must be positive (got %g)", rho0);
   const int64_t total = p->NG;
@@ -687,10 +715,22 @@ int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, dou
   const double factor = 5.0 / (9.0 * alpha * beta * pow(rho0, alpha + beta - 5.0 / 3.0)) * ctf;
   const int64_t total = p->NG;
   const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
-  if (p->prec == GBOFDFT_F64)
-    k_wt_kernel<double><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<double*>(out));
-  else
-    k_wt_kernel<float><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<float*>(out));
+  if (p->prec == GBOFDFT_F64) {
+    k_wt_kernel<double><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<double*>(out), nullptr);
+  } else {
+    // plans with the plane pipeline keep a plane-major copy of the table
+    // (allocated with the first table built on the plan)
+    if (p->plane && !p->wt_pm) {
+      cudaError_t e = cudaMalloc(&p->wt_pm, sizeof(float) * (size_t)p->NG);
+      if (e != cudaSuccess) {
+        p->wt_pm = nullptr;
+        return gb_set_error(GBOFDFT_ERR_ALLOC, "wt kernel: plane-major table: %s", cudaGetErrorString(e));
+      }
+    }
+    k_wt_kernel<float><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<float*>(out),
+                                             p->plane ? p->wt_pm : nullptr);
+    p->wt_pm_src = p->plane ? out : nullptr;
+  }
   GB_CHECK_LAUNCH();
   return 0;
 }

@@ -105,7 +105,9 @@ struct CtRowsFwd {
   const void* tw;
 };
 
-template <typename T, int N>
+// PM: write plane-major spectra (k2 * nrows + row) for the plane pass;
+// consecutive threads then take consecutive rows of one k2.
+template <typename T, int N, bool PM>
 __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_ct_rows_fwd(CtRowsFwd a) {
   constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -119,9 +121,22 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
   const T* in = reinterpret_cast<const T*>(a.in);
-  for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
-    const int64_t row = base + idx / N;
-    R[idx] = row < a.nrows ? __ldg(in + row * N + idx % N) : (T)0;
+  // input rows: batches of independent loads ahead of their stores
+  constexpr int NE = 2 * RP * N, UNR = 4;
+#pragma unroll 1
+  for (int b0 = 0; b0 < NE; b0 += UNR * (int)blockDim.x) {
+    T v[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int idx = b0 + u * (int)blockDim.x + tid;
+      const int64_t row = base + idx / N;
+      v[u] = (idx < NE && row < a.nrows) ? __ldg(in + row * N + idx % N) : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int idx = b0 + u * (int)blockDim.x + tid;
+      if (idx < NE) R[idx] = v[u];
+    }
   }
   __syncthreads();
   const bool b56 = a.b56 != 0;
@@ -140,15 +155,17 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   cpx<T>* out = reinterpret_cast<cpx<T>*>(a.out);
   const T half = sc<T>(a.half);
   for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
-    const int line = idx / NH, k = idx % NH;
+    const int line = PM ? idx % nl : idx / NH, k = PM ? idx / nl : idx % NH;
     const int f = line / RP, l2 = line % RP;
     const int64_t ra = base + 2 * l2, rb = ra + 1;
     if (ra >= a.nrows) continue;
     const cpx<T> Z = res[sw<T, NP>(line, k)];
     const cpx<T> Zc = res[sw<T, NP>(line, k == 0 ? 0 : N - k)];
     cpx<T>* o = out + f * a.fstride;
-    o[ra * a.ld2 + k] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
-    if (rb < a.nrows) o[rb * a.ld2 + k] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
+    const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
+    const int64_t ib = PM ? ia + 1 : ia + a.ld2;
+    o[ia] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
+    if (rb < a.nrows) o[ib] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
   }
 }
 
@@ -173,7 +190,7 @@ struct CtRowsInv {
 
 // irfftn line build (all fields) + inverse FFT; result line (f * RP + pair)
 // holds row 2 pair in .x and row 2 pair + 1 in .y.
-template <typename T, int N>
+template <typename T, int N, bool PM = false>
 __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t base, cpx<T>* tw, cpx<T>* A,
                                                      cpx<T>* B) {
   constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
@@ -181,13 +198,15 @@ __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t
   const int nl = a.nf * RP;
   const cpx<T>* src0 = reinterpret_cast<const cpx<T>*>(a.in);
   for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
-    const int line = idx / NH, k = idx % NH;
+    const int line = PM ? idx % nl : idx / NH, k = PM ? idx / nl : idx % NH;
     const int f = line / RP, l2 = line % RP;
     const cpx<T>* src = src0 + f * a.fstride;
     const int64_t ra = base + 2 * l2, rb = ra + 1;
+    const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
+    const int64_t ib = PM ? ia + 1 : ia + a.ld2;
     cpx<T> va = {(T)0, (T)0}, vb = {(T)0, (T)0};
-    if (ra < a.nrows) va = src[ra * a.ld2 + k];
-    if (rb < a.nrows) vb = src[rb * a.ld2 + k];
+    if (ra < a.nrows) va = src[ia];
+    if (rb < a.nrows) vb = src[ib];
     if (k == 0 || 2 * k == N) { va.y = (T)0; vb.y = (T)0; }
     A[sw<T, NP>(line, k)] = cpx<T>{va.x - vb.y, va.y + vb.x};
     if (k > 0 && 2 * k < N) A[sw<T, NP>(line, N - k)] = cpx<T>{va.x + vb.y, vb.x - va.y};
@@ -253,7 +272,7 @@ __device__ __forceinline__ void pz_lda_ct(T rho, T& eps, T& pot, bool want_e) {
 // WANT_E is a template parameter so the potential-only instantiation holds no
 // FP64 accumulation at all (if-converted, never-taken FP64 code still
 // occupies the FP64 pipe).
-template <typename T, int N, bool WANT_E>
+template <typename T, int N, bool WANT_E, bool PM = false>
 __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_ct_rows_inv_eval(CtRowsInv a) {
   constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -265,11 +284,24 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   const int64_t base = (int64_t)blockIdx.x * 2 * RP;
   const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
-  cpx<T>* res = A;
-  if (a.nf > 0) res = ct_rows_inv_lines<T, N>(a, base, tw, A, B);
   const EvalDesc& ev = a.ev;
   const T* rhop = reinterpret_cast<const T*>(a.rho);
   const T* vlocp = reinterpret_cast<const T*>(a.vloc);
+  // the density and v_loc of this thread's first PF elements, loaded before
+  // the transforms so their latency is hidden behind them
+  constexpr int PF = sizeof(T) == 4 ? 8 : 4;
+  T pre_rho[PF], pre_vl[PF];
+#pragma unroll
+  for (int m = 0; m < PF; ++m) {
+    const int idx = tid + m * (int)blockDim.x;
+    const int64_t row = base + idx / N;
+    const bool ok = idx < 2 * RP * N && row < a.nrows;
+    const int64_t gidx = row * N + idx % N;
+    pre_rho[m] = ok ? __ldg(rhop + gidx) : (T)0;
+    pre_vl[m] = (ok && ev.pp) ? __ldg(vlocp + gidx) : (T)0;
+  }
+  cpx<T>* res = A;
+  if (a.nf > 0) res = ct_rows_inv_lines<T, N, PM>(a, base, tw, A, B);
   T* potp = reinterpret_cast<T*>(a.pot);
   constexpr bool want_e = WANT_E;
   const T tf_v = sc<T>(a.tf_v);             // (5/3) C_TF x
@@ -282,14 +314,23 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   // per-thread energy sums in the field precision (a handful of elements per
   // thread); combined in FP64 across threads and CTAs
   T es[6] = {0, 0, 0, 0, 0, 0};
-  for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
+#pragma unroll 1
+  for (int m = 0, idx = tid; idx < 2 * RP * N; ++m, idx += blockDim.x) {
     const int rr = idx / N, j = idx % N;
     const int64_t row = base + rr;
     if (row >= a.nrows) continue;
     const int64_t gidx = row * N + j;
     const int pr = rr >> 1;
     const bool odd = rr & 1;
-    const T rho = __ldg(rhop + gidx);
+    T rho, vl_pre;
+    if (m < PF) {
+#pragma unroll
+      for (int q = 0; q < PF; ++q)
+        if (q == m) { rho = pre_rho[q]; vl_pre = pre_vl[q]; }
+    } else {
+      rho = __ldg(rhop + gidx);
+      vl_pre = ev.pp ? __ldg(vlocp + gidx) : (T)0;
+    }
     const bool pos = rho > (T)kZero;
     // rho^(-1/3) and rho^(-1/2) for positive densities (shared by TF, vW, WT)
     T z3 = (T)0, z2 = (T)0;
@@ -344,7 +385,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
       if (want_e) es[4] += (T)0.5 * vh * rho;
     }
     if (ev.pp) {
-      const T vl = __ldg(vlocp + gidx);
+      const T vl = vl_pre;
       pot += vl;
       if (want_e) es[5] += vl * rho;
     }
@@ -501,7 +542,7 @@ template <typename K> inline int ct_smem(K kern, size_t bytes) {
   return 0;
 }
 
-template <typename T>
+template <typename T, bool PM = false>
 int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf, const int* ops,
                 double beta, double scale, cudaStream_t st) {
   int rc = 1;
@@ -517,9 +558,9 @@ int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, in
     a.half.set(0.5 * scale);
     a.tw = p->tw[2];
     const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP) + sizeof(T) * 2 * RP * N;
-    if ((rc = ct_smem(k_ct_rows_fwd<T, N>, sm))) return;
+    if ((rc = ct_smem(k_ct_rows_fwd<T, N, PM>, sm))) return;
     const int nblk = (a.nrows + 2 * RP - 1) / (2 * RP);
-    k_ct_rows_fwd<T, N><<<nblk, Tpl<N>::value * RP * nf, sm, st>>>(a);
+    k_ct_rows_fwd<T, N, PM><<<nblk, Tpl<N>::value * RP * nf, sm, st>>>(a);
     gb_count_launch();
     cudaError_t e = cudaGetLastError();
     rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "ct_rows_fwd: %s", cudaGetErrorString(e));
@@ -527,7 +568,7 @@ int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, in
   return rc;
 }
 
-template <typename T>
+template <typename T, bool PM = false>
 int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int nf, void* out, int64_t ostride,
                 double scale, const EvalDesc* ev, const void* rho, const void* vloc, void* pot, int calc_e,
                 double* partials, int64_t* nblk_out, cudaStream_t st) {
@@ -554,12 +595,15 @@ int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int
       const int nfl = nf > 0 ? nf : 1;
       const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nfl * RP * NP);
       if (calc_e) {
-        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, true>, sm))) return;
-        k_ct_rows_inv_eval<T, N, true><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, true, PM>, sm))) return;
+        k_ct_rows_inv_eval<T, N, true, PM><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
       } else {
-        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, false>, sm))) return;
-        k_ct_rows_inv_eval<T, N, false><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
+        if ((rc = ct_smem(k_ct_rows_inv_eval<T, N, false, PM>, sm))) return;
+        k_ct_rows_inv_eval<T, N, false, PM><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
       }
+    } else if constexpr (PM) {
+      rc = gb_set_error(GBOFDFT_ERR_ARG, "ct_rows_inv: plane-major spectra only in the evaluation pass");
+      return;
     } else {
       const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP);
       if ((rc = ct_smem(k_ct_rows_inv_store<T, N>, sm))) return;
@@ -603,6 +647,69 @@ int ct_cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int
 }
 
 }  // namespace gbct
+
+#include "plane_ct.cuh"
+
+namespace gbct {
+
+// Plane convolution pass over plane-major spectra (FP32); returns 1 when the
+// plane sizes have no specialisation or do not fit in shared memory.
+inline int plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, const KerDesc& kd,
+                          const float* const* pm_arr, double scale, cudaStream_t st) {
+  int rc = 1;
+  plane_dispatch(p->n[0], p->n[1], [&](auto a0, auto a1) {
+    constexpr int N0 = decltype(a0)::value, N1 = decltype(a1)::value;
+    PlaneArgs a;
+    memset(&a, 0, sizeof(a));
+    a.spec = reinterpret_cast<float2*>(spec);
+    a.fstride = fstride;
+    a.tw0 = p->tw[0];
+    a.tw1 = p->tw[1];
+    a.gi = p->gi;
+    for (int i = 0; i < 9; ++i) a.bgf[i] = (float)p->bg[i];
+    for (int f = 0; f < GB_MAX_FIELDS; ++f) {
+      a.type[f] = f < nf ? kd.type[f] : KER_NONE;
+      a.arr[f] = (f < nf && kd.type[f] == KER_ARRAY) ? pm_arr[f] : nullptr;
+      a.coef[f] = (float)(kd.coef[f] * scale);
+    }
+    for (int f = 0; f < nf; ++f)
+      if (a.type[f] == KER_ARRAY && !a.arr[f]) {
+        rc = gb_set_error(GBOFDFT_ERR_ARG, "plane_conv: field %d has no plane-major kernel table", f);
+        return;
+      }
+    const size_t sm = PlaneCfg<N0, N1>::kSmem;
+    if ((rc = ct_smem(k_plane_conv<N0, N1>, sm))) return;
+    k_plane_conv<N0, N1><<<dim3(p->n2h, nf), PlaneCfg<N0, N1>::NT, sm, st>>>(a);
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "plane_conv: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+}  // namespace gbct
+
+// Plane-major evaluation pipeline (FP32 only).
+#define GB_CT_DEFINE_PLANE()                                                                                   \
+  int gb_ct_rows_fwd_pm_f32(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int nf,             \
+                            const int* ops, double beta, cudaStream_t st) {                                   \
+    return gbct::ct_rows_fwd<float, true>(p, in, spec, fstride, 0, nf, ops, beta, 1.0, st);                   \
+  }                                                                                                            \
+  int gb_ct_rows_inv_eval_pm_f32(gbofdft_plan* p, const void* spec, int64_t fstride, int nf,                  \
+                                 const EvalDesc* ev, const void* rho, const void* vloc, void* pot, int calc_e,  \
+                                 double* partials, int64_t* nblk, cudaStream_t st) {                           \
+    return gbct::ct_rows_inv<float, true>(p, spec, fstride, 0, nf, nullptr, 0, 1.0, ev, rho, vloc, pot,       \
+                                          calc_e, partials, nblk, st);                                         \
+  }                                                                                                            \
+  int gb_plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, const KerDesc* kd,               \
+                        const float* const* pm_arr, double scale, cudaStream_t st) {                          \
+    return gbct::plane_conv_f32(p, spec, fstride, nf, *kd, pm_arr, scale, st);                                \
+  }                                                                                                            \
+  int gb_plane_supported_f32(int n0, int n1, int n2) {                                                         \
+    bool rows = gbct::ct_dispatch(n2, [](auto) {});                                                            \
+    bool plane = gbct::plane_dispatch(n0, n1, [](auto, auto) {});                                              \
+    return rows && plane;                                                                                      \
+  }
 
 // Instantiate the launchers of one precision (one translation unit each).
 #define GB_CT_DEFINE(T, SUF)                                                                                    \

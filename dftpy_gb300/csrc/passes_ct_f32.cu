@@ -2,3 +2,4 @@
 #include "passes_ct.cuh"
 
 GB_CT_DEFINE(float, f32)
+GB_CT_DEFINE_PLANE()

@@ -30,6 +30,10 @@ struct gbofdft_plan {
   int tb[3];             // column tile width per axis
   int pairs;             // row pairs per CTA in the row passes
   GInfo gi;
+  // FP32 plane-major evaluation pipeline (rows -> plane convolution -> rows)
+  int plane;             // 1: the grid has the plane pipeline
+  float* wt_pm;          // plane-major copy of the last WT kernel table built on this plan
+  const void* wt_pm_src; // the table that copy belongs to
 };
 
 size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
@@ -74,6 +78,16 @@ int gb_ct_rows_inv_f32(gbofdft_plan*, const void*, int64_t, int, int, void*, int
 int gb_ct_rows_inv_f64(gbofdft_plan*, const void*, int64_t, int, int, void*, int64_t, double, const EvalDesc*,
                        const void*, const void*, void*, int, double*, int64_t*, cudaStream_t);
 int gb_ct_cols_f32(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
+// plane-major FP32 pipeline (passes_ct_f32.cu)
+int gb_ct_rows_fwd_pm_f32(gbofdft_plan*, const void*, void*, int64_t, int, const int*, double, cudaStream_t);
+int gb_ct_rows_inv_eval_pm_f32(gbofdft_plan*, const void*, int64_t, int, const EvalDesc*, const void*, const void*,
+                               void*, int, double*, int64_t*, cudaStream_t);
+int gb_plane_conv_f32(gbofdft_plan*, void*, int64_t, int, const KerDesc*, const float* const*, double, cudaStream_t);
+int gb_plane_supported_f32(int n0, int n1, int n2);
+// the plane-major evaluation (returns 1 when the plan has no plane pipeline
+// or a kernel table has no plane-major copy)
+int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, double beta, const KerDesc& kd,
+                  const EvalDesc& ev, const void* vloc, void* pot, int calc_e, double* energies, cudaStream_t st);
 int gb_ct_cols_f64(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
 void gb_count_launch();
 int gb_smem_granted(const void* kern, int dev);

@@ -1,0 +1,313 @@
+// Plane convolution pass: for one spectrum field and one k2, the whole
+// (n0 x n1) plane is held in shared memory and transformed forward along
+// axis 1 and axis 0, multiplied by the reciprocal-space kernel and
+// transformed back -- the three column passes of the evaluation pipeline in
+// one launch, with one read and one write of each spectrum.
+//
+// Spectra are plane-major here: element (i0, i1, k2) of field f sits at
+//   spec[f * fstride + (k2 * n0 + i0) * n1 + i1]
+// so a plane is one contiguous block; the row passes read and write that
+// layout (PM instantiations of k_ct_rows_fwd / k_ct_rows_inv_eval).
+//
+// The FFT stages run in place in the plane buffer: every thread loads the
+// inputs of its butterflies (and twiddles them) into registers, the CTA
+// synchronises, and the outputs are written over the inputs.  A Stockham
+// stage is a permutation of whole lines, so reading everything before
+// writing anything makes in-place exactly the ping-pong result.  Lines are
+// processed in chunks so that a thread holds at most GB_PLANE_REGS complex
+// values (16: no register spills at 512 threads for every specialised size).
+//
+// The plane uses the XOR-swizzled line-major layout of fft_ct.cuh with lines
+// = rows i0 (elements i1): axis-1 stages walk along a line, axis-0 stages
+// map consecutive threads to consecutive columns i1, so both access
+// patterns are free of bank conflicts.
+#pragma once
+
+namespace gbct {
+
+#ifndef GB_PLANE_THREADS
+#define GB_PLANE_THREADS 512       // threads per plane CTA
+#endif
+#ifndef GB_PLANE_THREADS_128
+#define GB_PLANE_THREADS_128 1024  // ... for 128 x 128 planes (measured best; 64 registers)
+#endif
+#ifndef GB_PLANE_REGS
+#define GB_PLANE_REGS 16
+#endif
+#ifndef GB_PLANE_R16
+#define GB_PLANE_R16 1      // 128-point plane transforms as 16 x 8 (else 8 x 4 x 4)
+#endif
+constexpr int kPlaneRegs = GB_PLANE_REGS;   // complex values a thread holds in one stage
+
+template <int N0, int N1> struct PlaneCfg {
+  static constexpr int NT = (N0 == 128 && N1 == 128) ? GB_PLANE_THREADS_128 : GB_PLANE_THREADS;
+  static constexpr int NP1 = Pad<float, N1>::NP;
+  static constexpr size_t kPlaneBytes = sizeof(float2) * (size_t)N0 * NP1;
+  static constexpr size_t kSmall = sizeof(float2) * (N0 + N1) + sizeof(float) * 3 * (N0 + N1);
+  static constexpr size_t kTable = sizeof(float) * (size_t)N0 * N1;
+  // the kernel table's plane is staged in shared memory (asynchronous copy
+  // overlapped with the forward transforms) when it fits beside the plane
+  static constexpr bool table_smem = kPlaneBytes + kTable + kSmall <= 227 * 1024 && (N0 * N1) % 4 == 0;
+  static constexpr size_t kSmem = kPlaneBytes + (table_smem ? kTable : 0) + kSmall;
+  static constexpr bool fits = kSmem <= 227 * 1024;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// smallest number of line chunks (a divisor of NL) with at most kPlaneRegs
+// complex values per thread in a radix-R stage
+template <int NL, int NB, int R, int NT>
+constexpr int plane_chunks() {
+  for (int c = 1; c <= NL; ++c) {
+    if (NL % c) continue;
+    const int per = (NL / c) * NB;
+    const int iters = (per + NT - 1) / NT;
+    if (iters * R <= kPlaneRegs) return c;
+  }
+  return NL;
+}
+
+// radix schedules of the plane transforms (fewer, larger stages than the
+// line passes: every stage is a full read and write of the plane)
+template <int N> struct PlaneSched { using S = typename Plan<N>::S; };
+#if GB_PLANE_R16
+template <> struct PlaneSched<128> { using S = Sched<16, 8>; };
+#endif
+
+template <int N1>
+__device__ __forceinline__ int paddr(int i0, int i1) {
+  return sw<float, Pad<float, N1>::NP>(i0, i1);
+}
+
+// One in-place Stockham stage (radix R, stride P) of every line along axis
+// AX (1: lines are rows i0, elements i1; 0: lines are columns i1, elements i0).
+template <int DIR, int AX, int N0, int N1, int R, int P>
+__device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __restrict__ tw) {
+  constexpr int N = AX == 1 ? N1 : N0;
+  constexpr int NL = AX == 1 ? N0 : N1;
+  constexpr int NB = N / R;
+  constexpr int TWS = N / (P * R);
+  constexpr int NT = PlaneCfg<N0, N1>::NT;
+  constexpr int CH = plane_chunks<NL, NB, R, NT>();
+  constexpr int LC = NL / CH;
+  constexpr int PER = LC * NB;
+  constexpr int IT = (PER + NT - 1) / NT;
+  const int tid = threadIdx.x;
+#pragma unroll 1
+  for (int c0 = 0; c0 < NL; c0 += LC) {
+    float2 u[IT][R];
+    int lo[IT], jo[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int b = tid + it * NT;
+      lo[it] = -1;
+      if ((PER % NT) != 0 && b >= PER) continue;
+      int l, i;
+      if constexpr (AX == 1) { l = c0 + b / NB; i = b % NB; }
+      else { l = c0 + b % LC; i = b / LC; }
+      const int k = (P == 1) ? 0 : i % P;
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        const int j = i + t * NB;
+        float2 v = AX == 1 ? pl[paddr<N1>(l, j)] : pl[paddr<N1>(j, l)];
+        if (P > 1 && t > 0) {
+          const float2 w = tw[t * k * TWS];
+          v = DIR < 0 ? c_mul(v, w) : c_mulc(v, w);
+        }
+        u[it][t] = v;
+      }
+      dft<DIR, float, R>(u[it]);
+      lo[it] = l;
+      jo[it] = (i - k) * R + k;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      if (lo[it] < 0) continue;
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        const int j = jo[it] + t * P;
+        if constexpr (AX == 1) pl[paddr<N1>(lo[it], j)] = u[it][t];
+        else pl[paddr<N1>(j, lo[it])] = u[it][t];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int DIR, int AX, int N0, int N1, int P, int R0, int... Rs>
+__device__ __forceinline__ void prun(float2* pl, const float2* tw) {
+  pstage<DIR, AX, N0, N1, R0, P>(pl, tw);
+  if constexpr (sizeof...(Rs) > 0) prun<DIR, AX, N0, N1, P * R0, Rs...>(pl, tw);
+}
+
+template <int DIR, int AX, int N0, int N1, int... Rs>
+__device__ __forceinline__ void prun_sched(Sched<Rs...>, float2* pl, const float2* tw) {
+  prun<DIR, AX, N0, N1, 1, Rs...>(pl, tw);
+}
+
+// whole-plane 1-D transforms along one axis
+template <int DIR, int AX, int N0, int N1>
+__device__ __forceinline__ void plane_fft(float2* pl, const float2* tw) {
+  prun_sched<DIR, AX, N0, N1>(typename PlaneSched<AX == 1 ? N1 : N0>::S{}, pl, tw);
+}
+
+struct PlaneArgs {
+  float2* spec;
+  int64_t fstride;
+  const void* tw0;
+  const void* tw1;
+  GInfo gi;
+  float bgf[9];         // reciprocal lattice rows in FP32
+  int type[GB_MAX_FIELDS];
+  const float* arr[GB_MAX_FIELDS];   // plane-major kernel tables (KER_ARRAY)
+  float coef[GB_MAX_FIELDS];
+};
+
+template <int N0, int N1>
+__global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArgs a) {
+  constexpr int kPlaneThreads = PlaneCfg<N0, N1>::NT;
+  constexpr int NP1 = Pad<float, N1>::NP;
+  using Cfg = PlaneCfg<N0, N1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* pl = reinterpret_cast<float2*>(smem_raw);
+  float* ktab = reinterpret_cast<float*>(smem_raw + Cfg::kPlaneBytes);      // [N0 * N1] when staged
+  float2* tw0 = reinterpret_cast<float2*>(smem_raw + Cfg::kPlaneBytes + (Cfg::table_smem ? Cfg::kTable : 0));
+  float2* tw1 = tw0 + N0;
+  float* gA = reinterpret_cast<float*>(tw1 + N1);   // [3][N0]: m0 b0 + m2 b2
+  float* gB = gA + 3 * N0;                          // [3][N1]: m1 b1
+  const int tid = threadIdx.x;
+  const int k2 = blockIdx.x, f = blockIdx.y;
+  const GInfo& g = a.gi;
+  float2* gp = a.spec + f * a.fstride + (int64_t)k2 * (N0 * N1);
+  const int type = a.type[f];
+  const float* karr = a.arr[f] ? a.arr[f] + (int64_t)k2 * (N0 * N1) : nullptr;
+  if constexpr (Cfg::table_smem) {
+    // start the table plane's copy; it completes behind the forward transforms
+    if (type == KER_ARRAY) {
+      for (int idx = tid; idx < N0 * N1 / 4; idx += kPlaneThreads) cp_async16(ktab + 4 * idx, karr + 4 * idx);
+    }
+    cp_async_commit();
+  }
+  // the plane (contiguous), as float4 pairs when the row length allows;
+  // batches of loads are issued before their shared-memory stores
+  if constexpr ((N1 % 2) == 0) {
+    constexpr int NV = N0 * N1 / 2, UNR = 4096 / kPlaneThreads;
+    const float4* g4 = reinterpret_cast<const float4*>(gp);
+#pragma unroll 1
+    for (int base = 0; base < NV; base += UNR * kPlaneThreads) {
+      float4 v[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int idx = base + u * kPlaneThreads + tid;
+        if (idx < NV) v[u] = g4[idx];
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int idx = base + u * kPlaneThreads + tid;
+        if (idx < NV) {
+          const int e = 2 * idx, i0 = e / N1, i1 = e % N1;
+          pl[paddr<N1>(i0, i1)] = make_float2(v[u].x, v[u].y);
+          pl[paddr<N1>(i0, i1 + 1)] = make_float2(v[u].z, v[u].w);
+        }
+      }
+    }
+  } else {
+    for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) pl[paddr<N1>(idx / N1, idx % N1)] = gp[idx];
+  }
+  const float2* t0 = reinterpret_cast<const float2*>(a.tw0);
+  const float2* t1 = reinterpret_cast<const float2*>(a.tw1);
+  for (int i = tid; i < N0; i += kPlaneThreads) tw0[i] = t0[i];
+  for (int i = tid; i < N1; i += kPlaneThreads) tw1[i] = t1[i];
+  const float m2 = (float)(g.full ? gbk::ffreq(k2, g.n2) : k2);
+  for (int i = tid; i < N0; i += kPlaneThreads) {
+    const float m0 = (float)gbk::ffreq(i, N0);
+    gA[i] = m0 * a.bgf[0] + m2 * a.bgf[6];
+    gA[N0 + i] = m0 * a.bgf[1] + m2 * a.bgf[7];
+    gA[2 * N0 + i] = m0 * a.bgf[2] + m2 * a.bgf[8];
+  }
+  for (int i = tid; i < N1; i += kPlaneThreads) {
+    const float m1 = (float)gbk::ffreq(i, N1);
+    gB[i] = m1 * a.bgf[3];
+    gB[N1 + i] = m1 * a.bgf[4];
+    gB[2 * N1 + i] = m1 * a.bgf[5];
+  }
+  __syncthreads();
+  plane_fft<-1, 1, N0, N1>(pl, tw1);
+  plane_fft<-1, 0, N0, N1>(pl, tw0);
+  // kernel multiply; points on a Nyquist line of a symmetrised plane take
+  // the partner-averaged general path (as the column passes do)
+  const bool plane_sym = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
+  const bool nyq2 = g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2;
+  const float coef = a.coef[f];
+  const float fourpi_c = 4.0f * 3.14159265358979323846f * coef;
+  if constexpr (Cfg::table_smem) {
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) {
+    const int i0 = idx / N1, i1 = idx % N1;
+    float kv;
+    if (type == KER_ARRAY) {
+      kv = (Cfg::table_smem ? ktab[idx] : __ldg(karr + idx)) * coef;
+    } else {
+      const bool special = plane_sym && (nyq2 || ((N0 & 1) == 0 && 2 * i0 == N0) || ((N1 & 1) == 0 && 2 * i1 == N1));
+      if (special) {
+        kv = kernel_value_slow<float>(g, type, nullptr, i0, i1, k2) * coef;
+      } else {
+        const float gx = gA[i0] + gB[i1], gy = gA[N0 + i0] + gB[N1 + i1], gz = gA[2 * N0 + i0] + gB[2 * N1 + i1];
+        const float gg = gx * gx + gy * gy + gz * gz;
+        kv = type == KER_HARTREE ? (gg > 0.0f ? fourpi_c / gg : 0.0f) : (type == KER_G2 ? gg * coef : coef);
+      }
+    }
+    const int p = paddr<N1>(i0, i1);
+    pl[p] = c_scale(pl[p], kv);
+  }
+  __syncthreads();
+  plane_fft<1, 0, N0, N1>(pl, tw0);
+  plane_fft<1, 1, N0, N1>(pl, tw1);
+  if constexpr ((N1 % 2) == 0) {
+    float4* g4 = reinterpret_cast<float4*>(gp);
+    for (int idx = tid; idx < N0 * N1 / 2; idx += kPlaneThreads) {
+      const int e = 2 * idx, i0 = e / N1, i1 = e % N1;
+      const float2 v0 = pl[paddr<N1>(i0, i1)], v1 = pl[paddr<N1>(i0, i1 + 1)];
+      g4[idx] = make_float4(v0.x, v0.y, v1.x, v1.y);
+    }
+  } else {
+    for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) gp[idx] = pl[paddr<N1>(idx / N1, idx % N1)];
+  }
+}
+
+// plane sizes with a specialisation (the workloads' grids)
+template <typename F>
+__host__ inline bool plane_size_dispatch(int n, F&& f) {
+  switch (n) {
+    case 64: f(std::integral_constant<int, 64>{}); return true;
+    case 96: f(std::integral_constant<int, 96>{}); return true;
+    case 128: f(std::integral_constant<int, 128>{}); return true;
+    case 160: f(std::integral_constant<int, 160>{}); return true;
+    default: return false;
+  }
+}
+
+template <typename F>
+__host__ inline bool plane_dispatch(int n0, int n1, F&& f) {
+  bool ok = false;
+  plane_size_dispatch(n0, [&](auto a) {
+    plane_size_dispatch(n1, [&](auto b) {
+      constexpr int N0 = decltype(a)::value, N1 = decltype(b)::value;
+      if constexpr (PlaneCfg<N0, N1>::fits) {
+        f(a, b);
+        ok = true;
+      }
+    });
+  });
+  return ok;
+}
+
+}  // namespace gbct

@@ -225,3 +225,63 @@ def test_eval_single_components(lib, golden, prec, comp, case):
     assert abs(e - eref) <= tol * max(1.0, abs(eref)), (e, eref)
     p = pot.cpu().numpy()
     assert np.abs(p - vref).max() <= tol * np.abs(vref).max()
+
+
+PLANE_CASES = [((64, 64, 64), False, False), ((64, 64, 64), True, True), ((96, 128, 160), False, True),
+               ((160, 96, 32), True, True), ((128, 128, 128), False, False)]
+
+
+def _plane_eval(lib, nr, L, full, rho, vloc, plane, copy_kernel=False):
+    import os
+    torch = _torch()
+    old = os.environ.get("GBOFDFT_PLANE")
+    os.environ["GBOFDFT_PLANE"] = "1" if plane else "0"
+    try:
+        plan = lib.Plan(nr, L, precision=0, full=full)
+    finally:
+        if old is None:
+            del os.environ["GBOFDFT_PLANE"]
+        else:
+            os.environ["GBOFDFT_PLANE"] = old
+    f = lib.Functional()
+    f.tf, f.tf_x, f.vw, f.vw_y, f.xc, f.hartree = 1, 1.0, 1, 1.0, 1, 1
+    kern = torch.empty(nr[0], nr[1], nr[2] // 2 + 1, dtype=torch.float32, device="cuda")
+    lib.check(lib.load().gbofdft_wt_kernel(plan.handle, float(rho.mean()), 1.0, 5 / 6, 5 / 6, lib.ptr(kern),
+                                           lib.stream_ptr()))
+    if copy_kernel:
+        kern = kern.clone()
+    f.wt, f.wt_alpha, f.wt_beta, f.wt_kernel = 1, 5 / 6, 5 / 6, kern.data_ptr()
+    rd = torch.tensor(np.ascontiguousarray(rho), dtype=torch.float32, device="cuda")
+    vd = torch.tensor(vloc, dtype=torch.float32, device="cuda")
+    f.vloc = vd.data_ptr()
+    pot = torch.empty_like(rd)
+    en = torch.zeros(lib.NE, dtype=torch.float64, device="cuda")
+    lib.check(lib.load().gbofdft_eval(plan.handle, lib.ptr(rd), f, lib.ptr(pot), lib.ptr(en),
+                                      lib.CALC_E | lib.CALC_V, lib.stream_ptr()))
+    torch.cuda.synchronize()
+    return en.cpu().numpy(), pot.cpu().numpy()
+
+
+@pytest.mark.parametrize("nr,full,skew", PLANE_CASES)
+def test_eval_plane_pipeline_fp32(lib, nr, full, skew):
+    """FP32 evaluation through the plane pipeline (rows -> whole-plane
+    convolution in shared memory -> rows) against the oracle and against the
+    column-pass pipeline; a WT table the plan did not build takes the column
+    passes and gives the same result."""
+    L = _lattice(nr, skew)
+    rng = np.random.default_rng(11)
+    rho = 0.02 + 0.01 * rng.random(nr)
+    vloc = np.cos(np.arange(np.prod(nr)).reshape(nr) * 0.003)
+    g = O.Grid(L, nr, full=full)
+    parts = [O.tf(rho, g), O.vw(rho, g), O.WTNL()(rho, g), O.lda(rho, g), O.hartree(rho, g)]
+    eref = sum(e for e, _ in parts) + float(np.einsum("ijk,ijk->", vloc, rho) * g.dV)
+    vref = sum(v for _, v in parts) + vloc
+    en_p, pot_p = _plane_eval(lib, nr, L, full, rho, vloc, True)
+    en_c, pot_c = _plane_eval(lib, nr, L, full, rho, vloc, False)
+    en_x, pot_x = _plane_eval(lib, nr, L, full, rho, vloc, True, copy_kernel=True)
+    for en, pot in ((en_p, pot_p), (en_c, pot_c), (en_x, pot_x)):
+        assert abs(en[lib.E_TOTAL] - eref) <= 3e-5 * max(1.0, abs(eref))
+        assert np.abs(pot - vref).max() <= 3e-5 * np.abs(vref).max()
+    # the two pipelines differ only by FP32 rounding
+    assert np.abs(pot_p - pot_c).max() <= 5e-6 * np.abs(vref).max()
+    np.testing.assert_array_equal(pot_x, pot_c)

@@ -46,7 +46,14 @@ template <int N> struct Plan;
 template <> struct Plan<32> { using S = Sched<8, 4>; static constexpr int R0 = 8; };
 template <> struct Plan<64> { using S = Sched<8, 8>; static constexpr int R0 = 8; };
 template <> struct Plan<96> { using S = Sched<8, 4, 3>; static constexpr int R0 = 8; };
+#ifndef GB_CT_R16_128
+#define GB_CT_R16_128 0
+#endif
+#if GB_CT_R16_128
+template <> struct Plan<128> { using S = Sched<16, 8>; static constexpr int R0 = 16; };
+#else
 template <> struct Plan<128> { using S = Sched<8, 4, 4>; static constexpr int R0 = 8; };
+#endif
 template <> struct Plan<160> { using S = Sched<8, 4, 5>; static constexpr int R0 = 8; };
 template <> struct Plan<256> { using S = Sched<8, 8, 4>; static constexpr int R0 = 8; };
 template <> struct Plan<360> { using S = Sched<8, 5, 3, 3>; static constexpr int R0 = 8; };
@@ -169,7 +176,7 @@ __device__ __forceinline__ double rsqrt_d(double x) {
   z = z * (1.5 - 0.5 * x * z * z);
   return z;
 }
-__device__ __forceinline__ float rcbrt_d(float x) { return 1.0f / cbrtf(x); }
+__device__ __forceinline__ float rcbrt_d(float x) { return rcbrtf(x); }
 __device__ __forceinline__ float rsqrt_d(float x) { return rsqrtf(x); }
 
 }  // namespace gbct

@@ -141,31 +141,42 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   __syncthreads();
   const bool b56 = a.b56 != 0;
   const T beta = sc<T>(a.beta);
-  for (int idx = tid; idx < nl * N; idx += blockDim.x) {
-    const int line = idx / N, j = idx % N;
-    const int f = line / RP, l2 = line % RP;
+  // fields in an unrolled outer loop: the field's prologue op is a
+  // compile-time parameter index, and every index split below is by a
+  // compile-time constant
+#pragma unroll
+  for (int f = 0; f < GB_MAX_FIELDS; ++f) {
+    if (f >= a.nf) break;
     const int op = a.op[f];
-    const int64_t ra = base + 2 * l2;
-    const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], b56, beta) : (T)0;
-    const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], b56, beta) : (T)0;
-    A[sw<T, NP>(line, j)] = cpx<T>{x0, x1};
+    for (int idx = tid; idx < RP * N; idx += blockDim.x) {
+      const int l2 = idx / N, j = idx % N;
+      const int64_t ra = base + 2 * l2;
+      const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], b56, beta) : (T)0;
+      const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], b56, beta) : (T)0;
+      A[sw<T, NP>(f * RP + l2, j)] = cpx<T>{x0, x1};
+    }
   }
   __syncthreads();
   cpx<T>* res = fft<-1, T, N>(A, B, tw, l, lane, true);
   cpx<T>* out = reinterpret_cast<cpx<T>*>(a.out);
   const T half = sc<T>(a.half);
-  for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
-    const int line = PM ? idx % nl : idx / NH, k = PM ? idx / nl : idx % NH;
-    const int f = line / RP, l2 = line % RP;
-    const int64_t ra = base + 2 * l2, rb = ra + 1;
-    if (ra >= a.nrows) continue;
-    const cpx<T> Z = res[sw<T, NP>(line, k)];
-    const cpx<T> Zc = res[sw<T, NP>(line, k == 0 ? 0 : N - k)];
+#pragma unroll
+  for (int f = 0; f < GB_MAX_FIELDS; ++f) {
+    if (f >= a.nf) break;
     cpx<T>* o = out + f * a.fstride;
-    const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
-    const int64_t ib = PM ? ia + 1 : ia + a.ld2;
-    o[ia] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
-    if (rb < a.nrows) o[ib] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
+    for (int idx = tid; idx < RP * NH; idx += blockDim.x) {
+      // plane-major: consecutive threads take consecutive row pairs of one k
+      const int l2 = PM ? idx % RP : idx / NH, k = PM ? idx / RP : idx % NH;
+      const int line = f * RP + l2;
+      const int64_t ra = base + 2 * l2, rb = ra + 1;
+      if (ra >= a.nrows) continue;
+      const cpx<T> Z = res[sw<T, NP>(line, k)];
+      const cpx<T> Zc = res[sw<T, NP>(line, k == 0 ? 0 : N - k)];
+      const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
+      const int64_t ib = PM ? ia + 1 : ia + a.ld2;
+      o[ia] = cpx<T>{(Z.x + Zc.x) * half, (Z.y - Zc.y) * half};
+      if (rb < a.nrows) o[ib] = cpx<T>{(Z.y + Zc.y) * half, (Zc.x - Z.x) * half};
+    }
   }
 }
 
@@ -197,19 +208,23 @@ __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t
   const int tid = threadIdx.x, l = tid / TPL, lane = tid % TPL;
   const int nl = a.nf * RP;
   const cpx<T>* src0 = reinterpret_cast<const cpx<T>*>(a.in);
-  for (int idx = tid; idx < nl * NH; idx += blockDim.x) {
-    const int line = PM ? idx % nl : idx / NH, k = PM ? idx / nl : idx % NH;
-    const int f = line / RP, l2 = line % RP;
+#pragma unroll
+  for (int f = 0; f < GB_MAX_FIELDS; ++f) {
+    if (f >= a.nf) break;
     const cpx<T>* src = src0 + f * a.fstride;
-    const int64_t ra = base + 2 * l2, rb = ra + 1;
-    const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
-    const int64_t ib = PM ? ia + 1 : ia + a.ld2;
-    cpx<T> va = {(T)0, (T)0}, vb = {(T)0, (T)0};
-    if (ra < a.nrows) va = src[ia];
-    if (rb < a.nrows) vb = src[ib];
-    if (k == 0 || 2 * k == N) { va.y = (T)0; vb.y = (T)0; }
-    A[sw<T, NP>(line, k)] = cpx<T>{va.x - vb.y, va.y + vb.x};
-    if (k > 0 && 2 * k < N) A[sw<T, NP>(line, N - k)] = cpx<T>{va.x + vb.y, vb.x - va.y};
+    for (int idx = tid; idx < RP * NH; idx += blockDim.x) {
+      const int l2 = PM ? idx % RP : idx / NH, k = PM ? idx / RP : idx % NH;
+      const int line = f * RP + l2;
+      const int64_t ra = base + 2 * l2, rb = ra + 1;
+      const int64_t ia = PM ? (int64_t)k * a.nrows + ra : ra * a.ld2 + k;
+      const int64_t ib = PM ? ia + 1 : ia + a.ld2;
+      cpx<T> va = {(T)0, (T)0}, vb = {(T)0, (T)0};
+      if (ra < a.nrows) va = src[ia];
+      if (rb < a.nrows) vb = src[ib];
+      if (k == 0 || 2 * k == N) { va.y = (T)0; vb.y = (T)0; }
+      A[sw<T, NP>(line, k)] = cpx<T>{va.x - vb.y, va.y + vb.x};
+      if (k > 0 && 2 * k < N) A[sw<T, NP>(line, N - k)] = cpx<T>{va.x + vb.y, vb.x - va.y};
+    }
   }
   __syncthreads();
   return fft<1, T, N>(A, B, tw, l, lane, true);
@@ -314,23 +329,13 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   // per-thread energy sums in the field precision (a handful of elements per
   // thread); combined in FP64 across threads and CTAs
   T es[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 1
-  for (int m = 0, idx = tid; idx < 2 * RP * N; ++m, idx += blockDim.x) {
+  auto point = [&](int idx, T rho, T vl_pre) {
     const int rr = idx / N, j = idx % N;
     const int64_t row = base + rr;
-    if (row >= a.nrows) continue;
+    if (row >= a.nrows) return;
     const int64_t gidx = row * N + j;
     const int pr = rr >> 1;
     const bool odd = rr & 1;
-    T rho, vl_pre;
-    if (m < PF) {
-#pragma unroll
-      for (int q = 0; q < PF; ++q)
-        if (q == m) { rho = pre_rho[q]; vl_pre = pre_vl[q]; }
-    } else {
-      rho = __ldg(rhop + gidx);
-      vl_pre = ev.pp ? __ldg(vlocp + gidx) : (T)0;
-    }
     const bool pos = rho > (T)kZero;
     // rho^(-1/3) and rho^(-1/2) for positive densities (shared by TF, vW, WT)
     T z3 = (T)0, z2 = (T)0;
@@ -390,6 +395,25 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
       if (want_e) es[5] += vl * rho;
     }
     potp[gidx] = pot;
+  };
+  // one element per iteration (not unrolled: an unrolled epilogue doubles the
+  // registers and halves the occupancy); the first PF come from the
+  // prefetch registers
+#pragma unroll 1
+  for (int m = 0, idx = tid; idx < 2 * RP * N; ++m, idx += blockDim.x) {
+    T rho, vl;
+    if (m < PF) {
+#pragma unroll
+      for (int q = 0; q < PF; ++q)
+        if (q == m) { rho = pre_rho[q]; vl = pre_vl[q]; }
+    } else {
+      const int64_t row = base + idx / N;
+      if (row >= a.nrows) continue;
+      const int64_t gidx = row * N + idx % N;
+      rho = __ldg(rhop + gidx);
+      vl = ev.pp ? __ldg(vlocp + gidx) : (T)0;
+    }
+    point(idx, rho, vl);
   }
   if constexpr (!WANT_E) return;
   __shared__ double red[32][6];

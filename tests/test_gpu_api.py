@@ -543,3 +543,25 @@ def test_multistep_al4_reaches_fine_grid_minimum(api, golden):
     E = total.Energy(rho)
     assert abs(E - float(a["E_final"])) < 1e-7
     assert np.abs(rho.to_numpy() - a["rho"]).max() < 1e-4
+
+
+def test_batch_matches_individual_solves(api):
+    """Several Al/Mg structures of different cells and grids optimised
+    concurrently (one stream and host thread each) give exactly the energies
+    of the same solves run one after another, and those energies equal the
+    oracle's functional at the solved densities."""
+    from dftpy_gb300 import batch
+    sts = [systems.fcc_supercell(r, sigma=0.15, seed=s, nr=n, mg_fraction=0.25, name="b%d" % s)
+           for s, (r, n) in enumerate([((1, 1, 1), (32, 32, 32)), ((1, 1, 2), (32, 32, 64)),
+                                       ((1, 2, 2), (32, 64, 64)), ((1, 1, 1), (36, 36, 36))])]
+    opts = {"econv": 1e-8, "precision": "fp64"}  # total, Ha
+    par = batch.optimize_batch(sts, workers=4, options=opts, kedf="TFVW")
+    seq = batch.optimize_batch(sts, workers=1, options=opts, kedf="TFVW")
+    assert [r.name for r in par] == [st.name for st in sts]
+    for st, a, b in zip(sts, par, seq):
+        assert a.converged == 0 and b.converged == 0
+        assert a.energy == b.energy
+        np.testing.assert_array_equal(a.rho.to_numpy(), b.rho.to_numpy())
+        ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
+        e_ref, _ = ev(a.rho.to_numpy())
+        assert abs(a.energy - e_ref) < 1e-9 * abs(e_ref)

@@ -34,6 +34,13 @@ class Lwt(ctypes.Structure):
                 ("work", ctypes.c_void_p), ("work_bytes", ctypes.c_int64), ("nknots", ctypes.c_int)]
 
 
+class Wgc(ctypes.Structure):
+    """Mirror of ``gbofdft_wgc``."""
+    _fields_ = [("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("rho0", ctypes.c_double), ("order", ctypes.c_int), ("kernels", ctypes.c_void_p),
+                ("work", ctypes.c_void_p), ("work_bytes", ctypes.c_int64)]
+
+
 class Functional(ctypes.Structure):
     """Mirror of ``gbofdft_functional``."""
     _fields_ = [
@@ -43,6 +50,7 @@ class Functional(ctypes.Structure):
         ("wt_kernel", ctypes.c_void_p),
         ("xc", ctypes.c_int), ("hartree", ctypes.c_int),
         ("vloc", ctypes.c_void_p), ("e_ion", ctypes.c_double), ("lwt", ctypes.POINTER(Lwt)),
+        ("wgc", ctypes.POINTER(Wgc)),
     ]
 
 
@@ -93,6 +101,9 @@ _SIGS = [
     ("gbofdft_wt_kernel", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _P, _P]),
     ("gbofdft_lwt_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_wgc_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_wgc_kernels", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_double, _P, _P]),
     ("gbofdft_mgp_table", ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, _P, _P]),
     ("gbofdft_setup_workspace_bytes", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_vloc", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(VTable), ctypes.c_int, _P, _P, ctypes.c_int,

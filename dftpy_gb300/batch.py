@@ -44,7 +44,7 @@ class BatchResult:
     extra: dict = field(default_factory=dict)
 
 
-def build_evaluator(st, kedf="WT", pme=True, full=False, **kedf_options):
+def build_evaluator(st, kedf="WGC", pme=True, full=False, **kedf_options):
     """TotalFunctional (KEDF + LDA + Hartree + analytic local PP) and a
     uniform guess density for a ``systems.Structure``."""
     grid = DirectGrid(st.lattice, st.nr, full=full)
@@ -82,7 +82,7 @@ def _solve_one(job, options, stream):
                        wall_s=time.perf_counter() - t0, name=name)
 
 
-def optimize_batch(jobs, workers=None, options=None, kedf="WT", **kedf_options):
+def optimize_batch(jobs, workers=None, options=None, kedf="WGC", **kedf_options):
     """Optimise every job; ``workers`` structures are in flight at a time
     (default: all of them, at most 16).  Jobs are ``(evaluator, guess_rho)``
     pairs or ``systems.Structure`` objects."""
@@ -133,7 +133,7 @@ def main():
     p = argparse.ArgumentParser(description="batched optimisation of Al/Mg alloy snapshots")
     p.add_argument("--n", type=int, default=64)
     p.add_argument("--workers", type=int, default=16)
-    p.add_argument("--kedf", default="WT")
+    p.add_argument("--kedf", default="WGC")
     p.add_argument("--precision", default="mixed")
     p.add_argument("--sequential", type=int, default=8, help="also time this many jobs one after another")
     p.add_argument("--check", type=int, default=4, help="solve this many in plain FP64 and report the error")

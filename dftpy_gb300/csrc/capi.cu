@@ -274,6 +274,9 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
     if (f->lwt)
       rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0,
                        (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
+    if (!rc && f->wgc)
+      rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0,
+                       (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
     return rc;
   }
   if (rc != 1) return rc;
@@ -288,6 +291,9 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
     rc = gb_rows_inv_eval(p, p->spec, fs, nf, ev, rho, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
   if (!rc && f->lwt)
     rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
+                     st);
+  if (!rc && f->wgc)
+    rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
                      st);
   return rc;
 }

@@ -96,6 +96,8 @@ int gb_use_ct();  // 0 forces the generic passes (GBOFDFT_GENERIC_FFT=1)
 
 int gb_lwt_eval(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double* energies, int calc_v,
                 int calc_e, cudaStream_t st);
+int gb_wgc_eval(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
+                int calc_e, cudaStream_t st);
 
 // phi-space TN preconditioner of the uniform gas rho0 on the half spectrum (real, NG values)
 int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st);

@@ -1,0 +1,288 @@
+// WGC nonlocal kinetic term (density-dependent kernel, second-order
+// expansion about the mean density rho*).  No reference counterpart: the
+// method is Wang, Govind and Carter, Phys. Rev. B 60, 16350 (1999).
+//
+//   E_NL = int int rho^a(r) K(xi(r, r'); r - r') rho^b(r'),
+//   xi = [ (k_F(r)^g + k_F(r')^g) / 2 ]^(1/g),
+//   K(xi) = K0 + K1 (u + u')/6 + Kq (u^2 + u'^2) + Kx u u',  u = (rho - rho*)/rho*,
+// K1 = k dK/dk, K2 = k^2 d^2K/dk^2, Kq = (g - 5)/72 K1 + K2/72,
+// Kx = (1 - g)/36 K1 + K2/36, and the kernel's shape tabulated on the host so
+// that the expanded functional keeps the Lindhard response at rho*.  With
+//   X0 = K0*B + K1*(uB)/6 + Kq*(u^2 B), X1 = K1*B/6 + Kx*(uB), X2 = Kq*B
+// (A = rho^a, B = rho^b; Y0..Y2 the same with A):
+//   E = int A (X0 + u X1 + u^2 X2),
+//   V = A'(X0 + u X1 + u^2 X2) + (A/rho*)(X1 + 2u X2) + B'(Y0 + u Y1 + u^2 Y2) + (B/rho*)(Y1 + 2u Y2).
+// One evaluation: a pointwise pass (the 3 or 6 transformed fields), their
+// forward transforms, one reciprocal-space pass forming X and Y, the
+// inverse transforms and a pointwise pass adding V and reducing E.  With
+// a == b, Y = X and half the transforms are skipped.
+#include <math.h>
+
+#include "gkernels.cuh"
+#include "plan.h"
+
+namespace {
+
+constexpr double kZeroRho = 1e-30;
+
+size_t r256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct WgcBufs {
+  void* f[6];       // real fields: transform inputs, then X0..X2, Y0..Y2
+  void* s[6];       // spectra (internal layout)
+  double* part;     // per-CTA energy partials
+};
+
+constexpr int kBlocks = 1216;
+constexpr int kThreads = 256;
+
+WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
+  const size_t fb = r256(gb_elem(p) * (size_t)p->N), sb = r256(2 * gb_elem(p) * (size_t)p->NGld);
+  char* b = reinterpret_cast<char*>(work);
+  WgcBufs W;
+  for (int i = 0; i < 6; ++i) { W.f[i] = b; b += fb; }
+  for (int i = 0; i < 6; ++i) { W.s[i] = b; b += sb; }
+  W.part = reinterpret_cast<double*>(b);
+  return W;
+}
+
+size_t wgc_bytes(const gbofdft_plan* p) {
+  return 6 * r256(gb_elem(p) * (size_t)p->N) + 6 * r256(2 * gb_elem(p) * (size_t)p->NGld) +
+         r256(sizeof(double) * kBlocks);
+}
+
+// Column c of the kernel table at eta: cubic (Catmull-Rom) interpolation in
+// t = ln(eta) on the uniform table grid; eta^2 scaling below the first point
+// (the kernels go as eta^2 there), the last value beyond the table.
+__device__ double table_at(const double* __restrict__ tab, int m, double t0, double h, int c, double eta) {
+  const double* col = tab + (size_t)c * m;
+  if (eta <= 0.0) return 0.0;
+  const double t = log(eta);
+  if (t <= t0) {
+    const double r = eta / exp(t0);
+    return col[0] * r * r;
+  }
+  const double x = (t - t0) / h;
+  int i = (int)floor(x);
+  if (i >= m - 1) return col[m - 1];
+  const double u = x - i;
+  const double y1 = col[i], y2 = col[i + 1];
+  const double y0 = i > 0 ? col[i - 1] : 2.0 * y1 - y2;
+  const double y3 = i + 2 < m ? col[i + 2] : 2.0 * y2 - y1;
+  return y1 + 0.5 * u * ((y2 - y0) + u * ((2.0 * y0 - 5.0 * y1 + 4.0 * y2 - y3) + u * (3.0 * (y1 - y2) + y3 - y0)));
+}
+
+// K0, K1, Kq, Kx on the half spectrum (API layout, 4 consecutive arrays):
+// C times the table columns at eta = |G| / 2k_F, partner-averaged on the
+// symmetrised planes like the Wang-Teter kernel
+template <typename T>
+__global__ void k_wgc_kernels(GInfo g, double tkf, double C, const double* __restrict__ tab, int m, double t0,
+                              double h, T* __restrict__ out) {
+  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int k2 = (int)(id % g.n2h);
+    const int64_t r = id / g.n2h;
+    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+    for (int c = 0; c < 4; ++c) {
+      const double v = gbk::sym_kernel<double>(
+          g, i0, i1, k2, [&](double gg) { return C * table_at(tab, m, t0, h, c, sqrt(gg) / tkf); });
+      out[c * total + id] = (T)v;
+    }
+  }
+}
+
+// transform inputs: F0 = B, F1 = u B, F2 = u^2 B (and A, u A, u^2 A)
+template <typename T>
+__global__ void k_wgc_prep(int64_t n, const T* __restrict__ rho, double rho0, double a, double b, int two,
+                           T* __restrict__ f0, T* __restrict__ f1, T* __restrict__ f2, T* __restrict__ f3,
+                           T* __restrict__ f4, T* __restrict__ f5) {
+  const double inv0 = 1.0 / rho0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double rc = fmax((double)rho[i], kZeroRho);
+    const double u = (rc - rho0) * inv0;
+    const double B = pow(rc, b);
+    f0[i] = (T)B;
+    f1[i] = (T)(u * B);
+    f2[i] = (T)(u * u * B);
+    if (two) {
+      const double A = pow(rc, a);
+      f3[i] = (T)A;
+      f4[i] = (T)(u * A);
+      f5[i] = (T)(u * u * A);
+    }
+  }
+}
+
+// X^ from the three spectra of one exponent (in place), scaled by 1/N
+template <typename T>
+__global__ void k_wgc_combine(GInfo g, int ld2, const T* __restrict__ K, T scale, cpx<T>* __restrict__ s0,
+                              cpx<T>* __restrict__ s1, cpx<T>* __restrict__ s2) {
+  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int k2 = (int)(id % g.n2h);
+    const int64_t r = id / g.n2h;
+    const int64_t j = r * ld2 + k2;
+    const T k0 = K[id], k1 = K[total + id] * (T)(1.0 / 6.0), kq = K[2 * total + id], kx = K[3 * total + id];
+    const cpx<T> a = s0[j], bb = s1[j], c = s2[j];
+    s0[j] = cpx<T>{(k0 * a.x + k1 * bb.x + kq * c.x) * scale, (k0 * a.y + k1 * bb.y + kq * c.y) * scale};
+    s1[j] = cpx<T>{(k1 * a.x + kx * bb.x) * scale, (k1 * a.y + kx * bb.y) * scale};
+    s2[j] = cpx<T>{kq * a.x * scale, kq * a.y * scale};
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __restrict__ rho, double rho0, double a,
+                                                         double b, int two, const T* __restrict__ x0,
+                                                         const T* __restrict__ x1, const T* __restrict__ x2,
+                                                         const T* __restrict__ y0, const T* __restrict__ y1,
+                                                         const T* __restrict__ y2, T* __restrict__ pot, int calc_v,
+                                                         double* __restrict__ part) {
+  const double inv0 = 1.0 / rho0;
+  KSum es;
+  es.init();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double rc = fmax((double)rho[i], kZeroRho);
+    const double u = (rc - rho0) * inv0;
+    const double A = pow(rc, a);
+    const double X0 = x0[i], X1 = x1[i], X2 = x2[i];
+    const double sx = X0 + u * X1 + u * u * X2;
+    es.add(A * sx);
+    if (calc_v) {
+      double v;
+      if (two) {
+        const double B = pow(rc, b);
+        const double Y0 = y0[i], Y1 = y1[i], Y2 = y2[i];
+        v = a * A / rc * sx + A * inv0 * (X1 + 2.0 * u * X2) + b * B / rc * (Y0 + u * Y1 + u * u * Y2) +
+            B * inv0 * (Y1 + 2.0 * u * Y2);
+      } else {
+        v = 2.0 * (a * A / rc * sx + A * inv0 * (X1 + 2.0 * u * X2));
+      }
+      pot[i] = (T)((double)pot[i] + v);
+    }
+  }
+  __shared__ double red[kThreads / 32];
+  const double v = warp_sum(es.value());
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    KSum t;
+    t.init();
+    for (int w = 0; w < kThreads / 32; ++w) t.add(red[w]);
+    part[blockIdx.x] = t.value();
+  }
+}
+
+// energies[NL] and energies[TOTAL] += dV * sum(partials)
+__global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV, double* __restrict__ e) {
+  __shared__ double red[32];
+  KSum s;
+  s.init();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s.add(part[i]);
+  const double v = warp_sum(s.value());
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    KSum t;
+    t.init();
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t.add(red[w]);
+    const double en = t.value() * dV;
+    e[GB_E_NL] += en;
+    e[GB_E_TOTAL] += en;
+  }
+}
+
+template <typename T>
+int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
+            int calc_e, cudaStream_t st) {
+  WgcBufs W = wgc_layout(p, d->work);
+  const int two = fabs(d->alpha - d->beta) > 1e-12;
+  const int nfield = two ? 6 : 3;
+  const T* r = reinterpret_cast<const T*>(rho);
+  k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, d->rho0, d->alpha, d->beta, two, (T*)W.f[0], (T*)W.f[1],
+                                              (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
+  GB_CHECK_LAUNCH();
+  gb_count_launch();
+  const int op = OP_RHO;
+  for (int i = 0; i < nfield; ++i) {
+    int rc = gb_rows_fwd(p, W.f[i], W.s[i], 0, p->ld2, 1, &op, 1.0, 1.0, st);
+    if (!rc) rc = gb_cols(p, W.s[i], 0, p->ld2, 1, 1, -1, 1.0, st);
+    if (!rc) rc = gb_cols(p, W.s[i], 0, p->ld2, 1, 0, -1, 1.0, st);
+    if (rc) return rc;
+  }
+  const T* K = reinterpret_cast<const T*>(d->kernels);
+  const T scale = (T)(1.0 / (double)p->N);
+  for (int h = 0; h < (two ? 2 : 1); ++h) {
+    k_wgc_combine<T><<<kBlocks, kThreads, 0, st>>>(p->gi, p->ld2, K, scale, (cpx<T>*)W.s[3 * h],
+                                                    (cpx<T>*)W.s[3 * h + 1], (cpx<T>*)W.s[3 * h + 2]);
+    GB_CHECK_LAUNCH();
+    gb_count_launch();
+  }
+  const int64_t fstride = (int64_t)((char*)W.s[1] - (char*)W.s[0]) / (int64_t)(2 * gb_elem(p));
+  const int64_t ostride = (int64_t)((char*)W.f[1] - (char*)W.f[0]) / (int64_t)gb_elem(p);
+  for (int h = 0; h < (two ? 2 : 1); ++h) {
+    int rc = gb_cols(p, W.s[3 * h], fstride, p->ld2, 3, 0, 1, 1.0, st);
+    if (!rc) rc = gb_cols(p, W.s[3 * h], fstride, p->ld2, 3, 1, 1, 1.0, st);
+    if (!rc) rc = gb_rows_inv_store(p, W.s[3 * h], fstride, p->ld2, 3, W.f[3 * h], ostride, 1.0, st);
+    if (rc) return rc;
+  }
+  const T* y = reinterpret_cast<const T*>(two ? W.f[3] : W.f[0]);
+  k_wgc_final<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, d->rho0, d->alpha, d->beta, two, (const T*)W.f[0],
+                                               (const T*)W.f[1], (const T*)W.f[2], y,
+                                               two ? (const T*)W.f[4] : nullptr, two ? (const T*)W.f[5] : nullptr,
+                                               (T*)pot, calc_v, W.part);
+  GB_CHECK_LAUNCH();
+  gb_count_launch();
+  if (calc_e) {
+    k_wgc_energy<<<1, 256, 0, st>>>(W.part, kBlocks, p->dV, energies);
+    GB_CHECK_LAUNCH();
+    gb_count_launch();
+  }
+  return 0;
+}
+
+}  // namespace
+
+int gb_wgc_eval(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
+                int calc_e, cudaStream_t st) {
+  GB_REQUIRE(d->kernels && d->work, "wgc: kernels or workspace missing");
+  GB_REQUIRE(d->rho0 > 0.0, "wgc: rho0 must be positive (got %g)", d->rho0);
+  GB_REQUIRE(d->work_bytes >= (int64_t)wgc_bytes(p), "wgc: workspace %lld < %lld bytes", (long long)d->work_bytes,
+             (long long)wgc_bytes(p));
+  GB_REQUIRE(((uintptr_t)d->work & 255) == 0, "wgc: workspace must be 256-byte aligned");
+  return p->prec == GBOFDFT_F64 ? wgc_run<double>(p, rho, d, pot, energies, calc_v, calc_e, st)
+                                : wgc_run<float>(p, rho, d, pot, energies, calc_v, calc_e, st);
+}
+
+extern "C" {
+
+int gbofdft_wgc_workspace_bytes(const gbofdft_plan* p, int64_t* bytes) {
+  GB_REQUIRE(p && bytes, "wgc_workspace_bytes: null argument");
+  *bytes = (int64_t)wgc_bytes(p);
+  return GBOFDFT_OK;
+}
+
+int gbofdft_wgc_kernels(gbofdft_plan* p, double rho0, double alpha, double beta, const double* table, int m,
+                        double t0, double h, void* out, void* stream) {
+  GB_REQUIRE(p && out && table, "wgc_kernels: null argument");
+  GB_REQUIRE(rho0 > 0.0, "wgc_kernels: rho0 must be positive (got %g)", rho0);
+  GB_REQUIRE(m >= 4 && h > 0.0, "wgc_kernels: table needs >= 4 points and a positive step");
+  GB_REQUIRE(alpha > 0.0 && beta > 0.0, "wgc_kernels: alpha, beta must be positive");
+  const double kPi = 3.14159265358979323846;
+  const double tkf = 2.0 * cbrt(3.0 * rho0 * kPi * kPi);
+  const double ctf = 0.3 * pow(3.0 * kPi * kPi, 2.0 / 3.0);
+  const double C = 5.0 / (9.0 * alpha * beta * pow(rho0, alpha + beta - 5.0 / 3.0)) * ctf;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t total = p->NG;
+  const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
+  if (p->prec == GBOFDFT_F64)
+    k_wgc_kernels<double><<<nblk, 256, 0, st>>>(p->gi, tkf, C, table, m, t0, h, (double*)out);
+  else
+    k_wgc_kernels<float><<<nblk, 256, 0, st>>>(p->gi, tkf, C, table, m, t0, h, (float*)out);
+  GB_CHECK_LAUNCH();
+  gb_count_launch();
+  return GBOFDFT_OK;
+}
+
+}  // extern "C"

@@ -24,9 +24,10 @@ class Spec:
         self.vloc = None
         self.e_ion = 0.0
         self.lwt = None           # LWTTerm descriptor (gbofdft_lwt)
+        self.wgc = None           # WGCTerm descriptor (gbofdft_wgc)
 
     def merge(self, other):
-        for k in ("tf", "vw", "wt", "hartree", "lwt"):
+        for k in ("tf", "vw", "wt", "hartree", "lwt", "wgc"):
             if getattr(self, k) and getattr(other, k):
                 raise ValueError("functional component %s given twice" % k)
         if self.xc and other.xc:
@@ -51,6 +52,8 @@ class Spec:
             out.vloc = other.vloc
         if other.lwt is not None:
             out.lwt = other.lwt
+        if other.wgc is not None:
+            out.wgc = other.wgc
         out.e_ion = self.e_ion + other.e_ion
         return out
 
@@ -65,6 +68,8 @@ class Spec:
         f.e_ion = float(self.e_ion)
         if self.lwt is not None:
             f.lwt = ctypes.pointer(self.lwt)
+        if self.wgc is not None:
+            f.wgc = ctypes.pointer(self.wgc)
         return f
 
 

@@ -1,7 +1,8 @@
 """Kinetic energy density functionals (``functional/kedf/__init__.py``).
 
 Supported names (``KEDFEngines``, ``kedf/__init__.py:27-69``): TF, VW, the
-TF+vW family (TFVW, X_TF_Y_VW, XTFYVW), WT-NL and WT (= TF + VW + WT-NL).
+TF+vW family (TFVW, X_TF_Y_VW, XTFYVW), WT-NL and WT (= TF + VW + WT-NL),
+LWT/LMGP; and WGC / WGC-NL (density-dependent kernel, no reference counterpart).
 """
 import torch
 
@@ -21,6 +22,8 @@ KEDF_PARTS = {
     "XTFYVW": ("TF", "VW"),
     "WT-NL": ("WT",),
     "WT": ("TF", "VW", "WT"),
+    "WGC-NL": ("WGC",),
+    "WGC": ("TF", "VW", "WGC"),
 }
 
 
@@ -42,6 +45,11 @@ class KEDF(AbstractFunctional):
             kt = "MGP" if self.name.startswith("LMGP") else "WT"
             opts = {k: v for k, v in self.options.items() if k not in ("kedf", "y", "sigma")}
             self._lwt = LWTTerm(kerneltype=kt, **opts)
+        self._wgc = None
+        if "WGC" in KEDF_PARTS[self.name]:
+            from .wgc import WGCTerm
+            opts = {k: v for k, v in self.options.items() if k not in ("kedf", "y", "sigma")}
+            self._wgc = WGCTerm(**opts)
 
     @property
     def parts(self):
@@ -91,6 +99,8 @@ class KEDF(AbstractFunctional):
             sp.wt_kernel = self._wt_kernel(rho)
         if "LWT" in parts:
             sp.lwt = self._lwt.prepare(rho)
+        if "WGC" in parts:
+            sp.wgc = self._wgc.prepare(rho)
         return sp
 
     def stress(self, density, split=False, **kwargs):
@@ -106,7 +116,8 @@ class KEDF(AbstractFunctional):
         if en is not None:
             if split:
                 res = {}
-                for p, slot in (("TF", _lib.E_TF), ("VW", _lib.E_VW), ("WT", _lib.E_NL), ("LWT", _lib.E_NL)):
+                for p, slot in (("TF", _lib.E_TF), ("VW", _lib.E_VW), ("WT", _lib.E_NL), ("LWT", _lib.E_NL),
+                                ("WGC", _lib.E_NL)):
                     if p in self.parts:
                         res[p if p != "WT" else "NL"] = FunctionalOutput(name=p, energy=float(en[slot]))
                         self.energies[p] = float(en[slot])

@@ -27,6 +27,8 @@ def functional_stress(rho, spec, energies=None):
     """Dict term -> 3x3 for the terms the Spec enables (keys of TERMS)."""
     if spec.lwt is not None:
         raise NotImplementedError("the LWT/LMGP stress is not part of this path")
+    if spec.wgc is not None:
+        raise NotImplementedError("the WGC stress is not part of this path")
     if energies is None:
         energies, _ = evaluate(rho, spec, {"E"})
     plan = rho.grid.plan(rho.dtype)

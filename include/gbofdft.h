@@ -154,6 +154,33 @@ int gbofdft_lwt_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
 int gbofdft_mgp_table(const double* gp, const double* coef, int m, const double* eta, int neta, int maxpoints,
                       double* table_out, void* stream);
 
+/*
+ * WGC nonlocal kinetic term (density-dependent kernel): no reference
+ * counterpart (the reference's KEDF set, kedf/__init__.py:27-69, has none);
+ * the published method of Wang, Govind and Carter, PRB 60, 16350 (1999), with
+ * the two-body Fermi wavevector xi = [(k_F(r)^gamma + k_F(r')^gamma)/2]^(1/gamma)
+ * and the kernel expanded to second order in (rho - rho0)/rho0 about rho0.
+ * The kernel's shape w(eta) solves the linear-response equation (so that the
+ * expanded functional keeps the Lindhard response at rho0); it is tabulated
+ * on the host: table = 4 columns of m FP64 values (K0, K1, Kq, Kx per unit
+ * prefactor, device) on t = ln(eta) = t0 + i h.  gbofdft_wgc_kernels scales
+ * and interpolates them onto the half spectrum (API layout, plan precision)
+ * for one rho0.  Order 0 tables are the Wang-Teter kernel (K1 = Kq = Kx = 0).
+ * alpha == beta halves the work.  Its energy goes to the NL slot.
+ */
+typedef struct gbofdft_wgc {
+  double alpha, beta, gamma;
+  double rho0;                     /* expansion density (the mean density) */
+  int order;                       /* 0, 1 or 2 */
+  const void* kernels;             /* 4 x NG real values */
+  void* work;                      /* device workspace, 256-byte aligned */
+  int64_t work_bytes;              /* >= gbofdft_wgc_workspace_bytes */
+} gbofdft_wgc;
+
+int gbofdft_wgc_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
+int gbofdft_wgc_kernels(gbofdft_plan* plan, double rho0, double alpha, double beta, const double* table, int m,
+                        double t0, double h, void* kernels_out, void* stream);
+
 /* Functional composition for gbofdft_eval (TotalFunctional of
  * KEDF(TF/vW/WT/LWT) + XC(LDA) + HARTREE + PSEUDO). */
 typedef struct gbofdft_functional {
@@ -170,6 +197,7 @@ typedef struct gbofdft_functional {
   double e_ion;          /* constant ion-ion energy added to the total */
   gbofdft_lwt* lwt;      /* LWT/LMGP nonlocal term or NULL (its energy goes to the NL slot); the
                             call reads the density extrema back to the host to place the knots */
+  gbofdft_wgc* wgc;      /* WGC nonlocal term or NULL (its energy goes to the NL slot) */
 } gbofdft_functional;
 
 /*

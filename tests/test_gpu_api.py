@@ -565,3 +565,26 @@ def test_batch_matches_individual_solves(api):
         ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
         e_ref, _ = ev(a.rho.to_numpy())
         assert abs(a.energy - e_ref) < 1e-9 * abs(e_ref)
+
+
+def test_wgc_solve_alloy(api):
+    """TN with the WGC KEDF (second-order density-dependent kernel) on an
+    Al/Mg cell: converges, the energy equals the oracle's functional at the
+    solved density, and the mixed-precision solve agrees with FP64 within
+    1e-5 eV/atom."""
+    from dftpy_gb300 import batch
+    from oracle import wgc as W
+    st = systems.fcc_supercell((1, 1, 2), sigma=0.15, seed=4, nr=(32, 32, 64), mg_fraction=0.25, name="wgc")
+    res = {}
+    for prec in ("fp64", "mixed"):
+        r = batch.optimize_batch([st], workers=1, options={"precision": prec, "econv": 1e-8}, kedf="WGC")[0]
+        assert r.converged == 0, prec
+        res[prec] = r
+    rho = res["fp64"].rho.to_numpy()
+    g = O.Grid(st.lattice, st.nr)
+    ev = O.OFDFT(st.lattice, st.nr, st.positions, st.symbols, kedf="TFVW")
+    e_base, _ = ev(rho)
+    e_nl, _ = W.WGCNL()(rho, g)
+    # the oracle solves the kernel equation by another method (agreement ~1e-6)
+    assert abs(res["fp64"].energy - (e_base + e_nl)) < 2e-5 * abs(e_nl)
+    assert abs(res["mixed"].energy - res["fp64"].energy) / st.nat * 27.211386 < 1e-5

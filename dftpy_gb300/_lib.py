@@ -102,6 +102,17 @@ _SIGS = [
                                          ctypes.c_double, _P, _P]),
     ("gbofdft_lwt_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     ("gbofdft_wgc_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_nn_conv3d", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, _P]),
+    ("gbofdft_nn_conv3d_wgrad", ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, _P, _P, _P]),
+    ("gbofdft_nn_pointwise", ctypes.c_int, [ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _P]),
+    ("gbofdft_nn_sqerr", ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _P, _P, _P]),
+    ("gbofdft_nn_sqerr_work_bytes", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
+    ("gbofdft_nn_adam", ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_int, _P]),
+    ("gbofdft_nn_to_bf16", ctypes.c_int, [_P, _P, ctypes.c_int64, _P]),
     ("gbofdft_wgc_kernels", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_double, _P, _P]),
     ("gbofdft_mgp_table", ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, _P, _P]),

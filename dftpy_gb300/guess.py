@@ -1,0 +1,456 @@
+"""Learned initial guess: a 3-D convolutional encoder-decoder that maps the
+superposed atomic densities and the local pseudopotential on the grid to a
+starting sqrt(rho).
+
+No reference counterpart: the reference starts from a uniform density or
+superposed atomic densities (``density/density.py:151-319``); those remain
+the network's inputs and its baseline.  The network predicts the correction
+to sqrt(rho_atom) (in units of sqrt(rho0), rho0 the mean density); the
+truncated-Newton optimiser always finishes from the guess and judges it.
+
+Architecture (all convolutions 3x3x3 and periodic, SiLU activations):
+``levels`` resolutions, two convolutions per level on the way down (2x
+average pooling between levels), 2x nearest upsampling, one convolution,
+an additive skip from the encoder and a second convolution per level on the
+way up, and a 1-channel head.  The network is fully convolutional at the
+grid spacing of the workloads (0.24 Bohr), so a net trained on small cells
+applies to any cell whose grid extents are divisible by 2^(levels-1).
+Weights are BF16 for the arithmetic with FP32 master copies; every kernel
+(forward, input and weight gradients, pooling, activations, loss, Adam) is
+the project's own (``gbofdft_nn_*``).
+"""
+import ctypes
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib, systems
+
+SQRT_CLAMP = 1e-30
+
+
+def _L():
+    return _lib.load()
+
+
+class Conv:
+    """One 3x3x3 periodic convolution layer with FP32 master weights, a BF16
+    copy, gradients and Adam moments."""
+
+    def __init__(self, cin, cout, rng):
+        self.cin, self.cout = cin, cout
+        std = math.sqrt(2.0 / (27 * cin))
+        w = rng.normal(0.0, std, size=(cout, cin, 27)).astype(np.float32)
+        self.w = torch.tensor(w, device="cuda")
+        self.b = torch.zeros(cout, dtype=torch.float32, device="cuda")
+        self.wb = torch.empty((cout, cin, 27), dtype=torch.bfloat16, device="cuda")
+        self.gw = torch.zeros_like(self.w)
+        self.gb = torch.zeros_like(self.b)
+        self.mw, self.vw = torch.zeros_like(self.w), torch.zeros_like(self.w)
+        self.mb, self.vb = torch.zeros_like(self.b), torch.zeros_like(self.b)
+        self.sync_bf16()
+
+    def sync_bf16(self):
+        _lib.check(_L().gbofdft_nn_to_bf16(_lib.ptr(self.w), _lib.ptr(self.wb), self.w.numel(), _lib.stream_ptr()))
+
+    @property
+    def nparams(self):
+        return self.w.numel() + self.b.numel()
+
+    def forward(self, x, shape):
+        D, H, W = shape
+        z = torch.empty((self.cout, D, H, W), dtype=torch.float32, device="cuda")
+        _lib.check(_L().gbofdft_nn_conv3d(_lib.ptr(x), self.cin, _lib.ptr(self.wb), _lib.ptr(self.b), _lib.ptr(z),
+                                          self.cout, D, H, W, 0, _lib.stream_ptr()), "nn_conv3d")
+        return z
+
+    def backward(self, x, gz, shape, need_input_grad=True):
+        """Weight and bias gradients (overwritten) and the input gradient."""
+        D, H, W = shape
+        _lib.check(_L().gbofdft_nn_conv3d_wgrad(_lib.ptr(x), self.cin, _lib.ptr(gz), self.cout, D, H, W,
+                                                _lib.ptr(self.gw), _lib.ptr(self.gb), _lib.stream_ptr()),
+                   "nn_conv3d_wgrad")
+        if not need_input_grad:
+            return None
+        gx = torch.empty((self.cin, D, H, W), dtype=torch.float32, device="cuda")
+        _lib.check(_L().gbofdft_nn_conv3d(_lib.ptr(gz), self.cout, _lib.ptr(self.wb), None, _lib.ptr(gx), self.cin,
+                                          D, H, W, 1, _lib.stream_ptr()), "nn_conv3d_t")
+        return gx
+
+    def adam(self, lr, step, b1=0.9, b2=0.999, eps=1e-8):
+        L = _L()
+        s = _lib.stream_ptr()
+        _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.w), _lib.ptr(self.gw), _lib.ptr(self.mw), _lib.ptr(self.vw),
+                                     _lib.ptr(self.wb), self.w.numel(), lr, b1, b2, eps, step, s))
+        _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.b), _lib.ptr(self.gb), _lib.ptr(self.mb), _lib.ptr(self.vb),
+                                     None, self.b.numel(), lr, b1, b2, eps, step, s))
+
+
+def _pw(op, a, b, out, C, shape):
+    D, H, W = shape
+    _lib.check(_L().gbofdft_nn_pointwise(op, _lib.ptr(a), _lib.ptr(b) if b is not None else None, _lib.ptr(out), C,
+                                         D, H, W, _lib.stream_ptr()), "nn_pointwise")
+    return out
+
+
+SILU, SILU_BWD, ADD, POOL2, POOL2_BWD, UP2, UP2_BWD = range(7)
+
+
+def silu(z):
+    return _pw(SILU, z, None, torch.empty_like(z), z.shape[0], tuple(z.shape[1:]))
+
+
+def silu_bwd(z, ga):
+    return _pw(SILU_BWD, z, ga, torch.empty_like(z), z.shape[0], tuple(z.shape[1:]))
+
+
+def pool2(x):
+    C, D, H, W = x.shape
+    return _pw(POOL2, x, None, torch.empty((C, D // 2, H // 2, W // 2), dtype=x.dtype, device="cuda"), C, (D, H, W))
+
+
+def pool2_bwd(g, fine_shape):
+    C = g.shape[0]
+    return _pw(POOL2_BWD, g, None, torch.empty((C,) + tuple(fine_shape), dtype=g.dtype, device="cuda"), C,
+               fine_shape)
+
+
+def up2(x):
+    C, D, H, W = x.shape
+    fine = (2 * D, 2 * H, 2 * W)
+    return _pw(UP2, x, None, torch.empty((C,) + fine, dtype=x.dtype, device="cuda"), C, fine)
+
+
+def up2_bwd(g):
+    C, D, H, W = g.shape
+    return _pw(UP2_BWD, g, None, torch.empty((C, D // 2, H // 2, W // 2), dtype=g.dtype, device="cuda"), C,
+               (D, H, W))
+
+
+def add(a, b):
+    return _pw(ADD, a, b, torch.empty_like(a), a.shape[0], tuple(a.shape[1:]))
+
+
+class GuessNet:
+    """The encoder-decoder (see module doc); ``channels`` per level."""
+
+    IN_CHANNELS = 2
+
+    def __init__(self, channels=(16, 32, 48, 64), seed=0):
+        rng = np.random.default_rng(seed)
+        self.channels = tuple(int(c) for c in channels)
+        c = self.channels
+        self.enc = []
+        cin = self.IN_CHANNELS
+        for ch in c:
+            self.enc.append((Conv(cin, ch, rng), Conv(ch, ch, rng)))
+            cin = ch
+        self.dec = []
+        for lvl in range(len(c) - 2, -1, -1):
+            self.dec.append((Conv(c[lvl + 1], c[lvl], rng), Conv(c[lvl], c[lvl], rng)))
+        self.head = Conv(c[0], 1, rng)
+        self.step_count = 0
+        self._tape = None
+
+    @property
+    def layers(self):
+        out = []
+        for a, b in self.enc + self.dec:
+            out += [a, b]
+        return out + [self.head]
+
+    @property
+    def nparams(self):
+        return sum(l.nparams for l in self.layers)
+
+    @property
+    def stride(self):
+        return 2 ** (len(self.channels) - 1)
+
+    def forward(self, x, keep=False):
+        """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward needs."""
+        shape = tuple(x.shape[1:])
+        if any(s % self.stride for s in shape):
+            raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
+        tape = []
+        skips = []
+        h = x
+        for lvl, (c1, c2) in enumerate(self.enc):
+            sh = tuple(h.shape[1:])
+            z1 = c1.forward(h, sh)
+            a1 = silu(z1)
+            z2 = c2.forward(a1, sh)
+            a2 = silu(z2)
+            tape.append(("enc", lvl, h, z1, a1, z2))
+            skips.append(a2)
+            h = pool2(a2) if lvl < len(self.enc) - 1 else a2
+        for k, (c1, c2) in enumerate(self.dec):
+            lvl = len(self.channels) - 2 - k
+            u = up2(h)
+            sh = tuple(u.shape[1:])
+            z1 = c1.forward(u, sh)
+            a1 = silu(z1)
+            s = add(a1, skips[lvl])
+            z2 = c2.forward(s, sh)
+            h = silu(z2)
+            tape.append(("dec", lvl, u, z1, s, z2))
+        out = self.head.forward(h, shape)
+        tape.append(("head", 0, h))
+        self._tape = tape if keep else None
+        return out
+
+    def backward(self, gout):
+        """Gradients of every layer from d loss / d out (the last forward's tape)."""
+        tape = self._tape
+        if tape is None:
+            raise RuntimeError("forward(keep=True) must precede backward")
+        _, _, h = tape[-1]
+        shape = tuple(h.shape[1:])
+        g = self.head.backward(h, gout, shape)
+        gskip = {}
+        for k in range(len(self.dec) - 1, -1, -1):
+            _, lvl, u, z1, s, z2 = tape[len(self.enc) + k]
+            c1, c2 = self.dec[k]
+            sh = tuple(u.shape[1:])
+            gz2 = silu_bwd(z2, g)
+            gs = c2.backward(s, gz2, sh)
+            gskip[lvl] = gs
+            gz1 = silu_bwd(z1, gs)
+            gu = c1.backward(u, gz1, sh)
+            g = up2_bwd(gu)
+        for lvl in range(len(self.enc) - 1, -1, -1):
+            _, _, hin, z1, a1, z2 = tape[lvl]
+            c1, c2 = self.enc[lvl]
+            sh = tuple(hin.shape[1:])
+            if lvl < len(self.enc) - 1:
+                g = pool2_bwd(g, sh)
+            if lvl in gskip:
+                g = add(g, gskip[lvl])
+            gz2 = silu_bwd(z2, g)
+            ga1 = c2.backward(a1, gz2, sh)
+            gz1 = silu_bwd(z1, ga1)
+            g = c1.backward(hin, gz1, sh, need_input_grad=lvl > 0)
+        self._tape = None
+
+    def adam_step(self, lr):
+        self.step_count += 1
+        for l in self.layers:
+            l.adam(lr, self.step_count)
+
+    def state(self):
+        return {"channels": np.array(self.channels),
+                **{"w%d" % i: l.w.cpu().numpy() for i, l in enumerate(self.layers)},
+                **{"b%d" % i: l.b.cpu().numpy() for i, l in enumerate(self.layers)}}
+
+    def save(self, path):
+        np.savez_compressed(path, **self.state())
+
+    @classmethod
+    def load(cls, path):
+        d = np.load(path)
+        net = cls(channels=tuple(int(c) for c in d["channels"]))
+        for i, l in enumerate(net.layers):
+            l.w.copy_(torch.tensor(d["w%d" % i]))
+            l.b.copy_(torch.tensor(d["b%d" % i]))
+            l.sync_bf16()
+        return net
+
+
+# --------------------------------------------------------------------------
+# features, targets, the guess
+# --------------------------------------------------------------------------
+
+def features(total, grid):
+    """Network input (2, D, H, W): superposed Gaussian atomic densities over
+    the mean minus one, and v_loc; plus sqrt(rho_atom) and rho0."""
+    from .density import get_3d_value_recipe
+    ps = total.PSEUDO
+    ions = ps.ions
+    tabs = {s: systems.atomic_density_table(systems.SPECIES[s][0], systems.ATOMIC_SIGMA[s]) for s in set(ions.symbols)}
+    r = {s: t[0] for s, t in tabs.items()}
+    arho = {s: t[1] for s, t in tabs.items()}
+    ratom = get_3d_value_recipe(r, arho, ions, grid, dtol=1e-12)
+    rho0 = float(ions.get_ncharges()) / grid.volume
+    ra = ratom.as_subclass(torch.Tensor).to(torch.float32)
+    vloc = ps.vreal_of(torch.float64).to(torch.float32).reshape(ra.shape)
+    x = torch.stack([ra / rho0 - 1.0, vloc]).contiguous()
+    phib = torch.sqrt(torch.clamp(ra, min=SQRT_CLAMP))
+    return x, phib, rho0
+
+
+class LearnedGuess:
+    """Starting density from a trained ``GuessNet``."""
+
+    def __init__(self, net):
+        self.net = net
+
+    def guess(self, total, grid=None, dtype=torch.float64):
+        from .field import DirectField
+        grid = grid or total.PSEUDO.grid
+        x, phib, rho0 = features(total, grid)
+        out = self.net.forward(x)[0]
+        phi = phib + math.sqrt(rho0) * out
+        rho = (phi * phi).to(torch.float64)
+        nel = float(total.PSEUDO.ions.get_ncharges())
+        rho = rho * (nel / (float(rho.sum()) * grid.dV))
+        return DirectField(grid, data=rho.to(dtype))
+
+
+def _solve(total, guess, precision="mixed", econv_per_atom=1e-8):
+    from .optimization import Optimization
+    nat = total.PSEUDO.ions.nat
+    opt = Optimization(EnergyEvaluator=total, optimization_method="TN",
+                       optimization_options={"econv": econv_per_atom * nat, "maxfun": 50, "maxiter": 100,
+                                             "precision": precision})
+    rho = opt.optimize_rho(guess_rho=guess)
+    return opt, rho
+
+
+def training_cell(seed, reps=(2, 2, 2), nr=(64, 64, 64)):
+    """Training / validation cell: an Al/Mg snapshot as the batched workload
+    draws them (Mg fraction U(0, 0.3), jitter 0.15 Bohr) on a small cell."""
+    f = float(np.random.default_rng(10_000 + seed).random() * 0.3)
+    return systems.fcc_supercell(reps, sigma=0.15, seed=seed, nr=nr, mg_fraction=f, name="train_%d" % seed)
+
+
+def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 64, 64), workers=16, chunk=64):
+    """(x, sqrt(rho_atom), sqrt(rho converged), rho0) per seed from the
+    solver's own converged densities (solved as batches)."""
+    from .batch import build_evaluator, optimize_batch
+    data = []
+    seeds = list(seeds)
+    for c0 in range(0, len(seeds), chunk):
+        jobs = [build_evaluator(training_cell(s, reps, nr), kedf=kedf) for s in seeds[c0:c0 + chunk]]
+        res = optimize_batch(jobs, workers=workers, options={"precision": precision})
+        for (total, rho_u), r in zip(jobs, res):
+            x, phib, rho0 = features(total, rho_u.grid)
+            phit = torch.sqrt(torch.clamp(r.rho.as_subclass(torch.Tensor).to(torch.float32), min=SQRT_CLAMP))
+            data.append((x, phib, phit, rho0))
+    return data
+
+
+def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None):
+    """Adam on the normalised squared error of sqrt(rho) (one cell per step),
+    random periodic translations; cosine learning-rate decay."""
+    L = _L()
+    nb = ctypes.c_int64()
+    _lib.check(L.gbofdft_nn_sqerr_work_bytes(ctypes.byref(nb)))
+    work = torch.empty(int(nb.value) // 8 + 8, dtype=torch.float64, device="cuda")
+    loss_d = torch.zeros(1, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(seed)
+    nsteps = epochs * len(data)
+    hist = []
+    k = 0
+    for ep in range(epochs):
+        order = rng.permutation(len(data))
+        tot = 0.0
+        for i in order:
+            x, phib, phit, rho0 = data[i]
+            sh = [int(rng.integers(n)) for n in x.shape[1:]]
+            x_ = torch.roll(x, shifts=sh, dims=(1, 2, 3)).contiguous()
+            pb = torch.roll(phib, shifts=sh, dims=(0, 1, 2)).contiguous()
+            pt = torch.roll(phit, shifts=sh, dims=(0, 1, 2)).contiguous()
+            out = net.forward(x_, keep=True)
+            s0 = math.sqrt(rho0)
+            pred = (pb + s0 * out[0]).contiguous()
+            grad = torch.empty_like(pred)
+            _lib.check(L.gbofdft_nn_sqerr(_lib.ptr(pred), _lib.ptr(pt), pred.numel(), _lib.ptr(grad),
+                                          _lib.ptr(loss_d), _lib.aligned_ptr(work, 16), _lib.stream_ptr()))
+            net.backward((grad * s0).reshape(out.shape).contiguous())
+            t = k / max(1, nsteps - 1)
+            net.adam_step(lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * t)))
+            k += 1
+            tot += float(loss_d)
+        hist.append(tot / len(data))
+        if log:
+            log("epoch %d loss %.3e" % (ep, hist[-1]))
+    return hist
+
+
+def evaluate_guesses(net, structures, kedf="WGC", precision="mixed"):
+    """TN from the uniform density, from the superposed atomic densities and
+    from the learned guess; per structure the evaluations, iterations, wall
+    time (guess included) and energy."""
+    from .batch import build_evaluator
+    from .field import DirectField
+    rows = []
+    lg = LearnedGuess(net)
+    for st in structures:
+        res = {}
+        for mode in ("uniform", "atomic", "learned"):
+            total, rho_u = build_evaluator(st, kedf=kedf)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "uniform":
+                g = rho_u
+            elif mode == "atomic":
+                x, phib, rho0 = features(total, rho_u.grid)
+                g = DirectField(rho_u.grid, data=(phib * phib).to(torch.float64))
+                g = g * (st.nelec / (float(g.sum()) * rho_u.grid.dV))
+            else:
+                g = lg.guess(total, rho_u.grid)
+            opt, rho = _solve(total, g, precision)
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            ev = sum(s["n_eval_ev"] + s["n_eval_v"] for s in opt.stats["stages"])
+            it = sum(s["n_iter"] for s in opt.stats["stages"])
+            res[mode] = {"wall_s": t, "evals": ev, "iters": it, "energy": float(opt.energy),
+                         "converged": int(opt.converged)}
+        rows.append({"name": st.name, "nr": list(st.nr), "nat": st.nat, **res})
+    return rows
+
+
+def main():
+    import argparse
+    import json
+    p = argparse.ArgumentParser(description="train the learned-guess network on the solver's own densities")
+    p.add_argument("--train", type=int, default=400, help="training cells (seeds 1000 ...)")
+    p.add_argument("--epochs", type=int, default=8)
+    p.add_argument("--lr", type=float, default=1e-3)
+    p.add_argument("--channels", default="16,32,48,64")
+    p.add_argument("--eval", type=int, default=8, help="held-out cells (seeds 5000 ...)")
+    p.add_argument("--eval-large", type=int, default=4, help="held-out batched-workload snapshots")
+    p.add_argument("--out", default=None)
+    a = p.parse_args()
+    t0 = time.perf_counter()
+    data = make_dataset(range(1000, 1000 + a.train))
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = GuessNet(channels=tuple(int(c) for c in a.channels.split(",")), seed=0)
+    t1 = time.perf_counter()
+    hist = train(net, data, epochs=a.epochs, lr=a.lr, log=lambda s: print(s, flush=True))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    if a.out:
+        net.save(a.out)
+    held = [training_cell(s) for s in range(5000, 5000 + a.eval)]
+    rows = evaluate_guesses(net, held)
+    large = [systems.config_alloy(5000 + s) for s in range(a.eval_large)]
+    rows_l = evaluate_guesses(net, large)
+
+    def summary(rs):
+        out = {}
+        for m in ("uniform", "atomic", "learned"):
+            out[m] = {"evals": sum(r[m]["evals"] for r in rs), "iters": sum(r[m]["iters"] for r in rs),
+                      "wall_s": sum(r[m]["wall_s"] for r in rs),
+                      "converged": sum(r[m]["converged"] == 0 for r in rs),
+                      "max_dE_eV_per_atom_vs_uniform": max(abs(r[m]["energy"] - r["uniform"]["energy"]) / r["nat"]
+                                                           * 27.211386024367243 for r in rs)}
+        return out
+    x, phib, phit, rho0 = data[0]
+    t2 = time.perf_counter()
+    for _ in range(10):
+        net.forward(x)
+    torch.cuda.synchronize()
+    t_inf = (time.perf_counter() - t2) / 10
+    print(json.dumps({"params": net.nparams, "channels": list(net.channels), "train_cells": a.train,
+                      "epochs": a.epochs, "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+                      "data_s": t_data, "train_s": t_train, "inference_64cubed_s": t_inf,
+                      "heldout_64": summary(rows), "heldout_batched": summary(rows_l),
+                      "rows": rows + rows_l}))
+
+
+if __name__ == "__main__":
+    main()

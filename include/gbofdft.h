@@ -456,6 +456,35 @@ int gbofdft_optimize_tn_split(gbofdft_plan* plan, const gbofdft_functional* f, g
  */
 int gbofdft_dcsrch(double* state, int64_t state_len, double* stp, double f, double g, int task);
 
+/* ---- learned initial guess: network kernels ----------------------------------
+ * No reference counterpart (the reference's guesses are density/density.py:
+ * 151-319: uniform or superposed atomic densities; the network maps those
+ * and v_loc to a starting sqrt(rho)).  Activations [C][D][H][W] FP32 on a
+ * periodic grid; weights [C_out][C_in][27] BF16 (tap = (dz+1)*9 + (dy+1)*3 +
+ * (dx+1)); FP32 accumulation; all pointers device.
+ */
+
+/* out = conv(in) + bias; transposed != 0: the input gradient (weights
+ * transposed in (C_out, C_in), taps reversed; in = output gradient with cin =
+ * the layer's C_out, out with cout = its C_in; bias must be NULL). */
+int gbofdft_nn_conv3d(const float* in, int cin, const void* w_bf16, const float* bias, float* out, int cout, int D,
+                      int H, int W, int transposed, void* stream);
+/* gw[co][ci][tap] = sum_v gout[co][v] in[ci][v + d_tap]; gb[co] = sum_v gout[co][v] (gb may be NULL). */
+int gbofdft_nn_conv3d_wgrad(const float* in, int cin, const float* gout, int cout, int D, int H, int W, float* gw,
+                            float* gb, void* stream);
+/* op: 0 SiLU(a), 1 b * SiLU'(a), 2 a + b, 3 2x average pool, 4 its adjoint, 5 2x nearest upsample, 6 its
+ * adjoint; (C, D, H, W) are the fine-grid extents for ops 3-6. */
+int gbofdft_nn_pointwise(int op, const float* a, const float* b, float* out, int C, int D, int H, int W,
+                         void* stream);
+/* loss = sum (pred - target)^2 / sum target^2 (device double), grad = d loss / d pred (may be NULL). */
+int gbofdft_nn_sqerr(const float* pred, const float* target, int64_t n, float* grad, double* loss_dev, void* work,
+                     void* stream);
+int gbofdft_nn_sqerr_work_bytes(int64_t* bytes);
+/* Adam step on FP32 master weights w (moments m, v; step >= 1); refreshes the BF16 copy when w_bf16 != NULL. */
+int gbofdft_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, int64_t n, double lr, double b1,
+                    double b2, double eps, int step, void* stream);
+int gbofdft_nn_to_bf16(const float* a, void* b, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,143 @@
+"""The learned-guess network kernels against the numpy oracle (FP64, the
+same BF16-rounded weights), whole-network gradients against finite
+differences of the oracle's loss, and the trained network's gain."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import guessnet as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gn():
+    from dftpy_gb300 import _lib
+    _lib.require_cuda()
+    from dftpy_gb300 import guess
+    return guess
+
+
+def _bf16_round(a):
+    import torch
+    return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).to(torch.float64).numpy()
+
+
+@pytest.mark.parametrize("shape,cin,cout", [((4, 6, 8), 3, 37), ((8, 8, 8), 16, 32), ((2, 4, 2), 5, 1)])
+def test_conv_kernels(gn, shape, cin, cout):
+    import torch
+    rng = np.random.default_rng(2)
+    layer = gn.Conv(cin, cout, rng)
+    layer.b.copy_(torch.tensor(rng.standard_normal(cout), dtype=torch.float32))
+    x = rng.standard_normal((cin,) + shape).astype(np.float32)
+    g = rng.standard_normal((cout,) + shape).astype(np.float32)
+    xd = torch.tensor(x, device="cuda")
+    gd = torch.tensor(g, device="cuda")
+    w = _bf16_round(layer.w.cpu().numpy())
+    b = layer.b.cpu().numpy().astype(np.float64)
+    y = layer.forward(xd, shape).cpu().numpy()
+    yr = G.conv3d(x.astype(np.float64), w, b)
+    assert np.abs(y - yr).max() <= 1e-5 * np.abs(yr).max()
+    gx = layer.backward(xd, gd, shape).cpu().numpy()
+    gxr = G.conv3d_input_grad(g.astype(np.float64), w)
+    assert np.abs(gx - gxr).max() <= 1e-5 * np.abs(gxr).max()
+    gwr, gbr = G.conv3d_weight_grad(x.astype(np.float64), g.astype(np.float64))
+    assert np.abs(layer.gw.cpu().numpy() - gwr).max() <= 1e-5 * np.abs(gwr).max()
+    assert np.abs(layer.gb.cpu().numpy() - gbr).max() <= 1e-5 * np.abs(gbr).max()
+
+
+def test_pointwise_kernels(gn):
+    import torch
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((3, 4, 6, 8)).astype(np.float32)
+    c = rng.standard_normal((3, 2, 3, 4)).astype(np.float32)
+    xd, cd = torch.tensor(x, device="cuda"), torch.tensor(c, device="cuda")
+    np.testing.assert_allclose(gn.silu(xd).cpu().numpy(), G.silu(x.astype(np.float64)), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(gn.silu_bwd(xd, xd).cpu().numpy(), x * G.silu_grad(x.astype(np.float64)),
+                               rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(gn.pool2(xd).cpu().numpy(), G.pool2(x), rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(gn.pool2_bwd(cd, (4, 6, 8)).cpu().numpy(), G.pool2_adjoint(c), rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(gn.up2(cd).cpu().numpy(), G.up2(c), rtol=0, atol=0)
+    np.testing.assert_allclose(gn.up2_bwd(xd).cpu().numpy(), G.up2_adjoint(x), rtol=1e-6, atol=1e-6)
+
+
+def _oracle_weights(net):
+    def wb(l):
+        return _bf16_round(l.w.cpu().numpy()), l.b.cpu().numpy().astype(np.float64)
+    enc = [wb(a) + wb(b) for a, b in net.enc]
+    dec = [wb(a) + wb(b) for a, b in net.dec]
+    return enc, dec, wb(net.head)
+
+
+def test_network_forward_and_gradients(gn):
+    """Forward equals the oracle's; the weight gradients of the loss
+    sum(out * c) equal the oracle's central differences (FP64)."""
+    import torch
+    net = gn.GuessNet(channels=(4, 6, 8), seed=1)
+    rng = np.random.default_rng(4)
+    for l in net.layers:     # non-zero biases exercise every path
+        l.b.copy_(torch.tensor(0.1 * rng.standard_normal(l.cout), dtype=torch.float32))
+    x = rng.standard_normal((2, 8, 8, 12)).astype(np.float32)
+    c = rng.standard_normal((1, 8, 8, 12)).astype(np.float32)
+    out = net.forward(torch.tensor(x, device="cuda"), keep=True).cpu().numpy()
+    enc, dec, head = _oracle_weights(net)
+    ref = G.net_forward(x.astype(np.float64), enc, dec, head)
+    assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max()
+    net.backward(torch.tensor(c, device="cuda"))
+    e = 1e-4
+    checks = [("enc", 0, 0, (1, 0, 13)), ("enc", 2, 2, (3, 5, 0)), ("dec", 0, 0, (2, 7, 26)), ("dec", 1, 2, (0, 3, 4)),
+              ("head", 0, 0, (0, 2, 13))]
+    for kind, lvl, which, idx in checks:
+        if kind == "head":
+            layer = net.head
+        else:
+            layer = (net.enc if kind == "enc" else net.dec)[lvl][which // 2]
+        g_gpu = float(layer.gw.cpu().numpy()[idx])
+
+        def loss(delta):
+            enc2, dec2, head2 = _oracle_weights(net)
+            if kind == "head":
+                w = head2[0].copy()
+                w[idx] += delta
+                head2 = (w, head2[1])
+            else:
+                lst = enc2 if kind == "enc" else dec2
+                t = list(lst[lvl])
+                w = t[which].copy()
+                w[idx] += delta
+                t[which] = w
+                lst[lvl] = tuple(t)
+            return float((G.net_forward(x.astype(np.float64), enc2, dec2, head2) * c).sum())
+        fd = (loss(e) - loss(-e)) / (2 * e)
+        assert abs(g_gpu - fd) <= 2e-3 * max(1.0, abs(fd)), (kind, lvl, which, idx, g_gpu, fd)
+
+
+def test_training_reduces_loss(gn):
+    """A few Adam steps on one synthetic cell lower the normalised error."""
+    import torch
+    net = gn.GuessNet(channels=(4, 8), seed=0)
+    rng = np.random.default_rng(5)
+    x = torch.tensor(rng.standard_normal((2, 8, 8, 8)).astype(np.float32), device="cuda")
+    phib = torch.full((8, 8, 8), 0.15, dtype=torch.float32, device="cuda")
+    phit = (phib + 0.02 * x[0].tanh()).contiguous()
+    hist = gn.train(net, [(x, phib, phit, 0.02)], epochs=60, lr=3e-3, lr_min=3e-4)
+    assert hist[-1] < 0.5 * hist[0]
+
+
+TRAINED = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "dftpy_gb300", "data",
+                       "guessnet.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(TRAINED), reason="no trained network committed")
+def test_trained_network_gain(gn):
+    """On held-out Al/Mg cells (seeds outside the training set) the learned
+    guess needs fewer TN evaluations than the uniform start and reaches the
+    same energy (within 1e-5 eV/atom)."""
+    net = gn.GuessNet.load(TRAINED)
+    cells = [gn.training_cell(s) for s in (5000, 5001, 5002)]
+    rows = gn.evaluate_guesses(net, cells)
+    for r in rows:
+        assert r["learned"]["converged"] == 0 and r["uniform"]["converged"] == 0
+        assert abs(r["learned"]["energy"] - r["uniform"]["energy"]) / r["nat"] * 27.211386 < 1e-5
+    assert sum(r["learned"]["evals"] for r in rows) < 0.8 * sum(r["uniform"]["evals"] for r in rows)

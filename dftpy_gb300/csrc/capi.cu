@@ -185,8 +185,32 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   // FP32 grids whose (n0, n1) plane fits in shared memory evaluate through
   // the plane pipeline (GBOFDFT_PLANE=0 selects the column passes instead)
   const char* pe = getenv("GBOFDFT_PLANE");
-  p->plane = precision == GBOFDFT_F32 && !(pe && pe[0] == '0') && gb_plane_supported_f32(nr[0], nr[1], nr[2]);
+  p->plane_ok = precision == GBOFDFT_F32 && gb_plane_supported_f32(nr[0], nr[1], nr[2]);
+  p->plane = p->plane_ok && !(pe && pe[0] == '0');
+  p->plane_variant = 0;
   *out = p;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_plan_schedules(const gbofdft_plan* p, int* count) {
+  GB_REQUIRE(p && count, "plan_schedules: null argument");
+  *count = 1 + (p->plane_ok ? gb_plane_variants_f32(p->n[0], p->n[1]) : 0);
+  return GBOFDFT_OK;
+}
+
+int gbofdft_plan_set_schedule(gbofdft_plan* p, int schedule) {
+  GB_REQUIRE(p, "plan_set_schedule: null argument");
+  int count = 0;
+  gbofdft_plan_schedules(p, &count);
+  GB_REQUIRE(schedule >= 0 && schedule < count, "plan_set_schedule: schedule %d outside [0, %d)", schedule, count);
+  p->plane = schedule > 0;
+  p->plane_variant = schedule > 0 ? schedule - 1 : 0;
+  return GBOFDFT_OK;
+}
+
+int gbofdft_plan_get_schedule(const gbofdft_plan* p, int* schedule) {
+  GB_REQUIRE(p && schedule, "plan_get_schedule: null argument");
+  *schedule = p->plane ? 1 + p->plane_variant : 0;
   return GBOFDFT_OK;
 }
 

@@ -702,9 +702,9 @@ int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, dou
   if (p->prec == GBOFDFT_F64) {
     k_wt_kernel<double><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<double*>(out), nullptr);
   } else {
-    // plans with the plane pipeline keep a plane-major copy of the table
+    // plans that can use the plane pipeline keep a plane-major copy of the table
     // (allocated with the first table built on the plan)
-    if (p->plane && !p->wt_pm) {
+    if (p->plane_ok && !p->wt_pm) {
       cudaError_t e = cudaMalloc(&p->wt_pm, sizeof(float) * (size_t)p->NG);
       if (e != cudaSuccess) {
         p->wt_pm = nullptr;
@@ -712,8 +712,8 @@ int gb_build_wt_kernel(gbofdft_plan* p, double rho0, double x, double alpha, dou
       }
     }
     k_wt_kernel<float><<<nblk, 256, 0, st>>>(p->gi, tkf, factor, x, reinterpret_cast<float*>(out),
-                                             p->plane ? p->wt_pm : nullptr);
-    p->wt_pm_src = p->plane ? out : nullptr;
+                                             p->plane_ok ? p->wt_pm : nullptr);
+    p->wt_pm_src = p->plane_ok ? out : nullptr;
   }
   GB_CHECK_LAUNCH();
   return 0;

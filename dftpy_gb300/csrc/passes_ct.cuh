@@ -702,8 +702,17 @@ inline int plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, 
         return;
       }
     const size_t sm = PlaneCfg<N0, N1>::kSmem;
-    if ((rc = ct_smem(k_plane_conv<N0, N1>, sm))) return;
-    k_plane_conv<N0, N1><<<dim3(p->n2h, nf), PlaneCfg<N0, N1>::NT, sm, st>>>(a);
+    auto launch = [&](auto kern) {
+      if ((rc = ct_smem(kern, sm))) return;
+      kern<<<dim3(p->n2h, nf), PlaneCfg<N0, N1>::NT, sm, st>>>(a);
+    };
+    if constexpr (plane_variants<N0, N1>() > 1) {
+      if (p->plane_variant == 1) launch(k_plane_conv<N0, N1, 1>);
+      else launch(k_plane_conv<N0, N1, 0>);
+    } else {
+      launch(k_plane_conv<N0, N1, 0>);
+    }
+    if (rc) return;
     gb_count_launch();
     cudaError_t e = cudaGetLastError();
     rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "plane_conv: %s", cudaGetErrorString(e));
@@ -733,6 +742,13 @@ inline int plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, 
     bool rows = gbct::ct_dispatch(n2, [](auto) {});                                                            \
     bool plane = gbct::plane_dispatch(n0, n1, [](auto, auto) {});                                              \
     return rows && plane;                                                                                      \
+  }                                                                                                            \
+  int gb_plane_variants_f32(int n0, int n1) {                                                                  \
+    int nv = 0;                                                                                                \
+    gbct::plane_dispatch(n0, n1, [&](auto a0, auto a1) {                                                       \
+      nv = gbct::plane_variants<decltype(a0)::value, decltype(a1)::value>();                                   \
+    });                                                                                                        \
+    return nv;                                                                                                 \
   }
 
 // Instantiate the launchers of one precision (one translation unit each).

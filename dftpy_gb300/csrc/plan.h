@@ -31,7 +31,9 @@ struct gbofdft_plan {
   int pairs;             // row pairs per CTA in the row passes
   GInfo gi;
   // FP32 plane-major evaluation pipeline (rows -> plane convolution -> rows)
-  int plane;             // 1: the grid has the plane pipeline
+  int plane;             // 1: the grid has the plane pipeline (and uses it)
+  int plane_ok;          // 1: the grid has a plane specialisation
+  int plane_variant;     // radix-schedule variant of the plane pass (autotuned)
   float* wt_pm;          // plane-major copy of the last WT kernel table built on this plan
   const void* wt_pm_src; // the table that copy belongs to
 };
@@ -84,6 +86,7 @@ int gb_ct_rows_inv_eval_pm_f32(gbofdft_plan*, const void*, int64_t, int, const E
                                void*, int, double*, int64_t*, cudaStream_t);
 int gb_plane_conv_f32(gbofdft_plan*, void*, int64_t, int, const KerDesc*, const float* const*, double, cudaStream_t);
 int gb_plane_supported_f32(int n0, int n1, int n2);
+int gb_plane_variants_f32(int n0, int n1);
 // the plane-major evaluation (returns 1 when the plan has no plane pipeline
 // or a kernel table has no plane-major copy)
 int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, double beta, const KerDesc& kd,

@@ -72,12 +72,15 @@ constexpr int plane_chunks() {
   return NL;
 }
 
-// radix schedules of the plane transforms (fewer, larger stages than the
-// line passes: every stage is a full read and write of the plane)
-template <int N> struct PlaneSched { using S = typename Plan<N>::S; };
+// radix schedules of the plane transforms (every stage is a full read and
+// write of the plane, so fewer, larger stages are usually better).  V selects
+// a variant where there is more than one: for 128, V = 0 is 16 x 8 and V = 1
+// is the line passes' 8 x 4 x 4 (the autotuner times both).
+template <int N, int V> struct PlaneSched { using S = typename Plan<N>::S; };
 #if GB_PLANE_R16
-template <> struct PlaneSched<128> { using S = Sched<16, 8>; };
+template <> struct PlaneSched<128, 0> { using S = Sched<16, 8>; };
 #endif
+template <int N0, int N1> constexpr int plane_variants() { return (N0 == 128 || N1 == 128) ? 2 : 1; }
 
 template <int N1>
 __device__ __forceinline__ int paddr(int i0, int i1) {
@@ -152,9 +155,9 @@ __device__ __forceinline__ void prun_sched(Sched<Rs...>, float2* pl, const float
 }
 
 // whole-plane 1-D transforms along one axis
-template <int DIR, int AX, int N0, int N1>
+template <int DIR, int AX, int N0, int N1, int V>
 __device__ __forceinline__ void plane_fft(float2* pl, const float2* tw) {
-  prun_sched<DIR, AX, N0, N1>(typename PlaneSched<AX == 1 ? N1 : N0>::S{}, pl, tw);
+  prun_sched<DIR, AX, N0, N1>(typename PlaneSched<AX == 1 ? N1 : N0, V>::S{}, pl, tw);
 }
 
 struct PlaneArgs {
@@ -169,7 +172,7 @@ struct PlaneArgs {
   float coef[GB_MAX_FIELDS];
 };
 
-template <int N0, int N1>
+template <int N0, int N1, int V>
 __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArgs a) {
   constexpr int kPlaneThreads = PlaneCfg<N0, N1>::NT;
   constexpr int NP1 = Pad<float, N1>::NP;
@@ -238,8 +241,8 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
     gB[2 * N1 + i] = m1 * a.bgf[5];
   }
   __syncthreads();
-  plane_fft<-1, 1, N0, N1>(pl, tw1);
-  plane_fft<-1, 0, N0, N1>(pl, tw0);
+  plane_fft<-1, 1, N0, N1, V>(pl, tw1);
+  plane_fft<-1, 0, N0, N1, V>(pl, tw0);
   // kernel multiply; points on a Nyquist line of a symmetrised plane take
   // the partner-averaged general path (as the column passes do)
   const bool plane_sym = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
@@ -269,8 +272,8 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
     pl[p] = c_scale(pl[p], kv);
   }
   __syncthreads();
-  plane_fft<1, 0, N0, N1>(pl, tw0);
-  plane_fft<1, 1, N0, N1>(pl, tw1);
+  plane_fft<1, 0, N0, N1, V>(pl, tw0);
+  plane_fft<1, 1, N0, N1, V>(pl, tw1);
   if constexpr ((N1 % 2) == 0) {
     float4* g4 = reinterpret_cast<float4*>(gp);
     for (int idx = tid; idx < N0 * N1 / 2; idx += kPlaneThreads) {

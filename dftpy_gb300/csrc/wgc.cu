@@ -92,24 +92,28 @@ __global__ void k_wgc_kernels(GInfo g, double tkf, double C, const double* __res
   }
 }
 
+// pointwise arithmetic in the field precision (FP32 plans stay off the FP64 pipe)
+__device__ __forceinline__ float wpow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double wpow(double x, double y) { return pow(x, y); }
+
 // transform inputs: F0 = B, F1 = u B, F2 = u^2 B (and A, u A, u^2 A)
 template <typename T>
-__global__ void k_wgc_prep(int64_t n, const T* __restrict__ rho, double rho0, double a, double b, int two,
-                           T* __restrict__ f0, T* __restrict__ f1, T* __restrict__ f2, T* __restrict__ f3,
-                           T* __restrict__ f4, T* __restrict__ f5) {
-  const double inv0 = 1.0 / rho0;
+__global__ void k_wgc_prep(int64_t n, const T* __restrict__ rho, T rho0, T a, T b, int two, T* __restrict__ f0,
+                           T* __restrict__ f1, T* __restrict__ f2, T* __restrict__ f3, T* __restrict__ f4,
+                           T* __restrict__ f5) {
+  const T inv0 = (T)1 / rho0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double rc = fmax((double)rho[i], kZeroRho);
-    const double u = (rc - rho0) * inv0;
-    const double B = pow(rc, b);
-    f0[i] = (T)B;
-    f1[i] = (T)(u * B);
-    f2[i] = (T)(u * u * B);
+    const T rc = rho[i] > (T)kZeroRho ? rho[i] : (T)kZeroRho;
+    const T u = (rc - rho0) * inv0;
+    const T B = wpow(rc, b);
+    f0[i] = B;
+    f1[i] = u * B;
+    f2[i] = u * u * B;
     if (two) {
-      const double A = pow(rc, a);
-      f3[i] = (T)A;
-      f4[i] = (T)(u * A);
-      f5[i] = (T)(u * u * A);
+      const T A = wpow(rc, a);
+      f3[i] = A;
+      f4[i] = u * A;
+      f5[i] = u * u * A;
     }
   }
 }
@@ -132,38 +136,40 @@ __global__ void k_wgc_combine(GInfo g, int ld2, const T* __restrict__ K, T scale
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __restrict__ rho, double rho0, double a,
-                                                         double b, int two, const T* __restrict__ x0,
-                                                         const T* __restrict__ x1, const T* __restrict__ x2,
-                                                         const T* __restrict__ y0, const T* __restrict__ y1,
-                                                         const T* __restrict__ y2, T* __restrict__ pot, int calc_v,
-                                                         double* __restrict__ part) {
-  const double inv0 = 1.0 / rho0;
-  KSum es;
-  es.init();
+// V added to pot and per-CTA partials of E = int A (X0 + u X1 + u^2 X2); the
+// field arithmetic runs in T, the energy sum in FP64 (per-thread sums in T,
+// combined in FP64 across threads and CTAs), and without CALC_E no FP64 at all
+template <typename T, bool WANT_E>
+__global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __restrict__ rho, T rho0, T a, T b,
+                                                         int two, const T* __restrict__ x0, const T* __restrict__ x1,
+                                                         const T* __restrict__ x2, const T* __restrict__ y0,
+                                                         const T* __restrict__ y1, const T* __restrict__ y2,
+                                                         T* __restrict__ pot, int calc_v, double* __restrict__ part) {
+  const T inv0 = (T)1 / rho0;
+  T es = (T)0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double rc = fmax((double)rho[i], kZeroRho);
-    const double u = (rc - rho0) * inv0;
-    const double A = pow(rc, a);
-    const double X0 = x0[i], X1 = x1[i], X2 = x2[i];
-    const double sx = X0 + u * X1 + u * u * X2;
-    es.add(A * sx);
+    const T rc = rho[i] > (T)kZeroRho ? rho[i] : (T)kZeroRho;
+    const T u = (rc - rho0) * inv0;
+    const T A = wpow(rc, a);
+    const T X0 = x0[i], X1 = x1[i], X2 = x2[i];
+    const T sx = X0 + u * X1 + u * u * X2;
+    if (WANT_E) es += A * sx;
     if (calc_v) {
-      double v;
+      T v;
       if (two) {
-        const double B = pow(rc, b);
-        const double Y0 = y0[i], Y1 = y1[i], Y2 = y2[i];
-        v = a * A / rc * sx + A * inv0 * (X1 + 2.0 * u * X2) + b * B / rc * (Y0 + u * Y1 + u * u * Y2) +
-            B * inv0 * (Y1 + 2.0 * u * Y2);
+        const T B = wpow(rc, b);
+        const T Y0 = y0[i], Y1 = y1[i], Y2 = y2[i];
+        v = a * A / rc * sx + A * inv0 * (X1 + (T)2 * u * X2) + b * B / rc * (Y0 + u * Y1 + u * u * Y2) +
+            B * inv0 * (Y1 + (T)2 * u * Y2);
       } else {
-        v = 2.0 * (a * A / rc * sx + A * inv0 * (X1 + 2.0 * u * X2));
+        v = (T)2 * (a * A / rc * sx + A * inv0 * (X1 + (T)2 * u * X2));
       }
-      pot[i] = (T)((double)pot[i] + v);
+      pot[i] += v;
     }
   }
+  if constexpr (!WANT_E) return;
   __shared__ double red[kThreads / 32];
-  const double v = warp_sum(es.value());
+  const double v = warp_sum((double)es);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -200,8 +206,8 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
   const int two = fabs(d->alpha - d->beta) > 1e-12;
   const int nfield = two ? 6 : 3;
   const T* r = reinterpret_cast<const T*>(rho);
-  k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, d->rho0, d->alpha, d->beta, two, (T*)W.f[0], (T*)W.f[1],
-                                              (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
+  k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],
+                                              (T*)W.f[1], (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
   GB_CHECK_LAUNCH();
   gb_count_launch();
   const int op = OP_RHO;
@@ -228,10 +234,16 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
     if (rc) return rc;
   }
   const T* y = reinterpret_cast<const T*>(two ? W.f[3] : W.f[0]);
-  k_wgc_final<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, d->rho0, d->alpha, d->beta, two, (const T*)W.f[0],
-                                               (const T*)W.f[1], (const T*)W.f[2], y,
-                                               two ? (const T*)W.f[4] : nullptr, two ? (const T*)W.f[5] : nullptr,
-                                               (T*)pot, calc_v, W.part);
+  if (calc_e)
+    k_wgc_final<T, true><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
+                                                       (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
+                                                       two ? (const T*)W.f[4] : nullptr,
+                                                       two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part);
+  else
+    k_wgc_final<T, false><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
+                                                        (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
+                                                        two ? (const T*)W.f[4] : nullptr,
+                                                        two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part);
   GB_CHECK_LAUNCH();
   gb_count_launch();
   if (calc_e) {

@@ -9,6 +9,8 @@ precision (FFT schedule, twiddle tables, workspaces).
 """
 import math
 
+import os
+
 import numpy as np
 
 from . import _lib
@@ -169,7 +171,11 @@ class DirectGrid(BaseGrid):
         import torch
         prec = _lib.F64 if dtype == torch.float64 else _lib.F32
         if prec not in self._plans:
-            self._plans[prec] = _lib.Plan(self._nrR, self.lattice, precision=prec, full=self._full)
+            plan = _lib.Plan(self._nrR, self.lattice, precision=prec, full=self._full)
+            if prec == _lib.F32 and os.environ.get("GBOFDFT_AUTOTUNE", "1") != "0":
+                from . import autotune
+                autotune.tune(plan)
+            self._plans[prec] = plan
         return self._plans[prec]
 
     def get_reciprocal(self):

@@ -456,6 +456,18 @@ int gbofdft_optimize_tn_split(gbofdft_plan* plan, const gbofdft_functional* f, g
  */
 int gbofdft_dcsrch(double* state, int64_t state_len, double* stp, double f, double g, int task);
 
+/* ---- evaluation schedules (autotuning) ----------------------------------------
+ * No reference counterpart (the reference's only FFT planning is pyFFTW's
+ * FFTW_MEASURE, math_utils.py:181-222).  Schedule 0 is the column-pass
+ * pipeline; schedules 1.. (FP32 plans whose (n0, n1) plane has a
+ * specialisation) are the plane pipeline with radix-schedule variant
+ * (schedule - 1).  All give the same result within FP32 rounding; an
+ * autotuner times them and keeps the fastest.
+ */
+int gbofdft_plan_schedules(const gbofdft_plan* plan, int* count);
+int gbofdft_plan_set_schedule(gbofdft_plan* plan, int schedule);
+int gbofdft_plan_get_schedule(const gbofdft_plan* plan, int* schedule);
+
 /* ---- learned initial guess: network kernels ----------------------------------
  * No reference counterpart (the reference's guesses are density/density.py:
  * 151-319: uniform or superposed atomic densities; the network maps those

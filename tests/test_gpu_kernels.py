@@ -339,3 +339,37 @@ def test_wgc_eval_matches_oracle(lib, prec, ab, nr, full, skew):
         if order == 0 and ab == "equal":
             e_wt, v_wt = O.WTNL()(rho, g)
             assert abs(e - e_wt) <= tol * abs(e_wt)
+
+
+def test_autotuned_schedules_agree(lib):
+    """Every evaluation schedule of a plan gives the same potential within
+    FP32 rounding; the autotuner picks one of them and remembers it."""
+    import torch
+    from dftpy_gb300 import autotune
+    nr = (64, 128, 96)
+    plan = lib.Plan(nr, _lattice(nr, True), precision=0)
+    n = autotune.schedules(plan)
+    assert n == 3      # column passes + two plane variants (a 128 axis)
+    rng = np.random.default_rng(8)
+    rho = torch.tensor(0.02 + 0.01 * rng.random(nr), dtype=torch.float32, device="cuda")
+    kern = torch.empty(nr[0], nr[1], nr[2] // 2 + 1, dtype=torch.float32, device="cuda")
+    lib.check(lib.load().gbofdft_wt_kernel(plan.handle, float(rho.mean()), 1.0, 5 / 6, 5 / 6, lib.ptr(kern),
+                                           lib.stream_ptr()))
+    f = lib.Functional()
+    f.tf, f.vw, f.xc, f.hartree, f.tf_x, f.vw_y = 1, 1, 1, 1, 1.0, 1.0
+    f.wt, f.wt_alpha, f.wt_beta, f.wt_kernel = 1, 5 / 6, 5 / 6, kern.data_ptr()
+    pots = []
+    for sc in range(n):
+        autotune.set_schedule(plan, sc)
+        assert autotune.get_schedule(plan) == sc
+        pot = torch.empty_like(rho)
+        lib.check(lib.load().gbofdft_eval(plan.handle, lib.ptr(rho), f, lib.ptr(pot), None, lib.CALC_V,
+                                          lib.stream_ptr()))
+        pots.append(pot.cpu().numpy())
+    scale = np.abs(pots[0]).max()
+    for p in pots[1:]:
+        assert np.abs(p - pots[0]).max() <= 5e-6 * scale
+    best, times = autotune.tune(plan, force=True)
+    assert 0 <= best < n and len(times) == n and autotune.get_schedule(plan) == best
+    with pytest.raises(ValueError):
+        autotune.set_schedule(plan, n)

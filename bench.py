@@ -156,10 +156,11 @@ def build_system(seed):
     return st, grid, total, rho0
 
 
-def solve(total, rho0, precision):
+def solve(total, rho0, precision, time_evals=False):
     from dftpy_gb300.optimization import Optimization
     opt = Optimization(EnergyEvaluator=total, optimization_method="TN",
-                       optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100, "precision": precision})
+                       optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100, "precision": precision,
+                                             "time_evals": time_evals})
     rho = opt.optimize_rho(guess_rho=rho0)
     return opt, rho
 
@@ -171,6 +172,7 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         solve(total, rho0, precision)
     torch.cuda.synchronize()
     times, energies, evals, glue = [], [], [], []
+    t_ev, n_ev = 0.0, 0
     l0 = _lib.launch_count()
     for _ in range(steps):
         flush.zero_()                      # 512 MB write: evicts L2 between steps
@@ -182,10 +184,13 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        opt, rho = solve(total, rho0, precision)
+        opt, rho = solve(total, rho0, precision, time_evals=True)
         e1.record(s)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1000.0)
+        for st in opt.stats["stages"]:
+            t_ev += st.get("t_eval_timed", 0.0)
+            n_ev += st.get("n_eval_timed", 0)
         energies.append(opt.energy)
         glue.append(opt.stats.get("t_glue", 0.0))
         evals.append([{"precision": st["precision"], "n_eval_ev": st["n_eval_ev"], "n_eval_v": st["n_eval_v"],
@@ -196,7 +201,7 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
                       for st in opt.stats["stages"]])
     launches = _lib.launch_count() - l0
     evals[-1].append({"python_glue_s": round(glue[-1], 4)})
-    return times, energies, evals, launches
+    return times, energies, evals, launches, (t_ev, n_ev)
 
 
 def eval_roofline(total, rho0, reps=50):
@@ -338,19 +343,22 @@ def main():
     # matches the reference-generated fixture)
     clocks = ClockSampler(local)
     clocks.start()
-    times, energies, evals, launches = timed_solves(total, rho0, args.precision, args.steps, args.warmup, flush,
-                                                    world)
+    times, energies, evals, launches, live = timed_solves(total, rho0, args.precision, args.steps, args.warmup,
+                                                          flush, world)
     clk = clocks.stop()
     plain = None
     if not args.no_plain:
-        pt, pe, pev, _ = timed_solves(total, rho0, "fp64", max(1, min(args.steps, 2)), 1, flush, world)
+        pt, pe, pev, _, _ = timed_solves(total, rho0, "fp64", max(1, min(args.steps, 2)), 1, flush, world)
         plain = {"value": statistics.mean(pt), "energy": pe[-1], "evals": pev[-1]}
     e_ref = plain["energy"] if plain else None
     if rank == 0 and e_golden is not None:
         e_ref = e_golden
     err = None if e_ref is None else max(abs(e - e_ref) for e in energies) * HA_EV / st.nat
     t_step = max_over_ranks(statistics.mean(times), world)
-    t_eval, b_eval = eval_roofline(total, rho0)
+    t_iso, b_eval = eval_roofline(total, rho0)
+    # the FP32 potential evaluations inside the timed solves (CUDA events on
+    # the solve's stream around each one); the isolated loop is reported beside
+    t_eval = live[0] / live[1] if live[1] else t_iso
     peak, peak_kind = measured_peaks()
     achieved = b_eval / t_eval / 1e9
     traffic = profile_traffic()
@@ -387,8 +395,11 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic.get("bytes_per_eval") if traffic else None,
-                     "kernel": "FP32 potential evaluation (5-kernel pipeline), 128^3",
-                     "t_eval_us": t_eval * 1e6, "algorithmic_bytes": b_eval},
+                     "kernel": "FP32 potential evaluation (rows / plane-convolution / rows pipeline, autotuned "
+                               "schedule), 128^3",
+                     "t_eval_us": t_eval * 1e6, "n_evals_timed": live[1],
+                     "timing": "CUDA events around each FP32 potential evaluation inside the timed solves",
+                     "t_eval_isolated_us": t_iso * 1e6, "algorithmic_bytes": b_eval},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

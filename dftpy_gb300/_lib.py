@@ -67,7 +67,7 @@ class TnOptions(ctypes.Structure):
                 ("maxls", ctypes.c_int), ("c1", ctypes.c_double), ("c2", ctypes.c_double),
                 ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double),
                 ("pred_stop", ctypes.c_double), ("eres", ctypes.c_double), ("cg_rtol", ctypes.c_double),
-                ("pred_next", ctypes.c_int), ("precond", ctypes.c_int)]
+                ("pred_next", ctypes.c_int), ("precond", ctypes.c_int), ("time_evals", ctypes.c_int)]
 
 
 class TnResult(ctypes.Structure):
@@ -76,7 +76,8 @@ class TnResult(ctypes.Structure):
                 ("n_iter", ctypes.c_int), ("n_eval_ev", ctypes.c_int), ("n_eval_v", ctypes.c_int),
                 ("energies", ctypes.c_double * 8), ("history", ctypes.POINTER(ctypes.c_double)),
                 ("history_cap", ctypes.c_int), ("n_history", ctypes.c_int), ("n_sync", ctypes.c_int),
-                ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double), ("n_eval_hess", ctypes.c_int)]
+                ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double), ("n_eval_hess", ctypes.c_int),
+                ("t_eval_timed", ctypes.c_double), ("n_eval_timed", ctypes.c_int)]
 
 
 _lib = None

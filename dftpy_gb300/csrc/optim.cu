@@ -159,7 +159,61 @@ struct TnState {
   const gbofdft_functional* hfn;
   void* hf[H_NF];
   bool verbose;   // GBOFDFT_TN_VERBOSE=1: per-iteration trace on stderr
+  bool time_evals;  // CUDA-event timing of the FP32 potential-only evaluations
 };
+
+// CUDA-event pairs around timed evaluations (per host thread, reused across
+// solves); completed pairs are read at the next stream synchronisation.
+struct EvTimer {
+  static constexpr int K = 64;
+  cudaEvent_t a[K], b[K];
+  bool init = false;
+  int n = 0;
+  double ms = 0.0;
+  int count = 0;
+};
+static thread_local EvTimer g_evt;
+
+static void evt_drain() {
+  for (int i = 0; i < g_evt.n; ++i) {
+    float t = 0.0f;
+    if (cudaEventSynchronize(g_evt.b[i]) == cudaSuccess && cudaEventElapsedTime(&t, g_evt.a[i], g_evt.b[i]) == cudaSuccess) {
+      g_evt.ms += t;
+      ++g_evt.count;
+    }
+  }
+  g_evt.n = 0;
+}
+
+static int evt_begin(cudaStream_t st) {
+  if (!g_evt.init) {
+    for (int i = 0; i < EvTimer::K; ++i) {
+      GB_CUDA(cudaEventCreate(&g_evt.a[i]));
+      GB_CUDA(cudaEventCreate(&g_evt.b[i]));
+    }
+    g_evt.init = true;
+  }
+  if (g_evt.n == EvTimer::K) evt_drain();
+  GB_CUDA(cudaEventRecord(g_evt.a[g_evt.n], st));
+  return 0;
+}
+
+static int evt_end(cudaStream_t st) {
+  GB_CUDA(cudaEventRecord(g_evt.b[g_evt.n], st));
+  ++g_evt.n;
+  return 0;
+}
+
+// gbofdft_eval, with the FP32 potential-only calls timed when requested
+static int tn_eval(TnState& s, gbofdft_plan* plan, const gbofdft_functional* fn, const void* rho, void* pot,
+                   double* en, int calc) {
+  const bool t = s.time_evals && plan->prec == GBOFDFT_F32 && !(calc & GBOFDFT_CALC_E);
+  int rc;
+  if (t && (rc = evt_begin(s.st))) return rc;
+  rc = gbofdft_eval(plan, rho, fn, pot, en, calc, s.st);
+  if (!rc && t) rc = evt_end(s.st);
+  return rc;
+}
 
 static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -171,13 +225,14 @@ static int ts_sync(TnState& s) {
   GB_CUDA(cudaStreamSynchronize(s.st));
   s.t_sync += now_s() - t0;
   ++s.n_sync;
+  if (s.time_evals) evt_drain();
   return 0;
 }
 
 static int ts_eval(TnState& s, const void* rho, void* pot, bool want_e) {
   if (want_e) ++s.n_ev; else ++s.n_v;
-  return gbofdft_eval(s.p, rho, s.fn, pot, want_e ? s.w.sc + S_EN : nullptr,
-                      GBOFDFT_CALC_V | (want_e ? GBOFDFT_CALC_E : 0), s.st);
+  return tn_eval(s, s.p, s.fn, rho, pot, want_e ? s.w.sc + S_EN : nullptr,
+                 GBOFDFT_CALC_V | (want_e ? GBOFDFT_CALC_E : 0));
 }
 
 template <typename T>
@@ -225,7 +280,7 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     }, S_A, st);
     if (rc) return rc;
     ++s.n_hv;
-    if ((rc = gbofdft_eval(plan, rho1, fn, d.pot1, nullptr, GBOFDFT_CALC_V, st))) return rc;
+    if ((rc = tn_eval(s, plan, fn, rho1, d.pot1, nullptr, GBOFDFT_CALC_V))) return rc;
     TH* pot1 = d.pot1;
     rc = launch_mr<0, TH>(w, N, [=] __device__(int64_t i, TH* c) { rb[i] = (pot1[i] - muH) * ph[i]; }, S_A, st);
     if (rc) return rc;
@@ -298,7 +353,7 @@ static int tn_direction(TnState& s, gbofdft_plan* plan, const gbofdft_functional
     if (rc) return rc;
     TH* pot1 = d.pot1;
     if (split) ++s.n_hv; else ++s.n_v;
-    if ((rc = gbofdft_eval(plan, rho1, fn, pot1, nullptr, GBOFDFT_CALC_V, st))) return rc;
+    if ((rc = tn_eval(s, plan, fn, rho1, pot1, nullptr, GBOFDFT_CALC_V))) return rc;
     TH* ap = d.ap;
     const TH inv_e = (TH)(1.0 / epsi);
     double* scw = w.sc;
@@ -641,6 +696,11 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   res->n_sync = s.n_sync;
   res->t_sync = s.t_sync;
   res->t_total = now_s() - s.t_start;
+  if (s.time_evals) {
+    evt_drain();
+    res->t_eval_timed = g_evt.ms * 1e-3;
+    res->n_eval_timed = g_evt.count;
+  }
   for (int k = 0; k < GBOFDFT_NE; ++k) res->energies[k] = s.host[S_EN + k];
   return 0;
 }
@@ -671,6 +731,7 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->cg_rtol = 0.1;
   o->pred_next = 0;
   o->precond = 0;
+  o->time_evals = 0;
   return GBOFDFT_OK;
 }
 
@@ -723,6 +784,14 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
   {
     const char* v = getenv("GBOFDFT_TN_VERBOSE");
     s.verbose = v && v[0] == '1';
+  }
+  s.time_evals = o->time_evals != 0;
+  res->t_eval_timed = 0.0;
+  res->n_eval_timed = 0;
+  if (s.time_evals) {
+    g_evt.n = 0;
+    g_evt.ms = 0.0;
+    g_evt.count = 0;
   }
   const size_t fb = ((gb_elem(p) * (size_t)p->N + 255) / 256) * 256;
   char* base = reinterpret_cast<char*>(workspace);

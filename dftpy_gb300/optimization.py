@@ -68,6 +68,9 @@ DEFAULTS = {
     "refine_cg_rtol": 0.01,
     # preconditioned inner CG in the stages of "mixed" (uniform-gas Hessian)
     "mixed_precond": True,
+    # CUDA-event timing of the FP32 potential-only evaluations (stats
+    # t_eval_timed / n_eval_timed per stage)
+    "time_evals": False,
 }
 
 
@@ -122,6 +125,7 @@ class Optimization:
         opts.cg_rtol = float(cg_rtol)
         opts.pred_next = int(bool(pred_next))
         opts.precond = int(bool(precond))
+        opts.time_evals = int(bool(o.get("time_evals", False)))
         spec = self.EnergyEvaluator.spec(rho)
         f = spec.ctypes()
         nb = ctypes.c_int64()
@@ -149,7 +153,8 @@ class Optimization:
         out = dict(energy=res.energy, mu=res.mu, converged=res.converged, n_iter=res.n_iter,
                    n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, n_eval_hess=res.n_eval_hess,
                    energies=list(res.energies), history=[hist[i] for i in range(res.n_history)],
-                   n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total)
+                   n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total,
+                   t_eval_timed=res.t_eval_timed, n_eval_timed=res.n_eval_timed)
         return DirectField(grid, data=r), out
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):

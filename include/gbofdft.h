@@ -392,6 +392,8 @@ typedef struct gbofdft_tn_options {
                        Hessian of the uniform electron gas at the mean density
                        (Lindhard kinetic + Hartree curvature, applied by FFT);
                        no reference counterpart.  0: the reference's plain CG */
+  int time_evals;   /* 1: time the FP32 potential-only evaluations with CUDA
+                       events (result t_eval_timed / n_eval_timed); 0: off */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {
@@ -409,6 +411,8 @@ typedef struct gbofdft_tn_result {
   double t_sync;          /* host seconds spent waiting in them (scalar read-backs) */
   double t_total;         /* host seconds in gbofdft_optimize_tn */
   int n_eval_hess;        /* potential evaluations in the Hessian plan (split mode) */
+  double t_eval_timed;    /* with time_evals: device seconds of the timed evaluations */
+  int n_eval_timed;       /* ... and their number */
 } gbofdft_tn_result;
 
 int gbofdft_tn_options_default(gbofdft_tn_options* opts);

@@ -87,10 +87,23 @@ __device__ __forceinline__ int paddr(int i0, int i1) {
   return sw<float, Pad<float, N1>::NP>(i0, i1);
 }
 
+// Stage modes: in place in shared memory, inputs read straight from the
+// plane in global memory (the first stage of the first transform), or
+// outputs written straight to global memory (the last stage of the last
+// transform) -- each saves one pass over the shared plane.
+enum { PS_SMEM = 0, PS_FROM_GLOBAL = 1, PS_TO_GLOBAL = 2 };
+
+struct PsIdentity {
+  __device__ __forceinline__ float2 operator()(int, int, float2 v) const { return v; }
+};
+
 // One in-place Stockham stage (radix R, stride P) of every line along axis
 // AX (1: lines are rows i0, elements i1; 0: lines are columns i1, elements i0).
-template <int DIR, int AX, int N0, int N1, int R, int P>
-__device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __restrict__ tw) {
+// outf(j, l, v) is applied to every output (element j of line l) before it
+// is stored.
+template <int DIR, int AX, int N0, int N1, int R, int P, int MODE, typename OUTF>
+__device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __restrict__ tw,
+                                       const float2* __restrict__ gsrc, float2* __restrict__ gdst, OUTF outf) {
   constexpr int N = AX == 1 ? N1 : N0;
   constexpr int NL = AX == 1 ? N0 : N1;
   constexpr int NB = N / R;
@@ -100,6 +113,7 @@ __device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __
   constexpr int LC = NL / CH;
   constexpr int PER = LC * NB;
   constexpr int IT = (PER + NT - 1) / NT;
+  static_assert(MODE == PS_SMEM || AX == 1, "global operands are rows of the plane");
   const int tid = threadIdx.x;
 #pragma unroll 1
   for (int c0 = 0; c0 < NL; c0 += LC) {
@@ -117,7 +131,9 @@ __device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __
 #pragma unroll
       for (int t = 0; t < R; ++t) {
         const int j = i + t * NB;
-        float2 v = AX == 1 ? pl[paddr<N1>(l, j)] : pl[paddr<N1>(j, l)];
+        float2 v;
+        if constexpr (MODE == PS_FROM_GLOBAL) v = gsrc[l * N1 + j];
+        else v = AX == 1 ? pl[paddr<N1>(l, j)] : pl[paddr<N1>(j, l)];
         if (P > 1 && t > 0) {
           const float2 w = tw[t * k * TWS];
           v = DIR < 0 ? c_mul(v, w) : c_mulc(v, w);
@@ -128,36 +144,50 @@ __device__ __forceinline__ void pstage(float2* __restrict__ pl, const float2* __
       lo[it] = l;
       jo[it] = (i - k) * R + k;
     }
-    __syncthreads();
+    if constexpr (MODE == PS_SMEM) __syncthreads();
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
       if (lo[it] < 0) continue;
 #pragma unroll
       for (int t = 0; t < R; ++t) {
         const int j = jo[it] + t * P;
-        if constexpr (AX == 1) pl[paddr<N1>(lo[it], j)] = u[it][t];
-        else pl[paddr<N1>(j, lo[it])] = u[it][t];
+        const float2 v = outf(j, lo[it], u[it][t]);
+        if constexpr (MODE == PS_TO_GLOBAL) gdst[lo[it] * N1 + j] = v;
+        else if constexpr (AX == 1) pl[paddr<N1>(lo[it], j)] = v;
+        else pl[paddr<N1>(j, lo[it])] = v;
       }
     }
-    __syncthreads();
+  }
+  if constexpr (MODE != PS_TO_GLOBAL) __syncthreads();
+}
+
+template <int DIR, int AX, int N0, int N1, int P, int FIRST, int LAST, typename OUTF, int R0, int... Rs>
+__device__ __forceinline__ void prun(float2* pl, const float2* tw, const float2* gsrc, float2* gdst, OUTF outf) {
+  constexpr bool last = sizeof...(Rs) == 0;
+  constexpr int mode = (P == 1 && FIRST == PS_FROM_GLOBAL) ? PS_FROM_GLOBAL : (last ? LAST : PS_SMEM);
+  static_assert(!(P == 1 && last && FIRST != PS_SMEM && LAST != PS_SMEM), "single-stage schedule");
+  if constexpr (last) {
+    pstage<DIR, AX, N0, N1, R0, P, mode>(pl, tw, gsrc, gdst, outf);
+  } else {
+    pstage<DIR, AX, N0, N1, R0, P, mode>(pl, tw, gsrc, gdst, PsIdentity{});
+    prun<DIR, AX, N0, N1, P * R0, FIRST, LAST, OUTF, Rs...>(pl, tw, gsrc, gdst, outf);
   }
 }
 
-template <int DIR, int AX, int N0, int N1, int P, int R0, int... Rs>
-__device__ __forceinline__ void prun(float2* pl, const float2* tw) {
-  pstage<DIR, AX, N0, N1, R0, P>(pl, tw);
-  if constexpr (sizeof...(Rs) > 0) prun<DIR, AX, N0, N1, P * R0, Rs...>(pl, tw);
+template <int DIR, int AX, int N0, int N1, int FIRST, int LAST, typename OUTF, int... Rs>
+__device__ __forceinline__ void prun_sched(Sched<Rs...>, float2* pl, const float2* tw, const float2* gsrc,
+                                           float2* gdst, OUTF outf) {
+  prun<DIR, AX, N0, N1, 1, FIRST, LAST, OUTF, Rs...>(pl, tw, gsrc, gdst, outf);
 }
 
-template <int DIR, int AX, int N0, int N1, int... Rs>
-__device__ __forceinline__ void prun_sched(Sched<Rs...>, float2* pl, const float2* tw) {
-  prun<DIR, AX, N0, N1, 1, Rs...>(pl, tw);
-}
-
-// whole-plane 1-D transforms along one axis
-template <int DIR, int AX, int N0, int N1, int V>
-__device__ __forceinline__ void plane_fft(float2* pl, const float2* tw) {
-  prun_sched<DIR, AX, N0, N1>(typename PlaneSched<AX == 1 ? N1 : N0, V>::S{}, pl, tw);
+// whole-plane 1-D transforms along one axis; FIRST / LAST select where the
+// first stage reads and the last stage writes, outf post-processes the last
+// stage's outputs
+template <int DIR, int AX, int N0, int N1, int V, int FIRST = PS_SMEM, int LAST = PS_SMEM,
+          typename OUTF = PsIdentity>
+__device__ __forceinline__ void plane_fft(float2* pl, const float2* tw, const float2* gsrc = nullptr,
+                                          float2* gdst = nullptr, OUTF outf = OUTF{}) {
+  prun_sched<DIR, AX, N0, N1, FIRST, LAST>(typename PlaneSched<AX == 1 ? N1 : N0, V>::S{}, pl, tw, gsrc, gdst, outf);
 }
 
 struct PlaneArgs {
@@ -197,32 +227,6 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
     }
     cp_async_commit();
   }
-  // the plane (contiguous), as float4 pairs when the row length allows;
-  // batches of loads are issued before their shared-memory stores
-  if constexpr ((N1 % 2) == 0) {
-    constexpr int NV = N0 * N1 / 2, UNR = 4096 / kPlaneThreads;
-    const float4* g4 = reinterpret_cast<const float4*>(gp);
-#pragma unroll 1
-    for (int base = 0; base < NV; base += UNR * kPlaneThreads) {
-      float4 v[UNR];
-#pragma unroll
-      for (int u = 0; u < UNR; ++u) {
-        const int idx = base + u * kPlaneThreads + tid;
-        if (idx < NV) v[u] = g4[idx];
-      }
-#pragma unroll
-      for (int u = 0; u < UNR; ++u) {
-        const int idx = base + u * kPlaneThreads + tid;
-        if (idx < NV) {
-          const int e = 2 * idx, i0 = e / N1, i1 = e % N1;
-          pl[paddr<N1>(i0, i1)] = make_float2(v[u].x, v[u].y);
-          pl[paddr<N1>(i0, i1 + 1)] = make_float2(v[u].z, v[u].w);
-        }
-      }
-    }
-  } else {
-    for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) pl[paddr<N1>(idx / N1, idx % N1)] = gp[idx];
-  }
   const float2* t0 = reinterpret_cast<const float2*>(a.tw0);
   const float2* t1 = reinterpret_cast<const float2*>(a.tw1);
   for (int i = tid; i < N0; i += kPlaneThreads) tw0[i] = t0[i];
@@ -241,10 +245,11 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
     gB[2 * N1 + i] = m1 * a.bgf[5];
   }
   __syncthreads();
-  plane_fft<-1, 1, N0, N1, V>(pl, tw1);
-  plane_fft<-1, 0, N0, N1, V>(pl, tw0);
-  // kernel multiply; points on a Nyquist line of a symmetrised plane take
-  // the partner-averaged general path (as the column passes do)
+  // forward along axis 1, its first stage reading the plane from global memory
+  plane_fft<-1, 1, N0, N1, V, PS_FROM_GLOBAL>(pl, tw1, gp);
+  // forward along axis 0 with the kernel multiply fused into its last stage;
+  // points on a Nyquist line of a symmetrised plane take the partner-averaged
+  // general path (as the column passes do)
   const bool plane_sym = g.full || k2 == 0 || ((g.n2 & 1) == 0 && 2 * k2 == g.n2);
   const bool nyq2 = g.full && (g.n2 & 1) == 0 && 2 * k2 == g.n2;
   const float coef = a.coef[f];
@@ -253,11 +258,10 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
     cp_async_wait_all();
     __syncthreads();
   }
-  for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) {
-    const int i0 = idx / N1, i1 = idx % N1;
+  auto kmul = [&](int i0, int i1, float2 v) {
     float kv;
     if (type == KER_ARRAY) {
-      kv = (Cfg::table_smem ? ktab[idx] : __ldg(karr + idx)) * coef;
+      kv = (Cfg::table_smem ? ktab[i0 * N1 + i1] : __ldg(karr + i0 * N1 + i1)) * coef;
     } else {
       const bool special = plane_sym && (nyq2 || ((N0 & 1) == 0 && 2 * i0 == N0) || ((N1 & 1) == 0 && 2 * i1 == N1));
       if (special) {
@@ -268,22 +272,12 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
         kv = type == KER_HARTREE ? (gg > 0.0f ? fourpi_c / gg : 0.0f) : (type == KER_G2 ? gg * coef : coef);
       }
     }
-    const int p = paddr<N1>(i0, i1);
-    pl[p] = c_scale(pl[p], kv);
-  }
-  __syncthreads();
+    return c_scale(v, kv);
+  };
+  plane_fft<-1, 0, N0, N1, V, PS_SMEM, PS_SMEM>(pl, tw0, nullptr, nullptr, kmul);
   plane_fft<1, 0, N0, N1, V>(pl, tw0);
-  plane_fft<1, 1, N0, N1, V>(pl, tw1);
-  if constexpr ((N1 % 2) == 0) {
-    float4* g4 = reinterpret_cast<float4*>(gp);
-    for (int idx = tid; idx < N0 * N1 / 2; idx += kPlaneThreads) {
-      const int e = 2 * idx, i0 = e / N1, i1 = e % N1;
-      const float2 v0 = pl[paddr<N1>(i0, i1)], v1 = pl[paddr<N1>(i0, i1 + 1)];
-      g4[idx] = make_float4(v0.x, v0.y, v1.x, v1.y);
-    }
-  } else {
-    for (int idx = tid; idx < N0 * N1; idx += kPlaneThreads) gp[idx] = pl[paddr<N1>(idx / N1, idx % N1)];
-  }
+  // inverse along axis 1, its last stage writing the plane to global memory
+  plane_fft<1, 1, N0, N1, V, PS_SMEM, PS_TO_GLOBAL>(pl, tw1, nullptr, gp);
 }
 
 // plane sizes with a specialisation (the workloads' grids)

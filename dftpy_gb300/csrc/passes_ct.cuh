@@ -42,6 +42,9 @@ __host__ inline bool ct_dispatch(int n, F&& f) {
 #ifndef GB_CT_COLS_MINB
 #define GB_CT_COLS_MINB 1
 #endif
+#ifndef GB_CT_PF_F32
+#define GB_CT_PF_F32 4      // density / v_loc values prefetched per thread in the FP32 evaluation epilogue (measured best)
+#endif
 #ifndef GB_CT_CONV_MINB
 #define GB_CT_CONV_MINB 5   // FP32 convolution pass, N <= 128: >= 5 CTAs/SM (measured best at 128^3; no spills)
 #endif
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   const T* vlocp = reinterpret_cast<const T*>(a.vloc);
   // the density and v_loc of this thread's first PF elements, loaded before
   // the transforms so their latency is hidden behind them
-  constexpr int PF = sizeof(T) == 4 ? 8 : 4;
+  constexpr int PF = sizeof(T) == 4 ? GB_CT_PF_F32 : 4;
   T pre_rho[PF], pre_vl[PF];
 #pragma unroll
   for (int m = 0; m < PF; ++m) {

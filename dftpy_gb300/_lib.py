@@ -67,7 +67,8 @@ class TnOptions(ctypes.Structure):
                 ("maxls", ctypes.c_int), ("c1", ctypes.c_double), ("c2", ctypes.c_double),
                 ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double),
                 ("pred_stop", ctypes.c_double), ("eres", ctypes.c_double), ("cg_rtol", ctypes.c_double),
-                ("pred_next", ctypes.c_int), ("precond", ctypes.c_int), ("time_evals", ctypes.c_int)]
+                ("pred_next", ctypes.c_int), ("precond", ctypes.c_int), ("time_evals", ctypes.c_int),
+                ("delta", ctypes.c_void_p), ("delta_rtol", ctypes.c_double)]
 
 
 class TnResult(ctypes.Structure):
@@ -77,7 +78,7 @@ class TnResult(ctypes.Structure):
                 ("energies", ctypes.c_double * 8), ("history", ctypes.POINTER(ctypes.c_double)),
                 ("history_cap", ctypes.c_int), ("n_history", ctypes.c_int), ("n_sync", ctypes.c_int),
                 ("t_sync", ctypes.c_double), ("t_total", ctypes.c_double), ("n_eval_hess", ctypes.c_int),
-                ("t_eval_timed", ctypes.c_double), ("n_eval_timed", ctypes.c_int)]
+                ("t_eval_timed", ctypes.c_double), ("n_eval_timed", ctypes.c_int), ("n_eval_delta", ctypes.c_int)]
 
 
 _lib = None
@@ -99,6 +100,10 @@ _SIGS = [
                                                 ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P,
                                                 ctypes.c_double, _P]),
     ("gbofdft_eval", ctypes.c_int, [_P, _P, ctypes.POINTER(Functional), _P, _P, ctypes.c_int, _P]),
+    ("gbofdft_delta_create", ctypes.c_int, [_P, _P, ctypes.POINTER(_P)]),
+    ("gbofdft_delta_destroy", ctypes.c_int, [_P]),
+    ("gbofdft_eval_delta", ctypes.c_int, [_P, _P, ctypes.POINTER(Functional), ctypes.POINTER(Functional), _P, _P,
+                                          ctypes.c_int, ctypes.c_int, _P]),
     ("gbofdft_wt_kernel", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _P, _P]),
     ("gbofdft_lwt_workspace_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
@@ -268,6 +273,28 @@ class Plan:
         if h is not None and _lib is not None:
             try:
                 _lib.gbofdft_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+class Delta:
+    """Delta-evaluation state (``gbofdft_delta``) of an FP64 plan and an FP32
+    plan on the same grid: the reference density and its FP64 convolution
+    results."""
+
+    def __init__(self, plan64, plan32):
+        L = load()
+        h = ctypes.c_void_p()
+        check(L.gbofdft_delta_create(plan64.handle, plan32.handle, ctypes.byref(h)), "delta_create")
+        self.handle = h
+        self._plans = (plan64, plan32)   # the state refers to both plans
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and _lib is not None:
+            try:
+                _lib.gbofdft_delta_destroy(h)
             except Exception:
                 pass
             self.handle = None

@@ -266,21 +266,18 @@ int gbofdft_convolve(gbofdft_plan* p, const void* in, void* out, int kernel, con
   return rc;
 }
 
-int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
-                 int calc, void* stream) {
-  GB_REQUIRE(p && rho && f && pot, "eval: null argument");
-  GB_REQUIRE(!(calc & GBOFDFT_CALC_E) || energies, "eval: energies buffer required with CALC_E");
+}  // extern "C"
+
+// Evaluation descriptors of a functional: the fused terms' epilogue flags and
+// constants, the convolution fields (prologue op, kernel) in slot order.
+static int eval_descs(const gbofdft_functional* f, EvalDesc& ev, KerDesc& kd, int* ops, int& nf) {
   GB_REQUIRE(!f->wt || f->wt_kernel, "eval: WT enabled without a kernel table");
   GB_REQUIRE(!f->wt || fabs(f->wt_alpha - f->wt_beta) < 1e-9,
              "eval: fused WT path requires alpha == beta (got %g, %g)", f->wt_alpha, f->wt_beta);
   GB_REQUIRE(f->xc == 0 || f->xc == 1, "eval: unsupported xc %d", f->xc);
-  cudaStream_t st = (cudaStream_t)stream;
-  EvalDesc ev;
   memset(&ev, 0, sizeof(ev));
-  KerDesc kd;
   memset(&kd, 0, sizeof(kd));
-  int ops[GB_MAX_FIELDS];
-  int nf = 0;
+  nf = 0;
   ev.tf = f->tf; ev.tf_x = f->tf_x;
   ev.vw = f->vw; ev.vw_y = f->vw_y;
   ev.wt = f->wt; ev.wt_alpha = f->wt_alpha; ev.wt_beta = f->wt_beta;
@@ -291,19 +288,45 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
     ev.slot_wt = nf; ops[nf] = OP_POWB; kd.type[nf] = KER_ARRAY; kd.arr[nf] = f->wt_kernel; kd.coef[nf] = 1.0;
     ++nf;
   }
+  return 0;
+}
+
+// the nonlocal terms evaluated outside the fused passes (added to pot / energies)
+static int eval_extra(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
+                      int calc, cudaStream_t st) {
+  int rc = 0;
+  if (f->lwt)
+    rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
+                     st);
+  if (!rc && f->wgc)
+    rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
+                     st);
+  return rc;
+}
+
+// gbofdft_eval; cout != nullptr (FP64 compile-time-size passes) also stores
+// the convolution results, field slot f at cout + f * N
+static int eval_impl(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
+                     int calc, void* cout, cudaStream_t st) {
+  GB_REQUIRE(p && rho && f && pot, "eval: null argument");
+  GB_REQUIRE(!(calc & GBOFDFT_CALC_E) || energies, "eval: energies buffer required with CALC_E");
+  EvalDesc ev;
+  KerDesc kd;
+  int ops[GB_MAX_FIELDS];
+  int nf = 0;
+  int rc = eval_descs(f, ev, kd, ops, nf);
+  if (rc) return rc;
+  ev.cout = cout;
+  ev.cstride = p->N;
   const int64_t fs = p->NGld;
-  int rc = gb_eval_plane(p, rho, nf, ops, f->wt_beta, kd, ev, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies,
-                         st);
-  if (rc == 0) {
-    if (f->lwt)
-      rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0,
-                       (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
-    if (!rc && f->wgc)
-      rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0,
-                       (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
-    return rc;
+  if (!cout) {
+    rc = gb_eval_plane(p, rho, nf, ops, f->wt_beta, kd, ev, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies,
+                       st);
+    if (rc == 0) return eval_extra(p, rho, f, pot, energies, calc, st);
+    if (rc != 1) return rc;
+  } else {
+    GB_REQUIRE(p->prec == GBOFDFT_F64 && gb_use_ct(), "eval: convolution output needs the FP64 specialised passes");
   }
-  if (rc != 1) return rc;
   rc = 0;
   if (nf > 0) {
     rc = gb_rows_fwd(p, rho, p->spec, fs, p->ld2, nf, ops, f->wt_beta, 1.0, st);
@@ -313,12 +336,102 @@ int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, 
   }
   if (!rc)
     rc = gb_rows_inv_eval(p, p->spec, fs, nf, ev, rho, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
-  if (!rc && f->lwt)
-    rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
-                     st);
-  if (!rc && f->wgc)
-    rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
-                     st);
+  if (!rc) rc = eval_extra(p, rho, f, pot, energies, calc, st);
+  return rc;
+}
+
+// Delta-evaluation state: the reference density and its FP64 convolution
+// results, on the FP64 plan's grid.
+struct gbofdft_delta {
+  gbofdft_plan* p64;
+  gbofdft_plan* p32;
+  double* buf;      // rho_ref [N], then C_ref [GB_MAX_FIELDS][N]
+  int valid;
+  int nf;
+  int ops[GB_MAX_FIELDS];
+  int kind[GB_MAX_FIELDS];
+};
+
+const double* gb_delta_ref(const gbofdft_delta* d) { return d->buf; }
+
+extern "C" {
+
+int gbofdft_eval(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
+                 int calc, void* stream) {
+  return eval_impl(p, rho, f, pot, energies, calc, nullptr, (cudaStream_t)stream);
+}
+
+int gbofdft_delta_create(gbofdft_plan* plan, gbofdft_plan* hplan, gbofdft_delta** out) {
+  GB_REQUIRE(plan && hplan && out, "delta_create: null argument");
+  *out = nullptr;
+  GB_REQUIRE(plan->prec == GBOFDFT_F64 && hplan->prec == GBOFDFT_F32,
+             "delta_create: needs an FP64 plan and an FP32 plan");
+  GB_REQUIRE(plan->n[0] == hplan->n[0] && plan->n[1] == hplan->n[1] && plan->n[2] == hplan->n[2] &&
+                 plan->full == hplan->full,
+             "delta_create: the plans are on different grids");
+  GB_REQUIRE(hplan->plane_ok && gb_delta_supported(plan->n[0], plan->n[1], plan->n[2]),
+             "delta_create: grid %d x %d x %d has no plane-pipeline specialisation", plan->n[0], plan->n[1],
+             plan->n[2]);
+  gbofdft_delta* d = new gbofdft_delta;
+  memset(d, 0, sizeof(*d));
+  d->p64 = plan;
+  d->p32 = hplan;
+  cudaError_t e = cudaMalloc(&d->buf, sizeof(double) * (size_t)plan->N * (1 + GB_MAX_FIELDS));
+  if (e != cudaSuccess) {
+    delete d;
+    return gb_set_error(GBOFDFT_ERR_ALLOC, "delta_create: %s", cudaGetErrorString(e));
+  }
+  *out = d;
+  return 0;
+}
+
+int gbofdft_delta_destroy(gbofdft_delta* d) {
+  if (!d) return 0;
+  if (d->buf) cudaFree(d->buf);
+  delete d;
+  return 0;
+}
+
+int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_functional* f,
+                       const gbofdft_functional* hf, void* pot, double* energies, int calc, int rebase,
+                       void* stream) {
+  GB_REQUIRE(d && rho && f && pot, "eval_delta: null argument");
+  GB_REQUIRE(!(calc & GBOFDFT_CALC_E) || energies, "eval_delta: energies buffer required with CALC_E");
+  cudaStream_t st = (cudaStream_t)stream;
+  EvalDesc ev;
+  KerDesc kd;
+  int ops[GB_MAX_FIELDS];
+  int nf = 0;
+  int rc = eval_descs(f, ev, kd, ops, nf);
+  if (rc) return rc;
+  const int64_t N = d->p64->N;
+  double* rho_ref = d->buf;
+  double* cref = d->buf + N;
+  if (rebase || nf == 0) {
+    rc = eval_impl(d->p64, rho, f, pot, energies, calc, nf > 0 ? cref : nullptr, st);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(rho_ref, rho, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, st));
+    d->valid = 1;
+    d->nf = nf;
+    for (int i = 0; i < GB_MAX_FIELDS; ++i) {
+      d->ops[i] = i < nf ? ops[i] : -1;
+      d->kind[i] = i < nf ? kd.type[i] : -1;
+    }
+    return 0;
+  }
+  GB_REQUIRE(d->valid, "eval_delta: no reference evaluation yet (call with rebase = 1 first)");
+  GB_REQUIRE(d->nf == nf, "eval_delta: functional terms differ from the reference evaluation's");
+  for (int i = 0; i < nf; ++i)
+    GB_REQUIRE(d->ops[i] == ops[i] && d->kind[i] == kd.type[i],
+               "eval_delta: functional terms differ from the reference evaluation's");
+  if (f->wt) {
+    GB_REQUIRE(hf && hf->wt && hf->wt_kernel, "eval_delta: WT needs the FP32 functional's kernel table");
+    kd.arr[ev.slot_wt] = hf->wt_kernel;
+  }
+  rc = gb_eval_delta_core(d->p64, d->p32, reinterpret_cast<const double*>(rho), rho_ref, cref, nf, ops, f->wt_beta,
+                          kd, ev, reinterpret_cast<const double*>(f->vloc), reinterpret_cast<double*>(pot),
+                          (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
+  if (!rc) rc = eval_extra(d->p64, rho, f, pot, energies, calc, st);
   return rc;
 }
 

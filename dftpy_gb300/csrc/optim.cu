@@ -33,6 +33,7 @@ enum {
   S_RZ = 14, S_RZN = 15,                // preconditioned CG: r.z (current, new)
   S_BETA = 24,                          // preconditioned CG: beta in the loop precision
   S_EN = 16,                            // energies (GB_NE)
+  S_DR = 28,                            // delta evaluation: ||rho - rho_ref||^2, ||rho_ref||^2
   S_COUNT = 64
 };
 
@@ -160,6 +161,12 @@ struct TnState {
   void* hf[H_NF];
   bool verbose;   // GBOFDFT_TN_VERBOSE=1: per-iteration trace on stderr
   bool time_evals;  // CUDA-event timing of the FP32 potential-only evaluations
+  // delta evaluations of the FP64 functional (split mode): state, rebase
+  // threshold, whether this solve has made a reference yet
+  gbofdft_delta* delta;
+  double delta_rtol;
+  bool delta_ref;
+  int n_delta;
 };
 
 // CUDA-event pairs around timed evaluations (per host thread, reused across
@@ -231,8 +238,27 @@ static int ts_sync(TnState& s) {
 
 static int ts_eval(TnState& s, const void* rho, void* pot, bool want_e) {
   if (want_e) ++s.n_ev; else ++s.n_v;
-  return tn_eval(s, s.p, s.fn, rho, pot, want_e ? s.w.sc + S_EN : nullptr,
-                 GBOFDFT_CALC_V | (want_e ? GBOFDFT_CALC_E : 0));
+  double* en = want_e ? s.w.sc + S_EN : nullptr;
+  const int calc = GBOFDFT_CALC_V | (want_e ? GBOFDFT_CALC_E : 0);
+  if (!s.delta) return tn_eval(s, s.p, s.fn, rho, pot, en, calc);
+  // delta evaluation against the solve's reference density unless rho has
+  // moved more than delta_rtol from it (then a full evaluation rebases)
+  bool rebase = !s.delta_ref;
+  if (!rebase) {
+    const double* r = reinterpret_cast<const double*>(rho);
+    const double* r0 = gb_delta_ref(s.delta);
+    int rc = launch_mr<2, double>(s.w, s.p->N, [=] __device__(int64_t i, double* c) {
+      const double d = r[i] - r0[i];
+      c[0] = d * d;
+      c[1] = r0[i] * r0[i];
+    }, S_DR, s.st);
+    if (rc || (rc = ts_sync(s))) return rc;
+    rebase = !(s.host[S_DR] <= s.delta_rtol * s.delta_rtol * s.host[S_DR + 1]);
+  }
+  if (!rebase) ++s.n_delta;
+  const int rc = gbofdft_eval_delta(s.delta, rho, s.fn, s.hfn, pot, en, calc, rebase ? 1 : 0, s.st);
+  if (!rc) s.delta_ref = true;
+  return rc;
 }
 
 template <typename T>
@@ -701,6 +727,7 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     res->t_eval_timed = g_evt.ms * 1e-3;
     res->n_eval_timed = g_evt.count;
   }
+  res->n_eval_delta = s.n_delta;
   for (int k = 0; k < GBOFDFT_NE; ++k) res->energies[k] = s.host[S_EN + k];
   return 0;
 }
@@ -732,6 +759,8 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->pred_next = 0;
   o->precond = 0;
   o->time_evals = 0;
+  o->delta = nullptr;
+  o->delta_rtol = 1e-3;
   return GBOFDFT_OK;
 }
 
@@ -766,6 +795,8 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
                (long long)hworkspace_bytes, (long long)hneed);
     GB_REQUIRE(((uintptr_t)hworkspace & 255) == 0, "optimize_tn_split: Hessian workspace must be 256-byte aligned");
   }
+  GB_REQUIRE(!o->delta || hp, "optimize_tn: delta evaluation needs the split mode (an FP32 Hessian plan)");
+  GB_REQUIRE(!o->delta || o->delta_rtol > 0.0, "optimize_tn: delta_rtol must be > 0");
   GB_REQUIRE(o->pred_stop >= 0.0, "optimize_tn: pred_stop must be >= 0");
   GB_REQUIRE(o->cg_rtol > 0.0 && o->cg_rtol < 1.0, "optimize_tn: cg_rtol must be in (0, 1)");
   int64_t need = 0;
@@ -788,6 +819,7 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
   s.time_evals = o->time_evals != 0;
   res->t_eval_timed = 0.0;
   res->n_eval_timed = 0;
+  res->n_eval_delta = 0;
   if (s.time_evals) {
     g_evt.n = 0;
     g_evt.ms = 0.0;
@@ -807,6 +839,8 @@ int gbofdft_optimize_tn_split(gbofdft_plan* p, const gbofdft_functional* f, gbof
     const size_t hb = ((gb_elem(hp) * (size_t)hp->N + 255) / 256) * 256;
     char* hbase = reinterpret_cast<char*>(hworkspace);
     for (int i = 0; i < H_NF; ++i) s.hf[i] = hbase + hb * i;
+    s.delta = o->delta;
+    s.delta_rtol = o->delta_rtol;
   }
   return p->prec == GBOFDFT_F64 ? tn_run<double>(s, rho_io, *o, res) : tn_run<float>(s, rho_io, *o, res);
 }

@@ -681,6 +681,35 @@ int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, doub
   return 0;
 }
 
+int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
+                       const double* cref, int nf, const int* ops, double beta, const KerDesc& kd,
+                       const EvalDesc& ev, const double* vloc, double* pot, int calc_e, double* energies,
+                       cudaStream_t st) {
+  GB_REQUIRE(p32->plane_ok && p32->prec == GBOFDFT_F32 && nf > 0 && gb_use_ct(),
+             "delta evaluation: needs an FP32 plan with the plane pipeline");
+  const float* pm_arr[GB_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
+  for (int f = 0; f < nf; ++f) {
+    if (kd.type[f] != KER_ARRAY) continue;
+    GB_REQUIRE(p32->wt_pm && kd.arr[f] == p32->wt_pm_src,
+               "delta evaluation: the FP32 kernel table was not built on the FP32 plan");
+    pm_arr[f] = p32->wt_pm;
+  }
+  const int64_t fs = p32->NG;
+  int rc = gb_delta_rows_fwd(p32, rho, rho_ref, p32->spec, fs, nf, ops, beta, st);
+  if (!rc) rc = gb_plane_conv_f32(p32, p32->spec, fs, nf, &kd, pm_arr, 1.0 / (double)p32->N, st);
+  if (rc) return rc == 1 ? gb_set_error(GBOFDFT_ERR_STATE, "delta evaluation: plane size without specialisation") : rc;
+  int64_t nblk = 0;
+  rc = gb_delta_rows_inv_eval(p32, p32->spec, fs, nf, &ev, rho, vloc, cref, p64->N, pot, calc_e, p64->partials,
+                              &nblk, st);
+  if (rc) return rc;
+  if (calc_e) {
+    if (nblk > p64->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
+    k_energy_final<<<6, 256, 0, st>>>(p64->partials, nblk, p64->dV, ev.e_ion, energies, gb_plan_counter(p64));
+    GB_CHECK_LAUNCH();
+  }
+  return 0;
+}
+
 int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
   GB_REQUIRE(rho0 > 0.0, "preconditioner: rho0 must be positive (got %g)", rho0);
   const int64_t total = p->NG;

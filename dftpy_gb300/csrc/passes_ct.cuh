@@ -332,6 +332,9 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   // per-thread energy sums in the field precision (a handful of elements per
   // thread); combined in FP64 across threads and CTAs
   T es[6] = {0, 0, 0, 0, 0, 0};
+  // FP64 only: optional copy of the convolution results (delta-evaluation reference)
+  T* coutp = nullptr;
+  if constexpr (sizeof(T) == 8) coutp = reinterpret_cast<T*>(ev.cout);
   auto point = [&](int idx, T rho, T vl_pre) {
     const int rr = idx / N, j = idx % N;
     const int64_t row = base + rr;
@@ -359,6 +362,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
     if (ev.vw) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_vw * RP + pr, j)];
       const T w = odd ? zz.y : zz.x;
+      if constexpr (sizeof(T) == 8) if (coutp) coutp[ev.slot_vw * ev.cstride + gidx] = w;
       // 1 / max(sqrt(rho_m), 1e-30), rho_m = rho if rho > 0 else 1e-30
       const T inv_sq = pos ? z2 : (rho > (T)0 ? (T)1 / fmax(sqrt(rho), (T)kZero) : (T)1e15);
       const T v = (T)0.5 * w * inv_sq;
@@ -368,6 +372,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
     if (ev.wt) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_wt * RP + pr, j)];
       const T kc = odd ? zz.y : zz.x;
+      if constexpr (sizeof(T) == 8) if (coutp) coutp[ev.slot_wt * ev.cstride + gidx] = kc;
       T rb_over_rc;                                       // rc^(beta - 1), rc = max(rho, 1e-30)
       if (b56) {
         if (pos) rb_over_rc = rho * z3 * z3 * z2;          // rho^(1/3) rho^(-1/2)
@@ -389,6 +394,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
     if (ev.hartree) {
       const cpx<T> zz = res[sw<T, NP>(ev.slot_h * RP + pr, j)];
       const T vh = odd ? zz.y : zz.x;
+      if constexpr (sizeof(T) == 8) if (coutp) coutp[ev.slot_h * ev.cstride + gidx] = vh;
       pot += vh;
       if (want_e) es[4] += (T)0.5 * vh * rho;
     }

@@ -52,6 +52,10 @@ struct EvalDesc {
   int slot_h, slot_vw, slot_wt;   // field slot of each convolution output
   double tf_x, vw_y, wt_alpha, wt_beta;
   double e_ion;
+  // optional (FP64 compile-time-size passes only): the convolution results
+  // before the pointwise epilogue, field slot f at cout + f * cstride
+  void* cout;
+  int64_t cstride;
 };
 
 struct KerDesc {
@@ -92,6 +96,23 @@ int gb_plane_variants_f32(int n0, int n1);
 int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, double beta, const KerDesc& kd,
                   const EvalDesc& ev, const void* vloc, void* pot, int calc_e, double* energies, cudaStream_t st);
 int gb_ct_cols_f64(gbofdft_plan*, void*, int64_t, int, int, int, int, double, const KerDesc*, cudaStream_t);
+// delta evaluation (passes_delta.cu): FP32 transforms of the change of the
+// derived fields against a reference density, FP64 pointwise work
+int gb_delta_rows_fwd(gbofdft_plan* p32, const double* rho, const double* rho_ref, void* spec, int64_t fstride,
+                      int nf, const int* ops, double beta, cudaStream_t st);
+int gb_delta_rows_inv_eval(gbofdft_plan* p32, const void* spec, int64_t fstride, int nf, const EvalDesc* ev,
+                           const double* rho, const double* vloc, const double* cref, int64_t cstride, double* pot,
+                           int calc_e, double* partials, int64_t* nblk, cudaStream_t st);
+int gb_delta_supported(int n0, int n1, int n2);
+// the whole delta evaluation of the fused terms (passes.cu): plane pipeline
+// of p32 on the changes, FP64 epilogue into pot / energies (energies use p64's
+// partials and dV)
+int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
+                       const double* cref, int nf, const int* ops, double beta, const KerDesc& kd,
+                       const EvalDesc& ev, const double* vloc, double* pot, int calc_e, double* energies,
+                       cudaStream_t st);
+// the reference density of a delta-evaluation state (device, N doubles)
+const double* gb_delta_ref(const gbofdft_delta* d);
 void gb_count_launch();
 int gb_smem_granted(const void* kern, int dev);
 void gb_smem_grant(const void* kern, int dev, int bytes);

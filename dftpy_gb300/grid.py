@@ -178,6 +178,18 @@ class DirectGrid(BaseGrid):
             self._plans[prec] = plan
         return self._plans[prec]
 
+    def delta_state(self):
+        """Delta-evaluation state of this grid's FP64 and FP32 plans (the FP64
+        evaluations of the mixed-precision refinement), or None when the grid
+        has no FP32 plane-pipeline specialisation."""
+        import torch
+        if "delta" not in self._plans:
+            try:
+                self._plans["delta"] = _lib.Delta(self.plan(torch.float64), self.plan(torch.float32))
+            except ValueError:            # no plane-pipeline specialisation
+                self._plans["delta"] = None
+        return self._plans["delta"]
+
     def get_reciprocal(self):
         if self._reciprocal is None:
             self._reciprocal = ReciprocalGrid(self)

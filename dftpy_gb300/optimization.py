@@ -79,6 +79,12 @@ DEFAULTS = {
     # the refined energy moves by 1e-9 eV/atom, forces by 1e-6 Ha/bohr)
     "fp32_c2": None,
     "refine_c2": 0.9,
+    # FP64 evaluations of the refinement as delta evaluations against its
+    # first (full FP64) one: FP32 transforms of the density change, FP64
+    # pointwise terms; a full evaluation rebases when the density has moved
+    # by more than delta_rtol (relative 2-norm) from the reference
+    "refine_delta": True,
+    "delta_rtol": 1e-3,
 }
 
 
@@ -114,7 +120,7 @@ class Optimization:
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
     def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None,
-             cg_rtol=0.1, pred_next=False, precond=False, c2=None):
+             cg_rtol=0.1, pred_next=False, precond=False, c2=None, delta=False):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -154,6 +160,10 @@ class Optimization:
             hb = ctypes.c_int64()
             _lib.check(L.gbofdft_tn_hess_workspace_bytes(hplan.handle, ctypes.byref(hb)))
             hws = _workspace(grid, ("hess", hess_rho.dtype), int(hb.value))
+            dstate = grid.delta_state() if delta else None
+            if dstate is not None:
+                opts.delta = dstate.handle
+                opts.delta_rtol = float(o["delta_rtol"])
             _lib.check(L.gbofdft_optimize_tn_split(
                 plan.handle, ctypes.byref(f), hplan.handle, ctypes.byref(hf), _lib.ptr(r), ctypes.byref(opts),
                 _lib.aligned_ptr(ws, 256), int(nb.value), _lib.aligned_ptr(hws, 256), int(hb.value),
@@ -162,7 +172,7 @@ class Optimization:
                    n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, n_eval_hess=res.n_eval_hess,
                    energies=list(res.energies), history=[hist[i] for i in range(res.n_history)],
                    n_sync=res.n_sync, t_sync=res.t_sync, t_total=res.t_total,
-                   t_eval_timed=res.t_eval_timed, n_eval_timed=res.n_eval_timed)
+                   t_eval_timed=res.t_eval_timed, n_eval_timed=res.n_eval_timed, n_eval_delta=res.n_eval_delta)
         return DirectField(grid, data=r), out
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):
@@ -208,7 +218,7 @@ class Optimization:
                 r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
                                    hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["refine_ncheck"],
                                    cg_rtol=o["refine_cg_rtol"], pred_next=True, precond=o["mixed_precond"],
-                                   c2=o["refine_c2"])
+                                   c2=o["refine_c2"], delta=o["refine_delta"])
             elif o["refine"] == "fp64":
                 r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
                                    eres=o["refine_eres"])

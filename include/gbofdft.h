@@ -211,6 +211,28 @@ int gbofdft_eval(gbofdft_plan* plan, const void* rho, const gbofdft_functional* 
                  double* energies_dev, int calc, void* stream);
 
 /*
+ * Delta evaluation (no reference counterpart; the FP64 evaluations of the
+ * mixed-precision refinement).  The convolutions of the fused terms are
+ * linear, so at a density rho near a reference density rho_ref
+ *   C(rho) = C(rho_ref) + K * (g(rho) - g(rho_ref))
+ * for each derived field g (rho, sqrt(rho), rho^beta).  A state holds rho_ref
+ * and its FP64 C(rho_ref); a delta evaluation transforms the change of g in
+ * FP32 (plane pipeline of hplan) and runs the pointwise terms in FP64, so its
+ * error is ~1e-7 of the change rather than of C.  rebase = 1 runs the full
+ * FP64 evaluation (gbofdft_eval) at rho and makes rho the reference.  The LWT
+ * and WGC terms, when present, are always evaluated in full FP64.
+ * plan: FP64, hplan: FP32 on the same grid (a plane-pipeline size); f: the
+ * FP64 functional, hf: the same terms in FP32 (its WT kernel table built on
+ * hplan).  Other arguments as gbofdft_eval.
+ */
+typedef struct gbofdft_delta gbofdft_delta;
+int gbofdft_delta_create(gbofdft_plan* plan, gbofdft_plan* hplan, gbofdft_delta** out);
+int gbofdft_delta_destroy(gbofdft_delta* d);
+int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_functional* f,
+                       const gbofdft_functional* hf, void* pot, double* energies_dev, int calc, int rebase,
+                       void* stream);
+
+/*
  * Wang-Teter kernel on the half spectrum for mean density rho0.
  * Replaces get_ke_kernel_wt / WTKernel (kedf/wt.py:58-73, kedf/kernel.py:325-334).
  */
@@ -394,6 +416,11 @@ typedef struct gbofdft_tn_options {
                        no reference counterpart.  0: the reference's plain CG */
   int time_evals;   /* 1: time the FP32 potential-only evaluations with CUDA
                        events (result t_eval_timed / n_eval_timed); 0: off */
+  gbofdft_delta* delta; /* split mode only: evaluate the FP64 energies and
+                           potentials by gbofdft_eval_delta against the last
+                           full evaluation (NULL: every one in full FP64) */
+  double delta_rtol;    /* rebase (full FP64 evaluation) when
+                           ||rho - rho_ref|| > delta_rtol ||rho_ref|| */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {
@@ -413,6 +440,7 @@ typedef struct gbofdft_tn_result {
   int n_eval_hess;        /* potential evaluations in the Hessian plan (split mode) */
   double t_eval_timed;    /* with time_evals: device seconds of the timed evaluations */
   int n_eval_timed;       /* ... and their number */
+  int n_eval_delta;       /* with opts.delta: evaluations done as delta evaluations */
 } gbofdft_tn_result;
 
 int gbofdft_tn_options_default(gbofdft_tn_options* opts);

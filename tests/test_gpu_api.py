@@ -226,6 +226,23 @@ def test_tn_al256_mixed_split_refine(api, golden):
     F = total.get_forces(rho)
     assert np.abs(F - a["forces"]).max() < 1e-5
     assert np.abs(F - t["forces"]).max() < 1e-5
+    # the refinement after its first evaluation runs delta evaluations
+    assert opt.stats["stages"][-1]["n_eval_delta"] > 0
+
+
+def test_tn_al256_mixed_delta_refine_matches_full_refine(api):
+    """The delta-evaluated refinement against the same refinement with every
+    FP64 evaluation in full: energies within 1e-9 eV/atom, forces within
+    1e-6 Ha/Bohr, densities within 1e-5 of max rho."""
+    st = systems.config_al256(0)
+    opt_d, rho_d, total = _solve(api, st, "WT", 1e-7, precision="mixed")
+    opt_f, rho_f, _ = _solve(api, st, "WT", 1e-7, precision="mixed", refine_delta=False)
+    assert opt_f.stats["stages"][-1]["n_eval_delta"] == 0
+    assert opt_d.stats["stages"][-1]["n_eval_delta"] > 0
+    assert abs(opt_d.energy - opt_f.energy) < 1e-9 / 27.211386 * st.nat
+    a, b = rho_d.to_numpy(), rho_f.to_numpy()
+    assert np.abs(a - b).max() < 1e-5 * np.abs(b).max()
+    assert np.abs(total.get_forces(rho_d) - total.get_forces(rho_f)).max() < 1e-6
 
 
 @pytest.mark.parametrize("interp", ["linear", "hermite"])

@@ -50,10 +50,37 @@ class Conv:
         self.gb = torch.zeros_like(self.b)
         self.mw, self.vw = torch.zeros_like(self.w), torch.zeros_like(self.w)
         self.mb, self.vb = torch.zeros_like(self.b), torch.zeros_like(self.b)
+        self.wtc = None            # BF16 weights packed for the tensor-core kernel (made on first use)
         self.sync_bf16()
 
     def sync_bf16(self):
         _lib.check(_L().gbofdft_nn_to_bf16(_lib.ptr(self.w), _lib.ptr(self.wb), self.w.numel(), _lib.stream_ptr()))
+        self.wtc = None
+
+    def tc_supported(self, shape):
+        D, H, W = shape
+        return bool(_L().gbofdft_nn_conv3d_tc_supported(self.cin, self.cout, D, H, W))
+
+    def forward_tc(self, x, shape, act, err):
+        """conv + bias (then SiLU when act) on the tensor cores, activations
+        rounded to BF16; err: device int32 flag of timed-out waits."""
+        D, H, W = shape
+        if self.wtc is None:
+            self.wtc = torch.empty(27 * self.cin * self.cout, dtype=torch.bfloat16, device="cuda")
+            _lib.check(_L().gbofdft_nn_conv3d_tc_pack(_lib.ptr(self.wb), self.cin, self.cout, _lib.ptr(self.wtc),
+                                                      _lib.stream_ptr()), "nn_conv3d_tc_pack")
+        z = torch.empty((self.cout, D, H, W), dtype=torch.float32, device="cuda")
+        _lib.check(_L().gbofdft_nn_conv3d_tc(_lib.ptr(x), self.cin, _lib.ptr(self.wtc), _lib.ptr(self.b), _lib.ptr(z),
+                                             self.cout, D, H, W, 1 if act else 0, _lib.ptr(err), _lib.stream_ptr()),
+                   "nn_conv3d_tc")
+        return z
+
+    def forward_act(self, x, shape, err, tc=True):
+        """silu(conv(x)) for inference: the tensor-core kernel with SiLU fused
+        where the layer shape has one, else the CUDA-core kernel."""
+        if tc and self.tc_supported(shape):
+            return self.forward_tc(x, shape, True, err)
+        return silu(self.forward(x, shape))
 
     @property
     def nparams(self):
@@ -84,6 +111,7 @@ class Conv:
         s = _lib.stream_ptr()
         _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.w), _lib.ptr(self.gw), _lib.ptr(self.mw), _lib.ptr(self.vw),
                                      _lib.ptr(self.wb), self.w.numel(), lr, b1, b2, eps, step, s))
+        self.wtc = None
         _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.b), _lib.ptr(self.gb), _lib.ptr(self.mb), _lib.ptr(self.vb),
                                      None, self.b.numel(), lr, b1, b2, eps, step, s))
 
@@ -169,11 +197,15 @@ class GuessNet:
     def stride(self):
         return 2 ** (len(self.channels) - 1)
 
-    def forward(self, x, keep=False):
-        """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward needs."""
+    def forward(self, x, keep=False, tc=True):
+        """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward
+        needs (FP32 activations, CUDA-core kernels).  Without keep the inner
+        layers run on the tensor cores (BF16 activations) when tc is set."""
         shape = tuple(x.shape[1:])
         if any(s % self.stride for s in shape):
             raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
+        if not keep:
+            return self._infer(x, shape, tc)
         tape = []
         skips = []
         h = x
@@ -199,6 +231,28 @@ class GuessNet:
         out = self.head.forward(h, shape)
         tape.append(("head", 0, h))
         self._tape = tape if keep else None
+        return out
+
+    def _infer(self, x, shape, tc):
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        skips = []
+        h = x
+        for lvl, (c1, c2) in enumerate(self.enc):
+            sh = tuple(h.shape[1:])
+            a1 = c1.forward_act(h, sh, err, tc)
+            a2 = c2.forward_act(a1, sh, err, tc)
+            skips.append(a2)
+            h = pool2(a2) if lvl < len(self.enc) - 1 else a2
+        for k, (c1, c2) in enumerate(self.dec):
+            lvl = len(self.channels) - 2 - k
+            u = up2(h)
+            sh = tuple(u.shape[1:])
+            s = add(c1.forward_act(u, sh, err, tc), skips[lvl])
+            h = c2.forward_act(s, sh, err, tc)
+        out = self.head.forward(h, shape)
+        self._tape = None
+        if int(err.item()) != 0:
+            raise RuntimeError("tensor-core convolution: a wait timed out (code %d)" % int(err.item()))
         return out
 
     def backward(self, gout):

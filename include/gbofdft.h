@@ -529,6 +529,21 @@ int gbofdft_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, 
                     double b2, double eps, int step, void* stream);
 int gbofdft_nn_to_bf16(const float* a, void* b, int64_t n, void* stream);
 
+/*
+ * Tensor-core (tcgen05) forward convolution of the inner layers: the
+ * activations are rounded to BF16, products accumulate in FP32 in tensor
+ * memory.  Layer shapes: c_in, c_out in {16, 32, 48, 64} pairs of the
+ * network, H a multiple of 16, W of 8 (..._supported returns 1 when a shape
+ * has a kernel).  w_packed: the BF16 weights repacked by ..._pack from
+ * [c_out][c_in][27] to [tap][c_in / 8][c_out][c_in % 8].  act = 1 applies
+ * SiLU to conv + bias.  err: device int, set non-zero if a wait inside the
+ * kernel timed out (the output is then incomplete).
+ */
+int gbofdft_nn_conv3d_tc_supported(int cin, int cout, int D, int H, int W);
+int gbofdft_nn_conv3d_tc_pack(const void* w_bf16, int cin, int cout, void* w_packed, void* stream);
+int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* w_packed, const void* bias, void* out, int cout, int D,
+                         int H, int W, int act, int* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

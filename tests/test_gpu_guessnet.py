@@ -47,6 +47,52 @@ def test_conv_kernels(gn, shape, cin, cout):
     assert np.abs(layer.gb.cpu().numpy() - gbr).max() <= 1e-5 * np.abs(gbr).max()
 
 
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 48), (48, 64), (64, 64), (64, 48)])
+@pytest.mark.parametrize("act", [0, 1])
+def test_conv_tensor_core(gn, cin, cout, act):
+    """tcgen05 convolution (BF16 activations and weights, FP32 accumulation)
+    against the oracle on the same BF16-rounded operands: within 2e-5 of
+    max |y|.  (3, 32, 24): odd depth, two y tiles, three x tiles, periodic
+    wrap in every direction; (64, 64) and (64, 48) stream the weights in
+    three slabs."""
+    import torch
+    from dftpy_gb300 import _lib
+    shape = (3, 32, 24)
+    rng = np.random.default_rng(7)
+    layer = gn.Conv(cin, cout, rng)
+    layer.b.copy_(torch.tensor(rng.standard_normal(cout), dtype=torch.float32))
+    assert layer.tc_supported(shape)
+    x = rng.standard_normal((cin,) + shape).astype(np.float32)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    y = layer.forward_tc(torch.tensor(x, device="cuda"), shape, act, err).cpu().numpy()
+    assert int(err.item()) == 0
+    w = _bf16_round(layer.w.cpu().numpy())
+    b = layer.b.cpu().numpy().astype(np.float64)
+    yr = G.conv3d(_bf16_round(x), w, b)
+    if act:
+        yr = G.silu(yr)
+    assert np.abs(y - yr).max() <= 2e-5 * np.abs(yr).max()
+    # shapes without a kernel are reported, not run
+    assert not layer.tc_supported((3, 8, 24)) and not layer.tc_supported((3, 32, 12))
+    assert not _lib.load().gbofdft_nn_conv3d_tc_supported(2, 16, 4, 16, 16)
+
+
+def test_network_inference_tensor_cores(gn):
+    """The tensor-core inference path of the whole network against the FP32
+    CUDA-core forward: BF16 activations move the output by < 2 % of its
+    range."""
+    import torch
+    net = gn.GuessNet(channels=(16, 32, 48, 64), seed=3)
+    rng = np.random.default_rng(4)
+    x = torch.tensor(rng.standard_normal((2, 16, 32, 16)).astype(np.float32), device="cuda")
+    ref = net.forward(x, keep=True).cpu().numpy()
+    net._tape = None
+    fast = net.forward(x).cpu().numpy()
+    slow = net.forward(x, tc=False).cpu().numpy()
+    np.testing.assert_allclose(slow, ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+    assert np.abs(fast - ref).max() <= 2e-2 * (np.abs(ref).max() + 1e-30)
+
+
 def test_pointwise_kernels(gn):
     import torch
     rng = np.random.default_rng(3)

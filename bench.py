@@ -4,11 +4,15 @@
 Workload (the single-GPU configuration the metric is quoted on): bulk fcc Al
 4x4x4 supercell, 256 atoms, 128^3 grid, KEDF WT (alpha = beta = 5/6) + LDA +
 Hartree + analytic local pseudopotential (PME), truncated-Newton direct
-minimisation from a uniform density, econv 1e-7 Ha.  One "step" is one full
-solve.  ``value`` is the mixed-precision solve (FP32 fields, FP64
-refinement) with the inputs already on the device; the FP64 ("plain") solve
-is timed beside it.  Each solve's energy is checked against the FP64
-reference within 1e-5 eV/atom.
+minimisation, econv 1e-7 Ha.  One "step" is one full solve.  ``value`` is
+the learned + mixed-precision solve: the starting density from the trained
+guess network (tensor-core inference on the step's own atomic-density and
+v_loc features, inside the timed region), then FP32 TN and the FP64
+refinement, with the evaluator's set-up (PP, kernel tables, plans) already
+on the device.  The FP64 ("plain") solve from the uniform density -- the
+reference's method -- and the mixed solve from the uniform density are timed
+beside it.  Each solve's energy is checked against the FP64 reference within
+1e-5 eV/atom.
 
 Under torchrun with N ranks every rank solves its own seeded snapshot (weak
 scaling, no data-path collective); rank 0 prints one JSON line.
@@ -41,6 +45,8 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
     p.add_argument("--no-plain", action="store_true", help="skip timing the FP64 plain path")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--guess", default="learned", choices=["learned", "uniform"],
+                   help="starting density of the timed solves (learned: the trained network's guess)")
     return p.parse_args()
 
 
@@ -156,8 +162,20 @@ def build_system(seed):
     return st, grid, total, rho0
 
 
-def solve(total, rho0, precision, time_evals=False):
+GUESS_WEIGHTS = os.path.join(ROOT, "dftpy_gb300", "data", "guessnet_al_wt.npz")
+
+
+def learned_guess():
+    """The trained guess network for this workload (weights loaded once, like
+    the plans; the guess itself is computed inside every timed step)."""
+    from dftpy_gb300 import guess as G
+    return G.LearnedGuess(G.GuessNet.load(GUESS_WEIGHTS))
+
+
+def solve(total, rho0, precision, time_evals=False, guesser=None):
     from dftpy_gb300.optimization import Optimization
+    if guesser is not None:
+        rho0 = guesser.guess(total, rho0.grid)
     opt = Optimization(EnergyEvaluator=total, optimization_method="TN",
                        optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100, "precision": precision,
                                              "time_evals": time_evals})
@@ -165,11 +183,11 @@ def solve(total, rho0, precision, time_evals=False):
     return opt, rho
 
 
-def timed_solves(total, rho0, precision, steps, warmup, flush, world):
+def timed_solves(total, rho0, precision, steps, warmup, flush, world, guesser=None):
     import torch
     from dftpy_gb300 import _lib
     for _ in range(warmup):
-        solve(total, rho0, precision)
+        solve(total, rho0, precision, guesser=guesser)
     torch.cuda.synchronize()
     times, energies, evals, glue = [], [], [], []
     t_ev, n_ev = 0.0, 0
@@ -184,7 +202,7 @@ def timed_solves(total, rho0, precision, steps, warmup, flush, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        opt, rho = solve(total, rho0, precision, time_evals=True)
+        opt, rho = solve(total, rho0, precision, time_evals=True, guesser=guesser)
         e1.record(s)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1000.0)
@@ -236,9 +254,11 @@ def eval_roofline(total, rho0, reps=50):
     return t, b_eval
 
 
-def e2e_solves(st, total, precision, steps, warmup):
-    """Public API with host buffers: pinned host density in, host density and
-    energy out, host<->device copies inside the timed region."""
+def e2e_solves(st, total, precision, steps, warmup, guesser=None):
+    """Public API with host buffers, host<->device copies inside the timed
+    region: the starting density from pinned host memory (uniform guess) or
+    the host positions the learned guess's features are built from (learned),
+    out the host density and energy."""
     import numpy as np
     import torch
     from dftpy_gb300.field import DirectField
@@ -249,8 +269,11 @@ def e2e_solves(st, total, precision, steps, warmup):
     for i in range(warmup + steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rho0 = DirectField(grid, data=host.to("cuda", non_blocking=True))
-        opt, rho = solve(total, rho0, precision)
+        if guesser is None:
+            rho0 = DirectField(grid, data=host.to("cuda", non_blocking=True))
+        else:
+            rho0 = DirectField(grid)            # only its grid is used: the guess copies the positions in
+        opt, rho = solve(total, rho0, precision, guesser=guesser)
         out_host.copy_(rho.as_subclass(torch.Tensor).to(torch.float64), non_blocking=True)
         torch.cuda.synchronize()
         e = float(opt.energy)
@@ -258,7 +281,8 @@ def e2e_solves(st, total, precision, steps, warmup):
         if i >= warmup:
             times.append(dt)
     nbytes = int(np.prod(st.nr)) * 8
-    return statistics.mean(times), nbytes, nbytes + 8, e
+    h2d = nbytes if guesser is None else st.nat * 3 * 8
+    return statistics.mean(times), h2d, nbytes + 8, e
 
 
 def cpu_baseline(st, golden_evals, workers):
@@ -341,15 +365,20 @@ def main():
     n_evals_ref, e_golden = golden_evals()
     # FP64 reference energy for this snapshot (plain GPU path; rank 0 also
     # matches the reference-generated fixture)
+    guesser = learned_guess() if args.guess == "learned" else None
     clocks = ClockSampler(local)
     clocks.start()
     times, energies, evals, launches, live = timed_solves(total, rho0, args.precision, args.steps, args.warmup,
-                                                          flush, world)
+                                                          flush, world, guesser=guesser)
     clk = clocks.stop()
     plain = None
     if not args.no_plain:
         pt, pe, pev, _, _ = timed_solves(total, rho0, "fp64", max(1, min(args.steps, 2)), 1, flush, world)
-        plain = {"value": statistics.mean(pt), "energy": pe[-1], "evals": pev[-1]}
+        plain = {"value": statistics.mean(pt), "energy": pe[-1], "evals": pev[-1], "guess": "uniform"}
+    uniform = None
+    if guesser is not None:
+        ut, ue, uev, _, _ = timed_solves(total, rho0, args.precision, max(1, min(args.steps, 2)), 1, flush, world)
+        uniform = {"value": statistics.mean(ut), "energy": ue[-1], "evals": uev[-1]}
     e_ref = plain["energy"] if plain else None
     if rank == 0 and e_golden is not None:
         e_ref = e_golden
@@ -362,7 +391,7 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = b_eval / t_eval / 1e9
     traffic = profile_traffic()
-    e2e_v, h2d, d2h, _ = e2e_solves(st, total, args.precision, 1 if args.steps < 2 else 2, 1)
+    e2e_v, h2d, d2h, _ = e2e_solves(st, total, args.precision, 1 if args.steps < 2 else 2, 1, guesser=guesser)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, t_ev, t_setup, ns = cpu_baseline(st, n_evals_ref, 1)
@@ -380,11 +409,15 @@ def main():
         "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1000.0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": {"mixed": "f32+f64", "fp64": "f64", "fp32": "f32"}[args.precision],
-        "data": "synthetic (seeded jittered fcc Al, uniform initial density)",
+        "data": "synthetic (seeded jittered fcc Al; starting density from the guess network trained on the "
+                "solver's own converged 2x2x2-cell densities)" if guesser is not None else
+                "synthetic (seeded jittered fcc Al, uniform initial density)",
         "config": {"workload": "al256_128_wt", "natoms": st.nat, "grid": list(st.nr),
                    "functional": "KEDF WT(5/6,5/6)+LDA+Hartree+analytic PP (PME order 10)",
                    "method": "TN econv 1e-7 Ha, maxfun 50", "precision": args.precision,
-                   "guess": "uniform", "l2": "512 MB buffer written between timed steps",
+                   "guess": ("learned (BF16 tcgen05 network, dftpy_gb300/data/guessnet_al_wt.npz; inference "
+                             "inside the timed step)") if guesser is not None else "uniform",
+                   "l2": "512 MB buffer written between timed steps",
                    "seed_per_rank": "rank"},
         "accuracy": {"max_err_ev_per_atom": err, "tolerance_ev_per_atom": TOL_EV_PER_ATOM,
                      "ok": None if err is None else err <= TOL_EV_PER_ATOM,
@@ -392,6 +425,7 @@ def main():
         "evaluations": evals[-1],
         "plain_fp64": plain,
         "speedup_vs_plain": (plain["value"] / t_step) if plain else None,
+        "mixed_uniform_guess": uniform,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic.get("bytes_per_eval") if traffic else None,

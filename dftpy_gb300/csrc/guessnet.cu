@@ -20,9 +20,11 @@
 namespace {
 
 constexpr int kVox = 256;     // output voxels per CTA (one per thread)
-constexpr int kCoT = 32;      // output channels per CTA
 constexpr int kCiT = 8;       // input channels staged per round
 
+// kCoT output channels per CTA (32, or 16 / 4 for narrower layers such as
+// the 1-channel head, so no CTA computes unused channels)
+template <int kCoT>
 __global__ void __launch_bounds__(kVox) k_conv3d(const float* __restrict__ in, int cin,
                                                   const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
                                                   float* __restrict__ out, int cout, int D, int H, int W,
@@ -263,9 +265,17 @@ int gbofdft_nn_conv3d(const float* in, int cin, const void* w_bf16, const float*
   GB_REQUIRE(cin > 0 && cout > 0 && D > 0 && H > 0 && W > 0, "nn_conv3d: bad shape");
   GB_REQUIRE(!transposed || !bias, "nn_conv3d: the transposed (input-gradient) convolution has no bias");
   const int64_t N = (int64_t)D * H * W;
-  dim3 grid((unsigned)((N + kVox - 1) / kVox), (unsigned)((cout + kCoT - 1) / kCoT));
-  k_conv3d<<<grid, kVox, 0, (cudaStream_t)stream>>>(in, cin, reinterpret_cast<const __nv_bfloat16*>(w_bf16), bias,
-                                                     out, cout, D, H, W, transposed);
+  const unsigned nv = (unsigned)((N + kVox - 1) / kVox);
+  const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(w_bf16);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cout <= 4) {
+    k_conv3d<4><<<dim3(nv, 1), kVox, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);
+  } else if (cout <= 16) {
+    k_conv3d<16><<<dim3(nv, 1), kVox, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);
+  } else {
+    k_conv3d<32><<<dim3(nv, (unsigned)((cout + 31) / 32)), kVox, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W,
+                                                                         transposed);
+  }
   GB_CHECK_LAUNCH();
   gb_count_launch();
   return GBOFDFT_OK;

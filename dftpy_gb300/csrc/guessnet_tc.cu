@@ -22,12 +22,15 @@
 // One thread issues the MMAs (M = 128, N = C_out, K = 16 per instruction,
 // 27 C_in / 16 of them); their completion is signalled on an mbarrier by
 // tcgen05.commit; the four warps then read the accumulator rows of their
-// TMEM lane quarter (tcgen05.ld 32x32b), add the bias, apply SiLU if asked
-// and store FP32 [C][D][H][W].  Layers whose 27-tap weights exceed 96 KB
-// stream them in three slabs of 9 taps (the slab buffer is reloaded after
-// the MMAs reading it have completed).  Waits are bounded: on a timeout the
-// kernel records an error code, waits (bounded) once more, releases its
-// tensor memory and returns.
+// TMEM lane quarter (tcgen05.ld 32x32b), add the bias, apply SiLU if asked,
+// add a skip tensor if given and store FP32 [C][D][H][W].  The input may be
+// read as the nearest-neighbour 2x upsampling of a half-size grid (the
+// decoder's upsample fused into the load).  CTAs are persistent (as many as
+// are resident; each loops over tiles), so weights that fit (27 taps <= 48
+// KB) are loaded once per CTA; larger layers stream them per tile in three
+// slabs of 9 taps (a slab buffer is reloaded after the MMAs reading it have
+// completed).  Waits are bounded: on a timeout the kernel records an error
+// code, waits (bounded) once more, releases its tensor memory and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -46,7 +49,7 @@ template <int CIN, int COUT> struct TcCfg {
   static constexpr int NCH = CIN / 8;
   static constexpr int HALO_BYTES = NCH * kChunkBytes;
   static constexpr int TAP_BYTES = CIN * COUT * 2;                 // one tap of packed weights
-  static constexpr int SLABS = 27 * TAP_BYTES > 96 * 1024 ? 3 : 1;
+  static constexpr int SLABS = 27 * TAP_BYTES > 64 * 1024 ? 3 : 1;
   static constexpr int TPS = 27 / SLABS;                           // taps per slab
   static constexpr int SLAB_BYTES = TPS * TAP_BYTES;
   static constexpr int SMEM = HALO_BYTES + SLAB_BYTES;
@@ -116,7 +119,8 @@ template <int CIN, int COUT>
 __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restrict__ in,
                                                           const __nv_bfloat16* __restrict__ wpk,
                                                           const float* __restrict__ bias, float* __restrict__ out,
-                                                          int D, int H, int W, int act, int* err) {
+                                                          int D, int H, int W, int act,
+                                                          const float* __restrict__ skip, int up, int* err) {
   using C = TcCfg<CIN, COUT>;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* halo = smem;
@@ -126,13 +130,14 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restric
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntx = W / 8, nty = H / 16;
-  int b = blockIdx.x;
-  const int x0 = (b % ntx) * 8;
-  b /= ntx;
-  const int y0 = (b % nty) * 16;
-  const int z = b / nty;
+  const int ntiles = ntx * nty * D;
   const int64_t HW = (int64_t)H * W, DHW = (int64_t)D * HW;
+  // input grid: the output grid, or (up) half of it in every direction,
+  // read as its nearest-neighbour 2x upsampling
+  const int Di = up ? D / 2 : D, Hi = up ? H / 2 : H, Wi = up ? W / 2 : W;
+  const int64_t HWi = (int64_t)Hi * Wi, DHWi = (int64_t)Di * HWi;
   const uint32_t bar_a = smem_u32(&bar);
+  const uint32_t halo_a = smem_u32(halo), w_a = smem_u32(wsm);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)),
                  "r"((uint32_t)C::TCOLS)
@@ -144,71 +149,83 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restric
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     failed = 0;
   }
-  // input brick in BF16: one 16-byte chunk (8 channels of one voxel) per item
-  for (int e = tid; e < C::NCH * kHalo; e += kTcThreads) {
-    const int v = e % kHalo, ch = e / kHalo;
-    const int hx = v % 10, hy = (v / 10) % 18, hz = v / 180;
-    const int gz = wrap(z + hz - 1, D), gy = wrap(y0 + hy - 1, H), gx = wrap(x0 + hx - 1, W);
-    const float* p = in + (int64_t)(ch * 8) * DHW + gz * HW + (int64_t)gy * W + gx;
-    uint32_t u[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const __nv_bfloat162 h2 = __floats2bfloat162_rn(__ldg(p + (2 * q) * DHW), __ldg(p + (2 * q + 1) * DHW));
-      u[q] = *reinterpret_cast<const uint32_t*>(&h2);
-    }
-    *reinterpret_cast<uint4*>(halo + ch * kChunkBytes + v * 16) = make_uint4(u[0], u[1], u[2], u[3]);
-  }
-  const uint32_t halo_a = smem_u32(halo), w_a = smem_u32(wsm);
-  uint32_t tbase = 0;
-  int committed = 0;
-  for (int s = 0; s < C::SLABS; ++s) {
-    if (s > 0) {
-      // the previous slab's MMAs must be done before its buffer is reused
-      if (!mbar_wait(bar_a, (uint32_t)((s - 1) & 1))) {
-        if (tid == 0) { failed = 1; atomicExch(err, 1); }
-      }
-      __syncthreads();
-      if (failed) break;
-    }
+  auto load_slab = [&](int s) {
     const uint4* src = reinterpret_cast<const uint4*>(wpk) + (int64_t)s * (C::SLAB_BYTES / 16);
     for (int i = tid; i < C::SLAB_BYTES / 16; i += kTcThreads) reinterpret_cast<uint4*>(wsm)[i] = __ldg(src + i);
-    // make the generic-proxy shared-memory writes visible to the tensor core
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    tbase = tslot;
-    if (tid == 0) {
-      for (int tl = 0; tl < C::TPS; ++tl) {
-        const int t = s * C::TPS + tl;
-        const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
-        const uint32_t a0 = halo_a + (uint32_t)(((dz * 18 + dy) * 10 + dx) * 16);
-        const uint32_t b0 = w_a + (uint32_t)(tl * C::TAP_BYTES);
+  };
+  // one-slab layers keep their weights for every tile of the CTA
+  if (C::SLABS == 1) load_slab(0);
+  uint32_t ncommit = 0;     // commits so far: the next wait is on parity (ncommit - 1) & 1
+  // persistent over tiles (tile = 16 rows x 8 columns of one z plane)
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int b = tile;
+    const int x0 = (b % ntx) * 8;
+    b /= ntx;
+    const int y0 = (b % nty) * 16;
+    const int z = b / nty;
+    // input brick in BF16: one 16-byte chunk (8 channels of one voxel) per item
+    for (int e = tid; e < C::NCH * kHalo; e += kTcThreads) {
+      const int v = e % kHalo, ch = e / kHalo;
+      const int hx = v % 10, hy = (v / 10) % 18, hz = v / 180;
+      int gz = wrap(z + hz - 1, D), gy = wrap(y0 + hy - 1, H), gx = wrap(x0 + hx - 1, W);
+      if (up) { gz >>= 1; gy >>= 1; gx >>= 1; }
+      const float* p = in + (int64_t)(ch * 8) * DHWi + gz * HWi + (int64_t)gy * Wi + gx;
+      uint32_t u[4];
 #pragma unroll
-        for (int kk = 0; kk < CIN / 16; ++kk) {
-          const uint64_t ad = sdesc(a0 + (uint32_t)(2 * kk * kChunkBytes), kChunkBytes, 160);
-          const uint64_t bd = sdesc(b0 + (uint32_t)(2 * kk * COUT * 16), COUT * 16, 128);
-          mma_bf16(tbase, ad, bd, C::IDESC, (t > 0 || kk > 0) ? 1u : 0u);
-        }
+      for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(__ldg(p + (2 * q) * DHWi), __ldg(p + (2 * q + 1) * DHWi));
+        u[q] = *reinterpret_cast<const uint32_t*>(&h2);
       }
-      mma_commit(bar_a);
+      *reinterpret_cast<uint4*>(halo + ch * kChunkBytes + v * 16) = make_uint4(u[0], u[1], u[2], u[3]);
     }
-    committed = s + 1;
-  }
-  // completion of the last committed slab (bounded; on a timeout one more
-  // bounded wait before the tensor memory is released)
-  const uint32_t last = (uint32_t)((committed - 1) & 1);
-  bool ok = !failed && mbar_wait(bar_a, last);
-  if (!ok) {
-    if (tid == 0) atomicExch(err, 2);
-    mbar_wait(bar_a, last);
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
+    for (int s = 0; s < C::SLABS; ++s) {
+      if (s > 0) {
+        // the previous slab's MMAs must be done before its buffer is reused
+        if (!mbar_wait(bar_a, (ncommit - 1) & 1u) && tid == 0) { failed = 1; atomicExch(err, 1); }
+        __syncthreads();
+        if (failed) break;
+      }
+      if (C::SLABS > 1) load_slab(s);
+      // make the generic-proxy shared-memory writes visible to the tensor core
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        const uint32_t tbase = tslot;
+        for (int tl = 0; tl < C::TPS; ++tl) {
+          const int t = s * C::TPS + tl;
+          const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+          const uint32_t a0 = halo_a + (uint32_t)(((dz * 18 + dy) * 10 + dx) * 16);
+          const uint32_t b0 = w_a + (uint32_t)(tl * C::TAP_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < CIN / 16; ++kk) {
+            const uint64_t ad = sdesc(a0 + (uint32_t)(2 * kk * kChunkBytes), kChunkBytes, 160);
+            const uint64_t bd = sdesc(b0 + (uint32_t)(2 * kk * COUT * 16), COUT * 16, 128);
+            mma_bf16(tbase, ad, bd, C::IDESC, (t > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(bar_a);
+      }
+      ++ncommit;
+    }
+    if (failed) break;
+    // completion of the tile's last commit (bounded; every thread waits, the
+    // decision to go on is taken together)
+    if (!mbar_wait(bar_a, (ncommit - 1) & 1u)) failed = 2;
+    __syncthreads();
+    if (failed) {
+      if (tid == 0) atomicExch(err, 2);
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // accumulator row m = warp * 32 + lane -> voxel (z, y0 + m / 8, x0 + m % 8)
     const int m = warp * 32 + lane;
     const int y = y0 + (m >> 3), x = x0 + (m & 7);
-    float* o = out + z * HW + (int64_t)y * W + x;
+    const int64_t off = z * HW + (int64_t)y * W + x;
+    float* o = out + off;
+    const float* sk = skip ? skip + off : nullptr;
+    const uint32_t tbase = tslot;
 #pragma unroll
     for (int cb = 0; cb < COUT / 16; ++cb) {
       float v[16];
@@ -218,14 +235,190 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restric
         const int co = cb * 16 + i;
         float r = v[i] + (bias ? __ldg(bias + co) : 0.0f);
         if (act) r = r / (1.0f + __expf(-r));
+        if (sk) r += __ldg(sk + (int64_t)co * DHW);
         o[(int64_t)co * DHW] = r;
       }
     }
+    // the accumulator and the halo are reused by the next tile
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
   }
+  // a timed-out wait: one more bounded wait for the MMAs in flight before
+  // the tensor memory is released
+  __syncthreads();
+  if (failed && ncommit > 0) mbar_wait(bar_a, (ncommit - 1) & 1u);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tslot), "r"((uint32_t)C::TCOLS)
+                 : "memory");
+}
+
+// z-pipelined form for layers whose weights stay in shared memory: a CTA
+// owns one column of tiles (16 rows x 8 columns) and walks zc planes of it.
+// The input brick is a ring of 4 planes (plane p in slot p mod 4; the taps
+// of output plane z read slots of planes z-1, z, z+1), so each step loads
+// one new plane, and it loads it while the MMAs of the current plane run;
+// the accumulator is double-buffered in TMEM, so the MMAs of plane z+1 run
+// while the epilogue of plane z drains.
+template <int CIN, int COUT> struct TczCfg {
+  static constexpr int NCH = CIN / 8;
+  static constexpr int PLANE = 18 * 10 * 16;            // one brick plane of one chunk (bytes)
+  static constexpr int CHUNK = 4 * PLANE;                // a chunk's ring of 4 planes
+  static constexpr int RING_BYTES = NCH * CHUNK;
+  static constexpr int SMEM = RING_BYTES + TcCfg<CIN, COUT>::SLAB_BYTES;
+  static constexpr int TCOLS = 2 * COUT <= 32 ? 32 : (2 * COUT <= 64 ? 64 : (2 * COUT <= 128 ? 128 : 256));
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kTcThreads) k_conv3d_tcz(const float* __restrict__ in,
+                                                           const __nv_bfloat16* __restrict__ wpk,
+                                                           const float* __restrict__ bias, float* __restrict__ out,
+                                                           int D, int H, int W, int act,
+                                                           const float* __restrict__ skip, int up, int zc,
+                                                           int* err) {
+  using C = TcCfg<CIN, COUT>;
+  using Z = TczCfg<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* ring = smem;
+  unsigned char* wsm = smem + Z::RING_BYTES;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  __shared__ int failed;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntx = W / 8, ncol = ntx * (H / 16);
+  const int col = blockIdx.x % ncol, chunk = blockIdx.x / ncol;
+  const int x0 = (col % ntx) * 8, y0 = (col / ntx) * 16;
+  const int z0 = chunk * zc, z1 = min(D, z0 + zc);
+  const int64_t HW = (int64_t)H * W, DHW = (int64_t)D * HW;
+  const int Di = up ? D / 2 : D, Hi = up ? H / 2 : H, Wi = up ? W / 2 : W;
+  const int64_t HWi = (int64_t)Hi * Wi, DHWi = (int64_t)Di * HWi;
+  const uint32_t bar_a = smem_u32(&bar);
+  const uint32_t ring_a = smem_u32(ring), w_a = smem_u32(wsm);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)),
+                 "r"((uint32_t)Z::TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    failed = 0;
+  }
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(wpk);
+    for (int i = tid; i < C::SLAB_BYTES / 16; i += kTcThreads) reinterpret_cast<uint4*>(wsm)[i] = __ldg(src + i);
+  }
+  // input plane p (periodic) into ring slot p & 3: items (chunk, voxel), the
+  // loads of up to 4 items issued before their stores
+  auto load_plane = [&](int p) {
+    const int gz0 = wrap(p, D);
+    const int gz = up ? gz0 >> 1 : gz0;
+    unsigned char* dst = ring + (p & 3) * Z::PLANE;
+    constexpr int NIT = Z::NCH * 180;
+    for (int e0 = 0; e0 < NIT; e0 += 4 * kTcThreads) {
+      float f[4][8];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * kTcThreads + tid;
+        if (e < NIT) {
+          const int v = e % 180, ch = e / 180;
+          int gy = wrap(y0 + v / 10 - 1, H), gx = wrap(x0 + v % 10 - 1, W);
+          if (up) { gy >>= 1; gx >>= 1; }
+          const float* q = in + (int64_t)(ch * 8) * DHWi + gz * HWi + (int64_t)gy * Wi + gx;
+#pragma unroll
+          for (int c = 0; c < 8; ++c) f[u][c] = __ldg(q + c * DHWi);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * kTcThreads + tid;
+        if (e < NIT) {
+          const int v = e % 180, ch = e / 180;
+          uint32_t w4[4];
+#pragma unroll
+          for (int q2 = 0; q2 < 4; ++q2) {
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(f[u][2 * q2], f[u][2 * q2 + 1]);
+            w4[q2] = *reinterpret_cast<const uint32_t*>(&h2);
+          }
+          *reinterpret_cast<uint4*>(dst + ch * Z::CHUNK + v * 16) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        }
+      }
+    }
+  };
+  auto publish = [&]() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  };
+  // MMAs of output plane z into accumulator buffer z & 1 (one thread)
+  auto issue = [&](int z) {
+    const uint32_t acc = tslot + (uint32_t)((z & 1) * COUT);
+    for (int t = 0; t < 27; ++t) {
+      const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+      const uint32_t a0 = ring_a + (uint32_t)(((z - 1 + dz) & 3) * Z::PLANE + (dy * 10 + dx) * 16);
+      const uint32_t b0 = w_a + (uint32_t)(t * C::TAP_BYTES);
+#pragma unroll
+      for (int kk = 0; kk < CIN / 16; ++kk) {
+        const uint64_t ad = sdesc(a0 + (uint32_t)(2 * kk * Z::CHUNK), Z::CHUNK, 160);
+        const uint64_t bd = sdesc(b0 + (uint32_t)(2 * kk * COUT * 16), COUT * 16, 128);
+        mma_bf16(acc, ad, bd, C::IDESC, (t > 0 || kk > 0) ? 1u : 0u);
+      }
+    }
+    mma_commit(bar_a);
+  };
+  // prologue: planes z0-1, z0, z0+1, the MMAs of z0
+  load_plane(z0 - 1);
+  load_plane(z0);
+  load_plane(z0 + 1);
+  publish();
+  if (tid == 0) issue(z0);
+  uint32_t ncommit = 1;
+  const int m = warp * 32 + lane;
+  const int y = y0 + (m >> 3), x = x0 + (m & 7);
+  for (int z = z0; z < z1; ++z) {
+    if (z + 1 < z1) load_plane(z + 2);     // overlaps the MMAs of z
+    const int64_t off = z * HW + (int64_t)y * W + x;
+    // the skip values of this thread's voxel, loaded before the wait
+    float skv[COUT];
+#pragma unroll
+    for (int co = 0; co < COUT; ++co) skv[co] = skip ? __ldg(skip + off + (int64_t)co * DHW) : 0.0f;
+    publish();
+    if (!mbar_wait(bar_a, (ncommit - 1) & 1u)) failed = 1;
+    __syncthreads();
+    if (failed) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (z + 1 < z1) {
+      if (tid == 0) issue(z + 1);         // overlaps the epilogue of z
+      ++ncommit;
+    }
+    float* o = out + off;
+    const uint32_t acc = tslot + (uint32_t)((z & 1) * COUT) + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int cb = 0; cb < COUT / 16; ++cb) {
+      float v[16];
+      tmem_ld16(acc + (uint32_t)(cb * 16), v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int co = cb * 16 + i;
+        float r = v[i] + (bias ? __ldg(bias + co) : 0.0f);
+        if (act) r = r / (1.0f + __expf(-r));
+        o[(int64_t)co * DHW] = r + skv[co];
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  if (failed) {
+    if (tid == 0) atomicExch(err, 3);
+    mbar_wait(bar_a, (ncommit - 1) & 1u);    // bounded, before the tensor memory is released
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tslot), "r"((uint32_t)Z::TCOLS)
                  : "memory");
 }
 
@@ -241,7 +434,7 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __
 
 template <int CIN, int COUT>
 int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, float* out, int D, int H, int W, int act,
-              int* err, cudaStream_t st) {
+              const float* skip, int up, int* err, cudaStream_t st) {
   using C = TcCfg<CIN, COUT>;
   static int granted[64] = {0};
   int dev = 0;
@@ -251,7 +444,29 @@ int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, floa
     granted[dev] = 1;
   }
   const int ntiles = (W / 8) * (H / 16) * D;
-  k_conv3d_tc<CIN, COUT><<<ntiles, kTcThreads, C::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, err);
+  if constexpr (C::SLABS == 1) {
+    // z-pipelined kernel: a CTA walks a column of tiles along z
+    using Z = TczCfg<CIN, COUT>;
+    static int zgranted[64] = {0}, nsms[64] = {0};
+    if (dev < 64 && !zgranted[dev]) {
+      GB_CUDA(cudaFuncSetAttribute(k_conv3d_tcz<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
+      GB_CUDA(cudaDeviceGetAttribute(&nsms[dev], cudaDevAttrMultiProcessorCount, dev));
+      zgranted[dev] = 1;
+    }
+    // about 8 CTAs per SM: z chunks of the columns (a chunk of zc planes
+    // loads zc + 2 input planes)
+    const int ncol = (W / 8) * (H / 16);
+    const int target = 8 * (dev < 64 && nsms[dev] > 0 ? nsms[dev] : 152);
+    int nchunk = (target + ncol - 1) / ncol;
+    if (nchunk < 1) nchunk = 1;
+    if (nchunk > D) nchunk = D;
+    const int zc = (D + nchunk - 1) / nchunk;
+    nchunk = (D + zc - 1) / zc;
+    k_conv3d_tcz<CIN, COUT><<<ncol * nchunk, kTcThreads, Z::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up,
+                                                                      zc, err);
+  } else {
+    k_conv3d_tc<CIN, COUT><<<ntiles, kTcThreads, C::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up, err);
+  }
   GB_CHECK_LAUNCH();
   gb_count_launch();
   return 0;
@@ -291,15 +506,17 @@ int gbofdft_nn_conv3d_tc_pack(const void* w, int cin, int cout, void* out, void*
 }
 
 int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* wpk, const void* bias, void* out, int cout, int D,
-                         int H, int W, int act, int* err, void* stream) {
+                         int H, int W, int act, const void* skip, int up, int* err, void* stream) {
   GB_REQUIRE(in && wpk && out && err, "nn_conv3d_tc: null argument");
   GB_REQUIRE(gbofdft_nn_conv3d_tc_supported(cin, cout, D, H, W),
              "nn_conv3d_tc: no tensor-core kernel for %d -> %d channels on %d x %d x %d", cin, cout, D, H, W);
+  GB_REQUIRE(!up || (D % 2 == 0 && H % 2 == 0 && W % 2 == 0), "nn_conv3d_tc: upsampled input needs even extents");
   int rc = 0;
   tc_dispatch(cin, cout, [&](auto a, auto b) {
     rc = launch_tc<decltype(a)::value, decltype(b)::value>(
         reinterpret_cast<const float*>(in), reinterpret_cast<const __nv_bfloat16*>(wpk),
-        reinterpret_cast<const float*>(bias), reinterpret_cast<float*>(out), D, H, W, act, err, (cudaStream_t)stream);
+        reinterpret_cast<const float*>(bias), reinterpret_cast<float*>(out), D, H, W, act,
+        reinterpret_cast<const float*>(skip), up, err, (cudaStream_t)stream);
   });
   return rc;
 }

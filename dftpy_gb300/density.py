@@ -45,6 +45,35 @@ class _RadialTable:
         return t
 
 
+_TABLES = {}
+_SMALL = {}
+
+
+def _cached(key, make):
+    """Small structure-independent device arrays (PME moduli of a grid,
+    species indices of a symbol list), kept by key."""
+    v = _SMALL.get(key)
+    if v is None:
+        if len(_SMALL) >= 256:
+            _SMALL.clear()
+        v = _SMALL[key] = make()
+    return v
+
+
+def _radial_table(q, v):
+    """_RadialTable of (q, v), cached by content (the spline fit is host work;
+    tables are per species, not per structure)."""
+    q = np.ascontiguousarray(q, dtype=float)
+    v = np.ascontiguousarray(v, dtype=float)
+    key = (q.shape, v.shape, hash(q.tobytes()), hash(v.tobytes()))
+    t = _TABLES.get(key)
+    if t is None:
+        if len(_TABLES) >= 64:
+            _TABLES.clear()
+        t = _TABLES[key] = _RadialTable(q, v)
+    return t
+
+
 def get_3d_value_recipe(r, arho, ions, grid, ncharge=None, rho=None, dtol=0.0, direct=True, pme=True, order=10,
                         **kwargs):
     """Superposed atomic values from reciprocal-space tables ``r[key]`` (|G|)
@@ -62,11 +91,15 @@ def get_3d_value_recipe(r, arho, ions, grid, ncharge=None, rho=None, dtol=0.0, d
         raise ValueError("no atomic table for %s" % sorted(missing))
     dtype = rho.dtype if rho is not None else torch.float64
     plan = grid.plan(dtype)
-    tables = [_RadialTable(r[k], arho[k]) for k in keys]
+    tables = [_radial_table(r[k], arho[k]) for k in keys]
     tabs = (_lib.VTable * len(keys))(*[t.ctypes() for t in tables])
-    spos = torch.tensor(ions.get_scaled_positions(), dtype=torch.float64, device="cuda").contiguous()
-    species = torch.tensor([keys.index(s) for s in ions.symbols], dtype=torch.int32, device="cuda")
-    bm = torch.tensor(pme_bm(grid.nrR, order).view(np.float64), device="cuda") if pme else None
+    # one host-to-device copy per call (each pageable copy waits for the
+    # stream); the species indices and the PME moduli are cached
+    spos = torch.from_numpy(np.ascontiguousarray(ions.get_scaled_positions(), dtype=np.float64)).to("cuda")
+    species = _cached(("species", tuple(keys), tuple(ions.symbols)),
+                      lambda: torch.tensor([keys.index(s) for s in ions.symbols], dtype=torch.int32, device="cuda"))
+    bm = _cached(("bm", tuple(int(x) for x in grid.nrR), int(order)),
+                 lambda: torch.tensor(pme_bm(grid.nrR, order).view(np.float64), device="cuda")) if pme else None
     nb = _lib.setup_workspace_bytes(plan, ions.nat)
     work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
     n0, n1, n2 = (int(x) for x in grid.nrR)

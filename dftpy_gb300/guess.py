@@ -61,9 +61,10 @@ class Conv:
         D, H, W = shape
         return bool(_L().gbofdft_nn_conv3d_tc_supported(self.cin, self.cout, D, H, W))
 
-    def forward_tc(self, x, shape, act, err):
-        """conv + bias (then SiLU when act) on the tensor cores, activations
-        rounded to BF16; err: device int32 flag of timed-out waits."""
+    def forward_tc(self, x, shape, act, err, skip=None, up=False):
+        """conv + bias (then SiLU when act, then + skip) on the tensor cores,
+        activations rounded to BF16; up: x is the half-size grid, read as its
+        2x nearest upsampling; err: device int32 flag of timed-out waits."""
         D, H, W = shape
         if self.wtc is None:
             self.wtc = torch.empty(27 * self.cin * self.cout, dtype=torch.bfloat16, device="cuda")
@@ -71,16 +72,19 @@ class Conv:
                                                       _lib.stream_ptr()), "nn_conv3d_tc_pack")
         z = torch.empty((self.cout, D, H, W), dtype=torch.float32, device="cuda")
         _lib.check(_L().gbofdft_nn_conv3d_tc(_lib.ptr(x), self.cin, _lib.ptr(self.wtc), _lib.ptr(self.b), _lib.ptr(z),
-                                             self.cout, D, H, W, 1 if act else 0, _lib.ptr(err), _lib.stream_ptr()),
-                   "nn_conv3d_tc")
+                                             self.cout, D, H, W, 1 if act else 0,
+                                             _lib.ptr(skip) if skip is not None else None, 1 if up else 0,
+                                             _lib.ptr(err), _lib.stream_ptr()), "nn_conv3d_tc")
         return z
 
-    def forward_act(self, x, shape, err, tc=True):
-        """silu(conv(x)) for inference: the tensor-core kernel with SiLU fused
-        where the layer shape has one, else the CUDA-core kernel."""
+    def forward_act(self, x, shape, err, tc=True, skip=None, up=False):
+        """silu(conv(x)) (+ skip) for inference, x upsampled 2x first when up:
+        the tensor-core kernel with all of it fused where the layer shape has
+        one, else the CUDA-core kernel and separate passes."""
         if tc and self.tc_supported(shape):
-            return self.forward_tc(x, shape, True, err)
-        return silu(self.forward(x, shape))
+            return self.forward_tc(x, shape, True, err, skip=skip, up=up)
+        a = silu(self.forward(up2(x) if up else x, shape))
+        return add(a, skip) if skip is not None else a
 
     @property
     def nparams(self):
@@ -245,9 +249,8 @@ class GuessNet:
             h = pool2(a2) if lvl < len(self.enc) - 1 else a2
         for k, (c1, c2) in enumerate(self.dec):
             lvl = len(self.channels) - 2 - k
-            u = up2(h)
-            sh = tuple(u.shape[1:])
-            s = add(c1.forward_act(u, sh, err, tc), skips[lvl])
+            sh = tuple(skips[lvl].shape[1:])
+            s = c1.forward_act(h, sh, err, tc, skip=skips[lvl], up=True)
             h = c2.forward_act(s, sh, err, tc)
         out = self.head.forward(h, shape)
         self._tape = None
@@ -320,15 +323,18 @@ def features(total, grid):
     """Network input (2, D, H, W): superposed Gaussian atomic densities over
     the mean minus one, and v_loc; plus sqrt(rho_atom) and rho0."""
     from .density import get_3d_value_recipe
+    from .field import DirectField
     ps = total.PSEUDO
     ions = ps.ions
     tabs = {s: systems.atomic_density_table(systems.SPECIES[s][0], systems.ATOMIC_SIGMA[s]) for s in set(ions.symbols)}
     r = {s: t[0] for s, t in tabs.items()}
     arho = {s: t[1] for s, t in tabs.items()}
-    ratom = get_3d_value_recipe(r, arho, ions, grid, dtol=1e-12)
+    # the network input is FP32: superpose in FP32 (the FP64 transforms of
+    # the superposition cost ten times more on this part)
+    ratom = get_3d_value_recipe(r, arho, ions, grid, dtol=1e-12, rho=DirectField(grid, dtype=torch.float32))
     rho0 = float(ions.get_ncharges()) / grid.volume
     ra = ratom.as_subclass(torch.Tensor).to(torch.float32)
-    vloc = ps.vreal_of(torch.float64).to(torch.float32).reshape(ra.shape)
+    vloc = ps.vreal_of(torch.float32).reshape(ra.shape)
     x = torch.stack([ra / rho0 - 1.0, vloc]).contiguous()
     phib = torch.sqrt(torch.clamp(ra, min=SQRT_CLAMP))
     return x, phib, rho0
@@ -362,21 +368,24 @@ def _solve(total, guess, precision="mixed", econv_per_atom=1e-8):
     return opt, rho
 
 
-def training_cell(seed, reps=(2, 2, 2), nr=(64, 64, 64)):
+def training_cell(seed, reps=(2, 2, 2), nr=(64, 64, 64), mg_max=0.3, sigmas=(0.15,)):
     """Training / validation cell: an Al/Mg snapshot as the batched workload
-    draws them (Mg fraction U(0, 0.3), jitter 0.15 Bohr) on a small cell."""
-    f = float(np.random.default_rng(10_000 + seed).random() * 0.3)
-    return systems.fcc_supercell(reps, sigma=0.15, seed=seed, nr=nr, mg_fraction=f, name="train_%d" % seed)
+    draws them (Mg fraction U(0, mg_max), jitter sigmas[seed % len(sigmas)]
+    Bohr) on a small cell; mg_max = 0 gives pure Al."""
+    f = float(np.random.default_rng(10_000 + seed).random() * mg_max)
+    sigma = float(sigmas[seed % len(sigmas)])
+    return systems.fcc_supercell(reps, sigma=sigma, seed=seed, nr=nr, mg_fraction=f, name="train_%d" % seed)
 
 
-def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 64, 64), workers=16, chunk=64):
+def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 64, 64), workers=16, chunk=64,
+                 mg_max=0.3, sigmas=(0.15,)):
     """(x, sqrt(rho_atom), sqrt(rho converged), rho0) per seed from the
     solver's own converged densities (solved as batches)."""
     from .batch import build_evaluator, optimize_batch
     data = []
     seeds = list(seeds)
     for c0 in range(0, len(seeds), chunk):
-        jobs = [build_evaluator(training_cell(s, reps, nr), kedf=kedf) for s in seeds[c0:c0 + chunk]]
+        jobs = [build_evaluator(training_cell(s, reps, nr, mg_max, sigmas), kedf=kedf) for s in seeds[c0:c0 + chunk]]
         res = optimize_batch(jobs, workers=workers, options={"precision": precision})
         for (total, rho_u), r in zip(jobs, res):
             x, phib, rho0 = features(total, rho_u.grid)
@@ -467,9 +476,14 @@ def main():
     p.add_argument("--eval", type=int, default=8, help="held-out cells (seeds 5000 ...)")
     p.add_argument("--eval-large", type=int, default=4, help="held-out batched-workload snapshots")
     p.add_argument("--out", default=None)
+    p.add_argument("--kedf", default="WGC", help="KEDF of the training solves (WGC: the batched workload's; "
+                                                  "WT: the 256-atom benchmark's)")
+    p.add_argument("--mg-max", type=float, default=0.3, help="Mg fraction drawn from U(0, mg_max); 0: pure Al")
+    p.add_argument("--sigma", default="0.15", help="position jitter(s) in Bohr, alternating over seeds")
     a = p.parse_args()
+    sigmas = tuple(float(v) for v in a.sigma.split(","))
     t0 = time.perf_counter()
-    data = make_dataset(range(1000, 1000 + a.train))
+    data = make_dataset(range(1000, 1000 + a.train), kedf=a.kedf, mg_max=a.mg_max, sigmas=sigmas)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     net = GuessNet(channels=tuple(int(c) for c in a.channels.split(",")), seed=0)
@@ -479,10 +493,11 @@ def main():
     t_train = time.perf_counter() - t1
     if a.out:
         net.save(a.out)
-    held = [training_cell(s) for s in range(5000, 5000 + a.eval)]
-    rows = evaluate_guesses(net, held)
-    large = [systems.config_alloy(5000 + s) for s in range(a.eval_large)]
-    rows_l = evaluate_guesses(net, large)
+    held = [training_cell(s, mg_max=a.mg_max, sigmas=sigmas) for s in range(5000, 5000 + a.eval)]
+    rows = evaluate_guesses(net, held, kedf=a.kedf)
+    large = [systems.config_alloy(5000 + s) for s in range(a.eval_large)] if a.kedf == "WGC" else \
+        [systems.config_al256(s) for s in range(a.eval_large)]
+    rows_l = evaluate_guesses(net, large, kedf=a.kedf)
 
     def summary(rs):
         out = {}

@@ -77,6 +77,29 @@ def test_conv_tensor_core(gn, cin, cout, act):
     assert not _lib.load().gbofdft_nn_conv3d_tc_supported(2, 16, 4, 16, 16)
 
 
+@pytest.mark.parametrize("cin,cout,shape", [(48, 32, (4, 32, 16)), (32, 16, (6, 32, 16)), (16, 32, (2, 16, 8))])
+def test_conv_tensor_core_fused_up_skip(gn, cin, cout, shape):
+    """The decoder form: input read as the 2x nearest upsampling of a
+    half-size grid, SiLU, then a skip tensor added, against the oracle's
+    up2 -> conv -> silu -> add on the same BF16-rounded operands.  (48, 32)
+    streams its weights per tile; (32, 16) and (16, 32) keep them and walk
+    columns of tiles along z (one and several planes per CTA)."""
+    import torch
+    rng = np.random.default_rng(8)
+    layer = gn.Conv(cin, cout, rng)
+    layer.b.copy_(torch.tensor(rng.standard_normal(cout), dtype=torch.float32))
+    xc = rng.standard_normal((cin,) + tuple(s // 2 for s in shape)).astype(np.float32)
+    sk = rng.standard_normal((cout,) + shape).astype(np.float32)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    y = layer.forward_tc(torch.tensor(xc, device="cuda"), shape, True, err, skip=torch.tensor(sk, device="cuda"),
+                         up=True).cpu().numpy()
+    assert int(err.item()) == 0
+    w = _bf16_round(layer.w.cpu().numpy())
+    b = layer.b.cpu().numpy().astype(np.float64)
+    yr = G.silu(G.conv3d(G.up2(_bf16_round(xc)), w, b)) + sk
+    assert np.abs(y - yr).max() <= 2e-5 * np.abs(yr).max()
+
+
 def test_network_inference_tensor_cores(gn):
     """The tensor-core inference path of the whole network against the FP32
     CUDA-core forward: BF16 activations move the output by < 2 % of its
@@ -187,3 +210,26 @@ def test_trained_network_gain(gn):
         assert r["learned"]["converged"] == 0 and r["uniform"]["converged"] == 0
         assert abs(r["learned"]["energy"] - r["uniform"]["energy"]) / r["nat"] * 27.211386 < 1e-5
     assert sum(r["learned"]["evals"] for r in rows) < 0.8 * sum(r["uniform"]["evals"] for r in rows)
+
+
+def test_al_network_gain_on_al256(gn):
+    """The network trained on pure-Al 2x2x2 WT cells (the benchmark's
+    functional) applied to the 256-atom 128^3 cell: from its guess the mixed
+    TN needs fewer than 85 % of the evaluations it needs from the uniform
+    density and ends at the same energy (1e-8 eV/atom: both stop within the
+    1e-7 Ha energy tolerance of the same minimum)."""
+    import torch
+    from dftpy_gb300 import systems
+    from dftpy_gb300.batch import build_evaluator
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    net = gn.GuessNet.load(os.path.join(here, "dftpy_gb300", "data", "guessnet_al_wt.npz"))
+    st = systems.config_al256(0)
+    total, rho_u = build_evaluator(st, kedf="WT")
+    o_u, _ = gn._solve(total, rho_u, econv_per_atom=1e-7 / st.nat)
+    g = gn.LearnedGuess(net).guess(total, rho_u.grid)
+    assert abs(float(g.as_subclass(torch.Tensor).sum()) * rho_u.grid.dV - st.nelec) < 1e-8 * st.nelec
+    o_l, _ = gn._solve(total, g, econv_per_atom=1e-7 / st.nat)
+    n_u = sum(s["n_eval_ev"] + s["n_eval_v"] + s.get("n_eval_hess", 0) for s in o_u.stats["stages"])
+    n_l = sum(s["n_eval_ev"] + s["n_eval_v"] + s.get("n_eval_hess", 0) for s in o_l.stats["stages"])
+    assert n_l < 0.85 * n_u, (n_l, n_u)
+    assert abs(o_l.energy - o_u.energy) / st.nat * 27.211386 < 1e-8

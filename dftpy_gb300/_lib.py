@@ -122,7 +122,7 @@ _SIGS = [
     ("gbofdft_nn_conv3d_tc_supported", ctypes.c_int, [ctypes.c_int] * 5),
     ("gbofdft_nn_conv3d_tc_pack", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, _P]),
     ("gbofdft_nn_conv3d_tc", ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                            ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, _P, _P]),
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, _P, _P]),
     ("gbofdft_plan_schedules", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     ("gbofdft_plan_set_schedule", ctypes.c_int, [_P, ctypes.c_int]),
     ("gbofdft_plan_get_schedule", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),

@@ -25,18 +25,20 @@ constexpr int kNormThreads = 256;
 template <typename T>
 __global__ void __launch_bounds__(kNormThreads) k_clamp_partial(T* __restrict__ rho, int64_t n, double dtol,
                                                                 double* __restrict__ partial) {
-  KSum s;
-  s.init();
+  // per-thread sums in the field precision (a handful of elements each; no
+  // FP64 instruction per element in the FP32 instantiation), FP64 above
+  const T tol = (T)dtol;
+  T acc = (T)0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     T v = rho[i];
-    if ((double)v < dtol) {
-      v = (T)dtol;
+    if (v < tol) {
+      v = tol;
       rho[i] = v;
     }
-    s.add((double)v);
+    acc += v;
   }
   __shared__ double red[kNormThreads / 32];
-  const double v = warp_sum(s.value());
+  const double v = warp_sum((double)acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -47,27 +49,32 @@ __global__ void __launch_bounds__(kNormThreads) k_clamp_partial(T* __restrict__ 
   }
 }
 
-__device__ __forceinline__ double sum_partials(const double* __restrict__ partial, int nblk) {
+// sum of the per-CTA partials by the whole CTA in a fixed order (thread t
+// takes partials t, t + kNormThreads, ...; then warps, then warp results), so
+// every CTA that computes it gets the same value
+__device__ __forceinline__ double cta_sum_partials(const double* __restrict__ partial, int nblk) {
+  __shared__ double red[kNormThreads / 32];
   KSum t;
   t.init();
-  for (int b = 0; b < nblk; ++b) t.add(partial[b]);
-  return t.value();
+  for (int b = threadIdx.x; b < nblk; b += kNormThreads) t.add(__ldcg(partial + b));
+  const double v = warp_sum(t.value());
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  KSum u;
+  u.init();
+  for (int w = 0; w < kNormThreads / 32; ++w) u.add(red[w]);
+  return u.value();
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kNormThreads) k_scale_to(T* __restrict__ rho, int64_t n,
                                                            const double* __restrict__ partial, int nblk, double dV,
                                                            double ncharge, double* __restrict__ nc_out) {
-  __shared__ double fac;
-  if (threadIdx.x == 0) {
-    const double nc = sum_partials(partial, nblk) * dV;
-    fac = ncharge > 1e-6 ? ncharge / nc : 1.0;
-    if (nc_out && blockIdx.x == 0) *nc_out = nc;
-  }
-  __syncthreads();
-  const double f = fac;
+  const double nc = cta_sum_partials(partial, nblk) * dV;
+  if (nc_out && blockIdx.x == 0 && threadIdx.x == 0) *nc_out = nc;
+  const T f = (T)(ncharge > 1e-6 ? ncharge / nc : 1.0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    rho[i] = (T)((double)rho[i] * f);
+    rho[i] = rho[i] * f;
 }
 
 }  // namespace

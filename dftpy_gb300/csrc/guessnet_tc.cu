@@ -120,7 +120,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restric
                                                           const __nv_bfloat16* __restrict__ wpk,
                                                           const float* __restrict__ bias, float* __restrict__ out,
                                                           int D, int H, int W, int act,
-                                                          const float* __restrict__ skip, int up, int* err) {
+                                                          const float* __restrict__ skip, int up, int nstore,
+                                                          int* err) {
   using C = TcCfg<CIN, COUT>;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* halo = smem;
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tc(const float* __restric
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int co = cb * 16 + i;
+        if (co >= nstore) continue;
         float r = v[i] + (bias ? __ldg(bias + co) : 0.0f);
         if (act) r = r / (1.0f + __expf(-r));
         if (sk) r += __ldg(sk + (int64_t)co * DHW);
@@ -275,8 +277,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tcz(const float* __restri
                                                            const __nv_bfloat16* __restrict__ wpk,
                                                            const float* __restrict__ bias, float* __restrict__ out,
                                                            int D, int H, int W, int act,
-                                                           const float* __restrict__ skip, int up, int zc,
-                                                           int* err) {
+                                                           const float* __restrict__ skip, int up, int nstore,
+                                                           int zc, int* err) {
   using C = TcCfg<CIN, COUT>;
   using Z = TczCfg<CIN, COUT>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -384,7 +386,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tcz(const float* __restri
     // the skip values of this thread's voxel, loaded before the wait
     float skv[COUT];
 #pragma unroll
-    for (int co = 0; co < COUT; ++co) skv[co] = skip ? __ldg(skip + off + (int64_t)co * DHW) : 0.0f;
+    for (int co = 0; co < COUT; ++co) skv[co] = (skip && co < nstore) ? __ldg(skip + off + (int64_t)co * DHW) : 0.0f;
     publish();
     if (!mbar_wait(bar_a, (ncommit - 1) & 1u)) failed = 1;
     __syncthreads();
@@ -403,6 +405,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3d_tcz(const float* __restri
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int co = cb * 16 + i;
+        if (co >= nstore) continue;
         float r = v[i] + (bias ? __ldg(bias + co) : 0.0f);
         if (act) r = r / (1.0f + __expf(-r));
         o[(int64_t)co * DHW] = r + skv[co];
@@ -434,7 +437,7 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __
 
 template <int CIN, int COUT>
 int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, float* out, int D, int H, int W, int act,
-              const float* skip, int up, int* err, cudaStream_t st) {
+              const float* skip, int up, int nstore, int* err, cudaStream_t st) {
   using C = TcCfg<CIN, COUT>;
   static int granted[64] = {0};
   int dev = 0;
@@ -463,9 +466,10 @@ int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, floa
     const int zc = (D + nchunk - 1) / nchunk;
     nchunk = (D + zc - 1) / zc;
     k_conv3d_tcz<CIN, COUT><<<ncol * nchunk, kTcThreads, Z::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up,
-                                                                      zc, err);
+                                                                      nstore, zc, err);
   } else {
-    k_conv3d_tc<CIN, COUT><<<ntiles, kTcThreads, C::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up, err);
+    k_conv3d_tc<CIN, COUT><<<ntiles, kTcThreads, C::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up, nstore,
+                                                                 err);
   }
   GB_CHECK_LAUNCH();
   gb_count_launch();
@@ -505,9 +509,10 @@ int gbofdft_nn_conv3d_tc_pack(const void* w, int cin, int cout, void* out, void*
   return 0;
 }
 
-int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* wpk, const void* bias, void* out, int cout, int D,
-                         int H, int W, int act, const void* skip, int up, int* err, void* stream) {
+int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* wpk, const void* bias, void* out, int cout, int nstore,
+                         int D, int H, int W, int act, const void* skip, int up, int* err, void* stream) {
   GB_REQUIRE(in && wpk && out && err, "nn_conv3d_tc: null argument");
+  GB_REQUIRE(nstore >= 1 && nstore <= cout, "nn_conv3d_tc: nstore %d outside [1, %d]", nstore, cout);
   GB_REQUIRE(gbofdft_nn_conv3d_tc_supported(cin, cout, D, H, W),
              "nn_conv3d_tc: no tensor-core kernel for %d -> %d channels on %d x %d x %d", cin, cout, D, H, W);
   GB_REQUIRE(!up || (D % 2 == 0 && H % 2 == 0 && W % 2 == 0), "nn_conv3d_tc: upsampled input needs even extents");
@@ -516,7 +521,7 @@ int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* wpk, const void* b
     rc = launch_tc<decltype(a)::value, decltype(b)::value>(
         reinterpret_cast<const float*>(in), reinterpret_cast<const __nv_bfloat16*>(wpk),
         reinterpret_cast<const float*>(bias), reinterpret_cast<float*>(out), D, H, W, act,
-        reinterpret_cast<const float*>(skip), up, err, (cudaStream_t)stream);
+        reinterpret_cast<const float*>(skip), up, nstore, err, (cudaStream_t)stream);
   });
   return rc;
 }

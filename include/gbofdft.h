@@ -538,13 +538,15 @@ int gbofdft_nn_to_bf16(const float* a, void* b, int64_t n, void* stream);
  * [c_out][c_in][27] to [tap][c_in / 8][c_out][c_in % 8].  act = 1 applies
  * SiLU to conv + bias; skip (or NULL): a [c_out][D][H][W] tensor added after
  * that; up = 1: in is a (D/2, H/2, W/2) grid read as its nearest-neighbour
- * 2x upsampling.  err: device int, set non-zero if a wait inside the kernel
- * timed out (the output is then incomplete).
+ * 2x upsampling.  nstore <= c_out: only output channels [0, nstore) are
+ * written (bias, skip and out hold nstore channels; a narrower layer runs as a
+ * c_out-wide one with zero weights).  err: device int, set non-zero if a wait
+ * inside the kernel timed out (the output is then incomplete).
  */
 int gbofdft_nn_conv3d_tc_supported(int cin, int cout, int D, int H, int W);
 int gbofdft_nn_conv3d_tc_pack(const void* w_bf16, int cin, int cout, void* w_packed, void* stream);
-int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* w_packed, const void* bias, void* out, int cout, int D,
-                         int H, int W, int act, const void* skip, int up, int* err, void* stream);
+int gbofdft_nn_conv3d_tc(const void* in, int cin, const void* w_packed, const void* bias, void* out, int cout,
+                         int nstore, int D, int H, int W, int act, const void* skip, int up, int* err, void* stream);
 
 #ifdef __cplusplus
 }

@@ -47,14 +47,15 @@ def test_conv_kernels(gn, shape, cin, cout):
     assert np.abs(layer.gb.cpu().numpy() - gbr).max() <= 1e-5 * np.abs(gbr).max()
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 48), (48, 64), (64, 64), (64, 48)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 48), (48, 64), (64, 64), (64, 48), (16, 1)])
 @pytest.mark.parametrize("act", [0, 1])
 def test_conv_tensor_core(gn, cin, cout, act):
     """tcgen05 convolution (BF16 activations and weights, FP32 accumulation)
     against the oracle on the same BF16-rounded operands: within 2e-5 of
     max |y|.  (3, 32, 24): odd depth, two y tiles, three x tiles, periodic
     wrap in every direction; (64, 64) and (64, 48) stream the weights in
-    three slabs."""
+    three slabs; (16, 1), the head, runs 16 wide with zero weights and
+    stores one channel."""
     import torch
     from dftpy_gb300 import _lib
     shape = (3, 32, 24)

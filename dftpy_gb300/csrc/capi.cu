@@ -305,9 +305,10 @@ static int eval_extra(gbofdft_plan* p, const void* rho, const gbofdft_functional
 }
 
 // gbofdft_eval; cout != nullptr (FP64 compile-time-size passes) also stores
-// the convolution results, field slot f at cout + f * N
+// the convolution results, field slot f at cout + f * N; extras = 0 leaves
+// out the LWT / WGC terms (the fused terms alone)
 static int eval_impl(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
-                     int calc, void* cout, cudaStream_t st) {
+                     int calc, void* cout, cudaStream_t st, bool extras = true) {
   GB_REQUIRE(p && rho && f && pot, "eval: null argument");
   GB_REQUIRE(!(calc & GBOFDFT_CALC_E) || energies, "eval: energies buffer required with CALC_E");
   EvalDesc ev;
@@ -322,7 +323,7 @@ static int eval_impl(gbofdft_plan* p, const void* rho, const gbofdft_functional*
   if (!cout) {
     rc = gb_eval_plane(p, rho, nf, ops, f->wt_beta, kd, ev, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies,
                        st);
-    if (rc == 0) return eval_extra(p, rho, f, pot, energies, calc, st);
+    if (rc == 0) return extras ? eval_extra(p, rho, f, pot, energies, calc, st) : 0;
     if (rc != 1) return rc;
   } else {
     GB_REQUIRE(p->prec == GBOFDFT_F64 && gb_use_ct(), "eval: convolution output needs the FP64 specialised passes");
@@ -336,16 +337,16 @@ static int eval_impl(gbofdft_plan* p, const void* rho, const gbofdft_functional*
   }
   if (!rc)
     rc = gb_rows_inv_eval(p, p->spec, fs, nf, ev, rho, f->vloc, pot, (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
-  if (!rc) rc = eval_extra(p, rho, f, pot, energies, calc, st);
+  if (!rc && extras) rc = eval_extra(p, rho, f, pot, energies, calc, st);
   return rc;
 }
 
-// Delta-evaluation state: the reference density and its FP64 convolution
-// results, on the FP64 plan's grid.
+// Delta-evaluation state: the reference density, its FP64 convolution
+// results, potential and energies of the fused terms, on the FP64 plan's grid.
 struct gbofdft_delta {
   gbofdft_plan* p64;
   gbofdft_plan* p32;
-  double* buf;      // rho_ref [N], then C_ref [GB_MAX_FIELDS][N]
+  double* buf;      // rho_ref [N], pot_ref [N], C_ref [GB_MAX_FIELDS][N], E_ref [GB_NE]
   int valid;
   int nf;
   int ops[GB_MAX_FIELDS];
@@ -376,7 +377,7 @@ int gbofdft_delta_create(gbofdft_plan* plan, gbofdft_plan* hplan, gbofdft_delta*
   memset(d, 0, sizeof(*d));
   d->p64 = plan;
   d->p32 = hplan;
-  cudaError_t e = cudaMalloc(&d->buf, sizeof(double) * (size_t)plan->N * (1 + GB_MAX_FIELDS));
+  cudaError_t e = cudaMalloc(&d->buf, sizeof(double) * ((size_t)plan->N * (2 + GB_MAX_FIELDS) + GB_NE));
   if (e != cudaSuccess) {
     delete d;
     return gb_set_error(GBOFDFT_ERR_ALLOC, "delta_create: %s", cudaGetErrorString(e));
@@ -406,18 +407,26 @@ int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_function
   if (rc) return rc;
   const int64_t N = d->p64->N;
   double* rho_ref = d->buf;
-  double* cref = d->buf + N;
-  if (rebase || nf == 0) {
-    rc = eval_impl(d->p64, rho, f, pot, energies, calc, nf > 0 ? cref : nullptr, st);
+  double* pot_ref = d->buf + N;
+  double* cref = d->buf + 2 * N;
+  double* eref = d->buf + (2 + GB_MAX_FIELDS) * N;
+  if (nf == 0) return eval_impl(d->p64, rho, f, pot, energies, calc, nullptr, st);
+  if (rebase) {
+    // the fused terms in full FP64 (energies always, into the state), kept as
+    // the reference; then the LWT / WGC terms on top of the caller's outputs
+    rc = eval_impl(d->p64, rho, f, pot, eref, calc | GBOFDFT_CALC_E, cref, st, false);
     if (rc) return rc;
     GB_CUDA(cudaMemcpyAsync(rho_ref, rho, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(pot_ref, pot, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, st));
+    if (calc & GBOFDFT_CALC_E)
+      GB_CUDA(cudaMemcpyAsync(energies, eref, sizeof(double) * GB_NE, cudaMemcpyDeviceToDevice, st));
     d->valid = 1;
     d->nf = nf;
     for (int i = 0; i < GB_MAX_FIELDS; ++i) {
       d->ops[i] = i < nf ? ops[i] : -1;
       d->kind[i] = i < nf ? kd.type[i] : -1;
     }
-    return 0;
+    return eval_extra(d->p64, rho, f, pot, energies, calc, st);
   }
   GB_REQUIRE(d->valid, "eval_delta: no reference evaluation yet (call with rebase = 1 first)");
   GB_REQUIRE(d->nf == nf, "eval_delta: functional terms differ from the reference evaluation's");
@@ -428,9 +437,9 @@ int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_function
     GB_REQUIRE(hf && hf->wt && hf->wt_kernel, "eval_delta: WT needs the FP32 functional's kernel table");
     kd.arr[ev.slot_wt] = hf->wt_kernel;
   }
-  rc = gb_eval_delta_core(d->p64, d->p32, reinterpret_cast<const double*>(rho), rho_ref, cref, nf, ops, f->wt_beta,
-                          kd, ev, reinterpret_cast<const double*>(f->vloc), reinterpret_cast<double*>(pot),
-                          (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
+  rc = gb_eval_delta_core(d->p64, d->p32, reinterpret_cast<const double*>(rho), rho_ref, pot_ref, eref, cref, nf, ops,
+                          f->wt_beta, kd, ev, reinterpret_cast<const double*>(f->vloc),
+                          reinterpret_cast<double*>(pot), (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
   if (!rc) rc = eval_extra(d->p64, rho, f, pot, energies, calc, st);
   return rc;
 }

@@ -681,10 +681,15 @@ int gb_eval_plane(gbofdft_plan* p, const void* rho, int nf, const int* ops, doub
   return 0;
 }
 
+// energies = reference energies + the changes k_energy_final wrote
+__global__ void k_add_ref_energies(double* __restrict__ e, const double* __restrict__ eref) {
+  if (threadIdx.x < GB_NE) e[threadIdx.x] += eref[threadIdx.x];
+}
+
 int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
-                       const double* cref, int nf, const int* ops, double beta, const KerDesc& kd,
-                       const EvalDesc& ev, const double* vloc, double* pot, int calc_e, double* energies,
-                       cudaStream_t st) {
+                       const double* pot_ref, const double* eref, const double* cref, int nf, const int* ops,
+                       double beta, const KerDesc& kd, const EvalDesc& ev, const double* vloc, double* pot,
+                       int calc_e, double* energies, cudaStream_t st) {
   GB_REQUIRE(p32->plane_ok && p32->prec == GBOFDFT_F32 && nf > 0 && gb_use_ct(),
              "delta evaluation: needs an FP32 plan with the plane pipeline");
   const float* pm_arr[GB_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
@@ -699,12 +704,15 @@ int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, 
   if (!rc) rc = gb_plane_conv_f32(p32, p32->spec, fs, nf, &kd, pm_arr, 1.0 / (double)p32->N, st);
   if (rc) return rc == 1 ? gb_set_error(GBOFDFT_ERR_STATE, "delta evaluation: plane size without specialisation") : rc;
   int64_t nblk = 0;
-  rc = gb_delta_rows_inv_eval(p32, p32->spec, fs, nf, &ev, rho, vloc, cref, p64->N, pot, calc_e, p64->partials,
-                              &nblk, st);
+  rc = gb_delta_rows_inv_eval(p32, p32->spec, fs, nf, &ev, rho, rho_ref, pot_ref, vloc, cref, p64->N, pot, calc_e,
+                              p64->partials, &nblk, st);
   if (rc) return rc;
   if (calc_e) {
     if (nblk > p64->max_partials) return gb_set_error(GBOFDFT_ERR_STATE, "partials buffer too small");
-    k_energy_final<<<6, 256, 0, st>>>(p64->partials, nblk, p64->dV, ev.e_ion, energies, gb_plan_counter(p64));
+    // the partials are energy changes: sum them (no ion term), add the reference's
+    k_energy_final<<<6, 256, 0, st>>>(p64->partials, nblk, p64->dV, 0.0, energies, gb_plan_counter(p64));
+    GB_CHECK_LAUNCH();
+    k_add_ref_energies<<<1, 32, 0, st>>>(energies, eref);
     GB_CHECK_LAUNCH();
   }
   return 0;

@@ -1,15 +1,15 @@
 // Delta evaluation: the functional at a density rho close to a reference
-// density rho_ref whose FP64 convolution results C_ref are known.  The
-// convolutions are linear, so
+// density rho_ref whose FP64 convolution results C_ref, potential and
+// energies are known.  The convolutions are linear, so
 //   C(rho) = C_ref + K * (g(rho) - g(rho_ref))
 // for each derived field g (rho, sqrt(rho), rho^beta): the change of g is
 // formed accurately (FP64 difference, power laws through log1p / expm1),
 // rounded to FP32 and transformed by the FP32 plane pipeline.  FP32 rounding
 // then perturbs C by ~1e-7 of the CHANGE instead of ~1e-16 of C, which for
 // changes below ~1e-3 of the density is at the FP64 energy resolution of the
-// functional.  The pointwise epilogue (TF, vW, WT, LDA, Hartree, local PP)
-// runs in FP64 on C_ref + the transformed change, with the same formulas and
-// clamps as the FP64 evaluation.
+// functional.  The pointwise terms (TF, vW, WT, LDA, Hartree, local PP) are
+// formed the same way, as FP32 changes added to the FP64 reference potential
+// and energies (the FP64 pipe of this part is ~60x slower than FP32).
 //
 // Layouts are those of the FP32 plane pipeline: the row passes read and
 // write plane-major spectra (passes_ct.cuh, plane_ct.cuh).
@@ -100,6 +100,8 @@ struct DeltaRowsInv {
   CtRowsInv c;          // spectra, geometry and twiddles of the FP32 inverse row pass
   EvalDesc ev;
   const double* rho;
+  const double* rho_ref;
+  const double* pot_ref;   // the reference evaluation's potential (fused terms)
   const double* vloc;
   const double* cref;   // field slot f at cref + f * cstride
   int64_t cstride;
@@ -109,8 +111,72 @@ struct DeltaRowsInv {
   int b56;
 };
 
-// Inverse row pass (C2R of the transformed changes) + FP64 epilogue on
-// C_ref + change; energies as per-CTA partial sums (GB_NE per CTA).
+// The FP64 epilogue of one point (the same formulas and clamps as the FP64
+// evaluation): potential and the six energy densities (before dV).
+__device__ __forceinline__ void point64(const DeltaRowsInv& a, double rho, double w, double kc, double vh,
+                                        double vl, double& pot, double (&e)[6]) {
+  const EvalDesc& ev = a.ev;
+  const bool pos = rho > kZero;
+  double z3 = 0.0, z2 = 0.0;
+  if (pos) { z3 = rcbrt_d(rho); z2 = rsqrt_d(rho); }
+  pot = 0.0;
+  for (int k = 0; k < 6; ++k) e[k] = 0.0;
+  if (ev.tf) {
+    pot += a.tf_v * (pos ? rho * z3 : cbrt(rho * rho));
+    double r53;
+    if (pos) r53 = rho * rho * z3;
+    else { double r5 = rho * rho; r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho; r53 = cbrt(r5); }
+    e[0] = r53 * a.tf_e;
+  }
+  if (ev.vw) {
+    const double inv_sq = pos ? z2 : (rho > 0.0 ? 1.0 / fmax(sqrt(rho), kZero) : 1e15);
+    const double v = 0.5 * w * inv_sq;
+    pot += v * a.vw_y;
+    if (rho > 0.0) e[1] = rho * v * a.vw_y;
+  }
+  if (ev.wt) {
+    double rb_over_rc;
+    if (a.b56) {
+      if (pos) rb_over_rc = rho * z3 * z3 * z2;
+      else { const double rc = kZero; rb_over_rc = sqrt(rc) * cbrt(rc) / rc; }
+    } else {
+      const double rc = rho < kZero ? kZero : rho;
+      rb_over_rc = pow(rc, a.wt_beta) / rc;
+    }
+    const double v = a.two_alpha * rb_over_rc * kc;
+    pot += v;
+    e[2] = v * rho * a.inv_two_alpha;
+  }
+  if (ev.xc) {
+    double eps, vx;
+    pz_lda_ct<double>(rho, eps, vx, true);
+    pot += vx;
+    e[3] = eps * rho;
+  }
+  if (ev.hartree) {
+    pot += vh;
+    e[4] = 0.5 * vh * rho;
+  }
+  if (ev.pp) {
+    pot += vl;
+    e[5] = vl * rho;
+  }
+}
+
+// (b (1 + t))^p - b^p = bp expm1(p L) for bp = b^p, L = log1p(t): FP32 with
+// the relative accuracy of FP32 in the change
+__device__ __forceinline__ float pdelta(float bp, float L, float p) { return bp * expm1f(p * L); }
+
+// Inverse row pass (C2R of the transformed changes) + the pointwise terms as
+// changes against the reference evaluation: with L = log1p((rho - rho_ref)
+// / rho_ref), every power law of rho changes by b^p expm1(p L); products
+// change by d(uv) = du v + u0 dv; the PZ81 correlation (rs >= 1: N(s) /
+// D(s)^2 and g / D(s), s = sqrt(rs)) by the exact rational-function
+// differences in ds = s - s0, and (rs < 1) through d ln rs = -L / 3.  All of
+// it in FP32, accurate to FP32 in the change, added to the reference
+// potential in FP64; energies as FP32 per-thread sums of the changes.  Points
+// with rho or rho_ref at the 1e-30 clamp, or with rs on different sides of 1
+// (or within 1e-5 of it), take the FP64 epilogue at both densities.
 template <int N, bool WANT_E>
 __global__ void __launch_bounds__(rows_threads_max<float, N>(), GB_CT_ROWS_MINB) k_delta_rows_inv_eval(DeltaRowsInv a) {
   constexpr int RP = RowsCfg<float>::RP, NP = Pad<float, N>::NP;
@@ -125,7 +191,13 @@ __global__ void __launch_bounds__(rows_threads_max<float, N>(), GB_CT_ROWS_MINB)
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
   const cpx<float>* res = ct_rows_inv_lines<float, N, true>(a.c, base, tw, A, B);
   const EvalDesc& ev = a.ev;
-  double es[6] = {0, 0, 0, 0, 0, 0};
+  constexpr float cx = 0.98474502184269654115f;           // (3/pi)^(1/3)
+  constexpr float RSC = 0.62035049089940001667f;          // (3/(4 pi))^(1/3)
+  constexpr float la = 0.0311f, lb = -0.048f, lc = 0.0020f, ld = -0.0116f;
+  constexpr float lg = -0.1423f, lb1 = 1.0529f, lb2 = 0.3334f;
+  const float tf_v = (float)a.tf_v, tf_e = (float)a.tf_e, vw_y = (float)a.vw_y;
+  const float two_alpha = (float)a.two_alpha, beta = (float)a.wt_beta;
+  float es[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
   for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
     const int rr = idx / N, j = idx % N;
@@ -134,70 +206,126 @@ __global__ void __launch_bounds__(rows_threads_max<float, N>(), GB_CT_ROWS_MINB)
     const int64_t gidx = row * N + j;
     const int pr = rr >> 1;
     const bool odd = rr & 1;
-    const double rho = __ldg(a.rho + gidx);
-    auto conv = [&](int slot) {
-      const cpx<float> zz = res[sw<float, NP>(slot * RP + pr, j)];
-      return __ldg(a.cref + slot * a.cstride + gidx) + (double)(odd ? zz.y : zz.x);
-    };
-    const bool pos = rho > kZero;
-    double z3 = 0.0, z2 = 0.0;
-    if (pos) { z3 = rcbrt_d(rho); z2 = rsqrt_d(rho); }
-    double pot = 0.0;
-    if (ev.tf) {
-      const double r23 = pos ? rho * z3 : cbrt(rho * rho);
-      pot += a.tf_v * r23;
-      if (WANT_E) {
-        double r53;
-        if (pos) r53 = rho * rho * z3;
-        else { double r5 = rho * rho; r5 = r5 * rho; r5 = r5 * rho; r5 = r5 * rho; r53 = cbrt(r5); }
-        es[0] += r53 * a.tf_e;
-      }
-    }
+    const double rho = __ldg(a.rho + gidx), rho0 = __ldg(a.rho_ref + gidx);
+    // transformed changes of the convolutions and their reference values
+    float dw = 0.f, dkc = 0.f, dvh = 0.f;
+    double w0 = 0.0, kc0 = 0.0, vh0 = 0.0;
     if (ev.vw) {
-      const double w = conv(ev.slot_vw);
-      const double inv_sq = pos ? z2 : (rho > 0.0 ? 1.0 / fmax(sqrt(rho), kZero) : 1e15);
-      const double v = 0.5 * w * inv_sq;
-      pot += v * a.vw_y;
-      if (WANT_E && rho > 0.0) es[1] += rho * v * a.vw_y;
+      const cpx<float> zz = res[sw<float, NP>(ev.slot_vw * RP + pr, j)];
+      dw = odd ? zz.y : zz.x;
+      w0 = __ldg(a.cref + ev.slot_vw * a.cstride + gidx);
     }
     if (ev.wt) {
-      const double kc = conv(ev.slot_wt);
-      double rb_over_rc;
-      if (a.b56) {
-        if (pos) rb_over_rc = rho * z3 * z3 * z2;
-        else { const double rc = kZero; rb_over_rc = sqrt(rc) * cbrt(rc) / rc; }
-      } else {
-        const double rc = rho < kZero ? kZero : rho;
-        rb_over_rc = pow(rc, a.wt_beta) / rc;
-      }
-      const double v = a.two_alpha * rb_over_rc * kc;
-      pot += v;
-      if (WANT_E) es[2] += v * rho * a.inv_two_alpha;
-    }
-    if (ev.xc) {
-      double eps, vx;
-      pz_lda_ct<double>(rho, eps, vx, WANT_E);
-      pot += vx;
-      if (WANT_E) es[3] += eps * rho;
+      const cpx<float> zz = res[sw<float, NP>(ev.slot_wt * RP + pr, j)];
+      dkc = odd ? zz.y : zz.x;
+      kc0 = __ldg(a.cref + ev.slot_wt * a.cstride + gidx);
     }
     if (ev.hartree) {
-      const double vh = conv(ev.slot_h);
-      pot += vh;
-      if (WANT_E) es[4] += 0.5 * vh * rho;
+      const cpx<float> zz = res[sw<float, NP>(ev.slot_h * RP + pr, j)];
+      dvh = odd ? zz.y : zz.x;
+      vh0 = __ldg(a.cref + ev.slot_h * a.cstride + gidx);
     }
-    if (ev.pp) {
-      const double vl = __ldg(a.vloc + gidx);
-      pot += vl;
-      if (WANT_E) es[5] += vl * rho;
+    const double vl = ev.pp ? __ldg(a.vloc + gidx) : 0.0;
+    // fast path: both densities above the clamp, LDA branch the same on both
+    bool fast = rho > kZero && rho0 > kZero;
+    const float r0 = (float)rho0, dr = (float)(rho - rho0);
+    float L = 0.f, z3 = 0.f, z2 = 0.f, rs0 = 0.f, drs = 0.f;
+    if (fast) {
+      L = log1pf(dr / r0);
+      z3 = rcbrtf(r0);
+      z2 = rsqrtf(r0);
+      rs0 = RSC * z3;
+      drs = pdelta(rs0, L, -1.0f / 3.0f);
+      if (ev.xc) {
+        const float rs = rs0 + drs;
+        if ((rs0 < 1.f) != (rs < 1.f) || fabsf(rs0 - 1.f) < 1e-5f || fabsf(rs - 1.f) < 1e-5f) fast = false;
+      }
     }
-    a.pot[gidx] = pot;
+    if (!fast) {
+      double e1[6], e0[6], p1;
+      point64(a, rho, w0 + (double)dw, kc0 + (double)dkc, vh0 + (double)dvh, vl, p1, e1);
+      a.pot[gidx] = p1;
+      if (WANT_E) {
+        double p0;
+        point64(a, rho0, w0, kc0, vh0, vl, p0, e0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) es[k] += (float)(e1[k] - e0[k]);
+      }
+      continue;
+    }
+    const float r = r0 + dr;                          // rho (FP32, for the small products)
+    const float c13 = r0 * z3 * z3;                   // rho0^(1/3)
+    float dpot = 0.f;
+    if (ev.tf) {
+      dpot += tf_v * pdelta(r0 * z3, L, 2.0f / 3.0f);               // rho^(2/3)
+      if (WANT_E) es[0] += tf_e * pdelta(r0 * r0 * z3, L, 5.0f / 3.0f);
+    }
+    if (ev.vw) {
+      // v = (1/2) w rho^(-1/2); e = (1/2) w rho^(1/2)
+      const float wr = (float)w0;
+      const float dzm = pdelta(z2, L, -0.5f);
+      dpot += 0.5f * vw_y * (dw * (z2 + dzm) + wr * dzm);
+      if (WANT_E) {
+        const float q0 = r0 * z2, dq = pdelta(q0, L, 0.5f);
+        es[1] += 0.5f * vw_y * (dw * (q0 + dq) + wr * dq);
+      }
+    }
+    if (ev.wt) {
+      // v = 2 alpha rho^(beta - 1) kc; e = rho^beta kc
+      const float kr = (float)kc0;
+      const float y0 = a.b56 ? z2 * c13 : powf(r0, beta - 1.0f);
+      const float dy = pdelta(y0, L, beta - 1.0f);
+      dpot += two_alpha * (dkc * (y0 + dy) + kr * dy);
+      if (WANT_E) {
+        const float q0 = r0 * y0, dq = pdelta(q0, L, beta);
+        es[2] += dkc * (q0 + dq) + kr * dq;
+      }
+    }
+    if (ev.xc) {
+      // exchange: v = -cx rho^(1/3), e = -(3/4) cx rho^(4/3)
+      dpot += -cx * pdelta(c13, L, 1.0f / 3.0f);
+      float de = 0.f;
+      if (WANT_E) de = -0.75f * cx * pdelta(r0 * c13, L, 4.0f / 3.0f);
+      float dvc, dec, ec0;
+      if (rs0 >= 1.f) {
+        // vc = N / D^2, ec = g / D; N = g + a1 s + a2 s^2, D = 1 + b1 s + b2 s^2
+        constexpr float a1 = 7.0f / 6.0f * lg * lb1, a2 = 4.0f / 3.0f * lg * lb2;
+        const float s0 = sqrtf(rs0);
+        const float ds = pdelta(s0, L, -1.0f / 6.0f);
+        const float s = s0 + ds;
+        const float N0 = lg + a1 * s0 + a2 * s0 * s0;
+        const float D0 = 1.0f + lb1 * s0 + lb2 * s0 * s0;
+        const float E = lb1 + lb2 * (s + s0);
+        const float Ap = a1 + a2 * (s + s0);
+        const float D = D0 + ds * E;
+        dvc = ds * (Ap * D0 * D0 - N0 * E * (2.0f * D0 + ds * E)) / (D * D * D0 * D0);
+        dec = -lg * ds * E / (D * D0);
+        ec0 = lg / D0;
+      } else {
+        // vc = a ln rs + b - a/3 + (2/3) c rs ln rs + (2d - c)/3 rs
+        const float dln = -L / 3.0f;
+        const float ln0 = logf(rs0);
+        const float drsln = (rs0 + drs) * dln + drs * ln0;
+        dvc = la * dln + (2.0f / 3.0f) * lc * drsln + (2.0f * ld - lc) / 3.0f * drs;
+        dec = la * dln + lc * drsln + ld * drs;
+        ec0 = la * ln0 + lb + lc * rs0 * ln0 + ld * rs0;
+      }
+      dpot += dvc;
+      if (WANT_E) es[3] += de + dec * r + ec0 * dr;
+    }
+    if (ev.hartree) {
+      dpot += dvh;
+      if (WANT_E) es[4] += 0.5f * (dvh * r + (float)vh0 * dr);
+    }
+    if (ev.pp && WANT_E) es[5] += (float)vl * dr;
+    a.pot[gidx] = __ldg(a.pot_ref + gidx) + (double)dpot;
   }
   if constexpr (!WANT_E) return;
   __shared__ double red[32][6];
   const int lane32 = tid & 31, warp = tid >> 5;
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
-    const double v = warp_sum(es[c]);
+    const double v = warp_sum((double)es[c]);
     if (lane32 == 0) red[warp][c] = v;
   }
   __syncthreads();
@@ -241,8 +369,9 @@ int gb_delta_rows_fwd(gbofdft_plan* p, const double* rho, const double* rho_ref,
 }
 
 int gb_delta_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, const EvalDesc* ev,
-                           const double* rho, const double* vloc, const double* cref, int64_t cstride, double* pot,
-                           int calc_e, double* partials, int64_t* nblk_out, cudaStream_t st) {
+                           const double* rho, const double* rho_ref, const double* pot_ref, const double* vloc,
+                           const double* cref, int64_t cstride, double* pot, int calc_e, double* partials,
+                           int64_t* nblk_out, cudaStream_t st) {
   using namespace gbct;
   int rc = 1;
   ct_dispatch(p->n[2], [&](auto nc) {
@@ -253,7 +382,8 @@ int gb_delta_rows_inv_eval(gbofdft_plan* p, const void* spec, int64_t fstride, i
     a.c.in = spec; a.c.fstride = fstride; a.c.nrows = p->n[0] * p->n[1]; a.c.ld2 = 0; a.c.nf = nf;
     a.c.tw = p->tw[2];
     a.ev = *ev;
-    a.rho = rho; a.vloc = vloc; a.cref = cref; a.cstride = cstride; a.pot = pot; a.partials = partials;
+    a.rho = rho; a.rho_ref = rho_ref; a.pot_ref = pot_ref; a.vloc = vloc; a.cref = cref; a.cstride = cstride;
+    a.pot = pot; a.partials = partials;
     const double ctf = 2.87123400018819181594;    // (3/10)(3 pi^2)^(2/3)
     a.tf_v = 5.0 / 3.0 * ctf * ev->tf_x;
     a.tf_e = ctf * ev->tf_x;

@@ -101,16 +101,17 @@ int gb_ct_cols_f64(gbofdft_plan*, void*, int64_t, int, int, int, int, double, co
 int gb_delta_rows_fwd(gbofdft_plan* p32, const double* rho, const double* rho_ref, void* spec, int64_t fstride,
                       int nf, const int* ops, double beta, cudaStream_t st);
 int gb_delta_rows_inv_eval(gbofdft_plan* p32, const void* spec, int64_t fstride, int nf, const EvalDesc* ev,
-                           const double* rho, const double* vloc, const double* cref, int64_t cstride, double* pot,
-                           int calc_e, double* partials, int64_t* nblk, cudaStream_t st);
+                           const double* rho, const double* rho_ref, const double* pot_ref, const double* vloc,
+                           const double* cref, int64_t cstride, double* pot, int calc_e, double* partials,
+                           int64_t* nblk, cudaStream_t st);
 int gb_delta_supported(int n0, int n1, int n2);
 // the whole delta evaluation of the fused terms (passes.cu): plane pipeline
 // of p32 on the changes, FP64 epilogue into pot / energies (energies use p64's
 // partials and dV)
 int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
-                       const double* cref, int nf, const int* ops, double beta, const KerDesc& kd,
-                       const EvalDesc& ev, const double* vloc, double* pot, int calc_e, double* energies,
-                       cudaStream_t st);
+                       const double* pot_ref, const double* eref, const double* cref, int nf, const int* ops,
+                       double beta, const KerDesc& kd, const EvalDesc& ev, const double* vloc, double* pot,
+                       int calc_e, double* energies, cudaStream_t st);
 // the reference density of a delta-evaluation state (device, N doubles)
 const double* gb_delta_ref(const gbofdft_delta* d);
 void gb_count_launch();

@@ -108,12 +108,15 @@ def _lat(nr):
     return np.diag([0.24 * n + 1.0 for n in nr])
 
 
-@pytest.mark.parametrize("nr", [(128, 128, 128), (64, 96, 128)])
+@pytest.mark.parametrize("nr,scale", [((128, 128, 128), 1.0), ((64, 96, 128), 1.0), ((64, 64, 64), 14.0)])
 @pytest.mark.parametrize("eps", [1e-5, 1e-3])
-def test_delta_matches_full_fp64(lib, nr, eps):
+def test_delta_matches_full_fp64(lib, nr, scale, eps):
+    """scale 14: densities 0.07-0.5, both PZ81 branches (r_s < 1 above
+    rho = 0.239) and points whose r_s crosses 1 (the FP64 path at both
+    densities)."""
     torch = pytest.importorskip("torch")
     s = _Setup(lib, nr, _lat(nr))
-    ra = _density(nr)
+    ra = scale * _density(nr)
     rb = ra * (1.0 + _change(nr, eps))
     rho_a = torch.tensor(ra, dtype=torch.float64, device="cuda")
     rho_b = torch.tensor(rb, dtype=torch.float64, device="cuda")

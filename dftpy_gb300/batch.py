@@ -66,7 +66,7 @@ def _natoms(total):
     return 1
 
 
-def _solve_one(job, options, stream):
+def _solve_one(job, options, stream, guess=None):
     total, rho0, name = job
     t0 = time.perf_counter()
     o = dict(options)
@@ -74,6 +74,8 @@ def _solve_one(job, options, stream):
     if "econv" not in o:
         o["econv"] = per_atom * _natoms(total)
     with torch.cuda.stream(stream):
+        if guess is not None:
+            rho0 = guess.guess(total, rho0.grid)
         opt = Optimization(EnergyEvaluator=total, optimization_method="TN", optimization_options=o)
         rho = opt.optimize_rho(guess_rho=rho0)
         energy = float(opt.energy)
@@ -82,10 +84,12 @@ def _solve_one(job, options, stream):
                        wall_s=time.perf_counter() - t0, name=name)
 
 
-def optimize_batch(jobs, workers=None, options=None, kedf="WGC", **kedf_options):
+def optimize_batch(jobs, workers=None, options=None, kedf="WGC", guess=None, **kedf_options):
     """Optimise every job; ``workers`` structures are in flight at a time
     (default: all of them, at most 16).  Jobs are ``(evaluator, guess_rho)``
-    pairs or ``systems.Structure`` objects."""
+    pairs or ``systems.Structure`` objects.  ``guess``: a
+    ``guess.LearnedGuess`` whose starting density replaces each job's (made
+    on the job's stream)."""
     _lib.require_cuda()
     opts = dict(DEFAULT_OPTIONS)
     opts.update(options or {})
@@ -104,6 +108,10 @@ def optimize_batch(jobs, workers=None, options=None, kedf="WGC", **kedf_options)
     streams = [torch.cuda.Stream() for _ in range(workers)]
     slots = list(range(workers))
     lock = threading.Lock()
+    if guess is not None:
+        # the network's lazily packed weights are made once, here, not by
+        # racing worker threads
+        guess.prepare(prepared[0][0], prepared[0][1].grid)
     # set-up work queued on the default stream (device copies of the inputs)
     # must be complete before other streams read it
     torch.cuda.synchronize()
@@ -112,7 +120,7 @@ def optimize_batch(jobs, workers=None, options=None, kedf="WGC", **kedf_options)
         with lock:
             k = slots.pop()
         try:
-            return _solve_one(job, opts, streams[k])
+            return _solve_one(job, opts, streams[k], guess)
         finally:
             with lock:
                 slots.append(k)
@@ -137,9 +145,17 @@ def main():
     p.add_argument("--precision", default="mixed")
     p.add_argument("--sequential", type=int, default=8, help="also time this many jobs one after another")
     p.add_argument("--check", type=int, default=4, help="solve this many in plain FP64 and report the error")
+    p.add_argument("--guess", default="uniform", choices=["uniform", "learned"],
+                   help="starting densities (learned: data/guessnet.npz, trained on Al/Mg WGC cells)")
     a = p.parse_args()
     sts = alloy_batch(a.n)
     opts = {"precision": a.precision}
+    lg = None
+    if a.guess == "learned":
+        import os
+        from .guess import GuessNet, LearnedGuess
+        lg = LearnedGuess(GuessNet.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                                                     "guessnet.npz")))
     # warm-up: one small solve per distinct grid (plans, tables, kernels)
     seen = set()
     warm = []
@@ -147,11 +163,11 @@ def main():
         if st.nr not in seen:
             seen.add(st.nr)
             warm.append(st)
-    optimize_batch(warm, workers=len(warm), options=opts, kedf=a.kedf)
+    optimize_batch(warm, workers=len(warm), options=opts, kedf=a.kedf, guess=lg)
     jobs = [build_evaluator(st, kedf=a.kedf) for st in sts]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = optimize_batch(jobs, workers=a.workers, options=opts)
+    res = optimize_batch(jobs, workers=a.workers, options=opts, guess=lg)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     seq = None
@@ -159,7 +175,7 @@ def main():
         jobs2 = [build_evaluator(st, kedf=a.kedf) for st in sts[:a.sequential]]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        res2 = optimize_batch(jobs2, workers=1, options=opts)
+        res2 = optimize_batch(jobs2, workers=1, options=opts, guess=lg)
         t_seq = time.perf_counter() - t1
         same = all(r.energy == q.energy for r, q in zip(res2, res[:a.sequential]))
         seq = {"n": a.sequential, "wall_s": t_seq, "per_structure_s": t_seq / a.sequential,
@@ -169,7 +185,9 @@ def main():
         ref = optimize_batch(sts[:a.check], workers=a.check, options={"precision": "fp64"}, kedf=a.kedf)
         err = [abs(r.energy - q.energy) / st.nat * 27.211386024367243 for r, q, st in zip(res, ref, sts)]
         check = {"n": a.check, "max_abs_dE_eV_per_atom": max(err), "fp64_converged": sum(q.converged == 0 for q in ref)}
-    print(json.dumps({"n": a.n, "workers": a.workers, "kedf": a.kedf, "precision": a.precision,
+    print(json.dumps({"n": a.n, "workers": a.workers, "kedf": a.kedf, "precision": a.precision, "guess": a.guess,
+                      "evaluations": sum(sum(s_["n_eval_ev"] + s_["n_eval_v"] + s_.get("n_eval_hess", 0)
+                                             for s_ in r.stats["stages"]) for r in res),
                       "wall_s": t_batch, "structures_per_s": a.n / t_batch,
                       "converged": sum(1 for r in res if r.converged == 0),
                       "natoms": [len(st.symbols) for st in sts], "grids": sorted({st.nr for st in sts}),

@@ -358,6 +358,13 @@ class LearnedGuess:
     def __init__(self, net):
         self.net = net
 
+    def prepare(self, total, grid=None):
+        """Make the network's packed tensor-core weights (and the cached
+        set-up of the features) by one guess on the current stream; callers
+        that guess from several threads call this first."""
+        self.guess(total, grid)
+        torch.cuda.synchronize()
+
     def guess(self, total, grid=None, dtype=torch.float64):
         from .field import DirectField
         grid = grid or total.PSEUDO.grid

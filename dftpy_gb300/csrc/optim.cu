@@ -226,10 +226,21 @@ static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Page-locked landing buffer of the scalar read-back, one per host thread
+// (a copy into pageable memory is staged by the driver and costs more than
+// the copy itself on every one of a solve's ~70 synchronisations).
+static thread_local double* g_pinned_sc = nullptr;
+
 static int ts_sync(TnState& s) {
   const double t0 = now_s();
-  GB_CUDA(cudaMemcpyAsync(s.host, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
+  if (!g_pinned_sc) {
+    void* ptr = nullptr;
+    GB_CUDA(cudaMallocHost(&ptr, sizeof(double) * S_COUNT));
+    g_pinned_sc = reinterpret_cast<double*>(ptr);
+  }
+  GB_CUDA(cudaMemcpyAsync(g_pinned_sc, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
   GB_CUDA(cudaStreamSynchronize(s.st));
+  memcpy(s.host, g_pinned_sc, sizeof(double) * S_COUNT);
   s.t_sync += now_s() - t0;
   ++s.n_sync;
   if (s.time_evals) evt_drain();

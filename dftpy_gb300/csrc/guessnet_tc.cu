@@ -435,31 +435,35 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __
   }
 }
 
+// the dynamic shared-memory attribute of a kernel, set once per device (the
+// plans' registry of granted sizes, shared with the other passes)
+template <typename K>
+int tc_smem(K kern, int bytes) {
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  const void* key = reinterpret_cast<const void*>(kern);
+  if (gb_smem_granted(key, dev) >= bytes) return 0;
+  GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  gb_smem_grant(key, dev, bytes);
+  return 0;
+}
+
 template <int CIN, int COUT>
 int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, float* out, int D, int H, int W, int act,
               const float* skip, int up, int nstore, int* err, cudaStream_t st) {
   using C = TcCfg<CIN, COUT>;
-  static int granted[64] = {0};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 64 && !granted[dev]) {
-    GB_CUDA(cudaFuncSetAttribute(k_conv3d_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    granted[dev] = 1;
-  }
-  const int ntiles = (W / 8) * (H / 16) * D;
+  int rc = 0;
   if constexpr (C::SLABS == 1) {
     // z-pipelined kernel: a CTA walks a column of tiles along z
     using Z = TczCfg<CIN, COUT>;
-    static int zgranted[64] = {0}, nsms[64] = {0};
-    if (dev < 64 && !zgranted[dev]) {
-      GB_CUDA(cudaFuncSetAttribute(k_conv3d_tcz<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
-      GB_CUDA(cudaDeviceGetAttribute(&nsms[dev], cudaDevAttrMultiProcessorCount, dev));
-      zgranted[dev] = 1;
-    }
+    if ((rc = tc_smem(k_conv3d_tcz<CIN, COUT>, Z::SMEM))) return rc;
+    int dev = 0, nsm = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     // about 8 CTAs per SM: z chunks of the columns (a chunk of zc planes
     // loads zc + 2 input planes)
     const int ncol = (W / 8) * (H / 16);
-    const int target = 8 * (dev < 64 && nsms[dev] > 0 ? nsms[dev] : 152);
+    const int target = 8 * (nsm > 0 ? nsm : 152);
     int nchunk = (target + ncol - 1) / ncol;
     if (nchunk < 1) nchunk = 1;
     if (nchunk > D) nchunk = D;
@@ -468,6 +472,8 @@ int launch_tc(const float* in, const __nv_bfloat16* wpk, const float* bias, floa
     k_conv3d_tcz<CIN, COUT><<<ncol * nchunk, kTcThreads, Z::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up,
                                                                       nstore, zc, err);
   } else {
+    if ((rc = tc_smem(k_conv3d_tc<CIN, COUT>, C::SMEM))) return rc;
+    const int ntiles = (W / 8) * (H / 16) * D;
     k_conv3d_tc<CIN, COUT><<<ntiles, kTcThreads, C::SMEM, st>>>(in, wpk, bias, out, D, H, W, act, skip, up, nstore,
                                                                  err);
   }

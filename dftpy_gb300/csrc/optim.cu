@@ -15,6 +15,8 @@
 #include <string.h>
 
 #include <chrono>
+#include <mutex>
+#include <vector>
 
 #include "dcsrch.h"
 #include "plan.h"
@@ -226,21 +228,51 @@ static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Page-locked landing buffer of the scalar read-back, one per host thread
-// (a copy into pageable memory is staged by the driver and costs more than
-// the copy itself on every one of a solve's ~70 synchronisations).
-static thread_local double* g_pinned_sc = nullptr;
+// Page-locked landing buffers of the scalar read-back, one per host thread
+// while it lives (a copy into pageable memory is staged by the driver and
+// costs more than the copy itself on every one of a solve's ~70
+// synchronisations).  Buffers of exited threads go back to a pool, so
+// short-lived worker threads do not allocate page-locked memory each time.
+static std::mutex g_pin_mu;
+static std::vector<double*> g_pin_free;
+
+struct PinnedScalars {
+  double* p = nullptr;
+  ~PinnedScalars() {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    g_pin_free.push_back(p);
+  }
+};
+static thread_local PinnedScalars g_pinned;
+
+static int pinned_scalars(double** out) {
+  if (!g_pinned.p) {
+    {
+      std::lock_guard<std::mutex> lk(g_pin_mu);
+      if (!g_pin_free.empty()) {
+        g_pinned.p = g_pin_free.back();
+        g_pin_free.pop_back();
+      }
+    }
+    if (!g_pinned.p) {
+      void* ptr = nullptr;
+      GB_CUDA(cudaMallocHost(&ptr, sizeof(double) * S_COUNT));
+      g_pinned.p = reinterpret_cast<double*>(ptr);
+    }
+  }
+  *out = g_pinned.p;
+  return 0;
+}
 
 static int ts_sync(TnState& s) {
   const double t0 = now_s();
-  if (!g_pinned_sc) {
-    void* ptr = nullptr;
-    GB_CUDA(cudaMallocHost(&ptr, sizeof(double) * S_COUNT));
-    g_pinned_sc = reinterpret_cast<double*>(ptr);
-  }
-  GB_CUDA(cudaMemcpyAsync(g_pinned_sc, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
+  double* pin = nullptr;
+  int rc = pinned_scalars(&pin);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(pin, s.w.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s.st));
   GB_CUDA(cudaStreamSynchronize(s.st));
-  memcpy(s.host, g_pinned_sc, sizeof(double) * S_COUNT);
+  memcpy(s.host, pin, sizeof(double) * S_COUNT);
   s.t_sync += now_s() - t0;
   ++s.n_sync;
   if (s.time_evals) evt_drain();

@@ -29,6 +29,9 @@ pseudo_files.npz  reciprocal tables of the reference's example pseudopotential
              stand-in in ``_shims`` for UPF).
 dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
              (``LineSearchDcsrch2``) on analytic 1-D functions.
+gaas.npz     the reference's own TN test (GaAs_random, recpot pseudopotentials,
+             WT + LDA + Hartree, PME): structure, full reciprocal PP tables,
+             converged energy and forces.
 """
 import os
 import sys
@@ -467,7 +470,43 @@ def gen_dcsrch():
     print("dcsrch: %d cases" % len(cases))
 
 
-GENERATORS = {"fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files, "formats": gen_formats, "gridmap": gen_gridmap}
+def gen_gaas():
+    """The reference's own TN test (``test_density_opt.py:15-46``): GaAs_random
+    (5 Ga + 5 As), recpot pseudopotentials through ReadPseudo, PME, WT + LDA +
+    Hartree, grid from ecut2nr(spacing=0.4), econv 1e-6 * nat; the structure,
+    the full reciprocal tables the reference builds, the converged energy and
+    forces."""
+    from dftpy.functional.pseudo import ReadPseudo
+    from dftpy.math_utils import ecut2nr
+    ions = io.read(refenv.REF_DATA / "GaAs_random.vasp", names=["Al"])
+    files = {"Ga": refenv.REF_DATA / "Ga_lda.oe04.recpot", "As": refenv.REF_DATA / "As_lda.oe04.recpot"}
+    nr = ecut2nr(lattice=ions.cell, spacing=0.4)
+    grid = DirectGrid(lattice=ions.cell, nr=nr, full=False)
+    rho_ini = DirectField(grid=grid)
+    pseudo = LocalPseudo(grid=grid, ions=ions, PP_list=files, PME=True)
+    total = TotalFunctional(KineticEnergyFunctional=Functional(type="KEDF", name="WT", optional_kwargs={}),
+                            XCFunctional=Functional(type="XC", name="LDA"),
+                            HARTREE=Functional(type="HARTREE"), PSEUDO=pseudo)
+    rho_ini[:] = ions.get_ncharges() / ions.cell.volume
+    opt = Optimization(EnergyEvaluator=total, optimization_method="TN",
+                       optimization_options={"econv": 1e-6 * ions.nat, "maxfun": 50, "maxiter": 100})
+    t0 = time.time()
+    rho = opt.optimize_rho(guess_rho=rho_ini)
+    e_final = float(total.Energy(rho=rho, ions=ions, usePME=True))
+    out = {"lattice": np.array(ions.cell.array if hasattr(ions.cell, "array") else ions.cell, dtype=float),
+           "positions": np.array(ions.positions, dtype=float), "symbols": np.array(list(ions.symbols)),
+           "nr": np.array(nr), "E_final": e_final, "forces": total.get_forces(rho, ions=ions),
+           "nelec": float(ions.get_ncharges())}
+    rp = ReadPseudo({k: str(v) for k, v in files.items()})
+    for k in files:
+        out[k + "_gp"] = np.asarray(rp._gp[k], dtype=float)
+        out[k + "_vp"] = np.asarray(rp._vp[k], dtype=float)
+        out[k + "_zval"] = float(rp._zval[k])
+    np.savez_compressed(HERE / "gaas.npz", **out)
+    print("gaas: nr %s E=%.10f (reference test asserts -43.3046), %.1f s" % (list(nr), e_final, time.time() - t0))
+
+
+GENERATORS = {"gaas": gen_gaas, "fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files, "formats": gen_formats, "gridmap": gen_gridmap}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

@@ -135,6 +135,44 @@ def alloy_batch(n=64, seed0=0, **kw):
     return [systems.config_alloy(seed0 + i, **kw) for i in range(n)]
 
 
+def structure_cost(st):
+    """Work estimate of one structure's solve: its number of grid points."""
+    return int(np.prod(st.nr))
+
+
+def partition_lpt(costs, nparts):
+    """Longest-processing-time assignment of independent items to ``nparts``
+    ranks: items in decreasing cost (ties by index), each to the rank with
+    the smallest load so far (ties to the lower rank).  Deterministic, so
+    every rank computes the same partition without communicating.  Returns
+    (parts, loads): per rank the item indices in increasing order, and its
+    total cost.  The largest load is at most 4/3 of the optimum."""
+    nparts = int(nparts)
+    if nparts < 1:
+        raise ValueError("nparts must be >= 1")
+    costs = [float(c) for c in costs]
+    if any(c < 0 for c in costs):
+        raise ValueError("costs must be non-negative")
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    parts = [[] for _ in range(nparts)]
+    loads = [0.0] * nparts
+    for i in order:
+        k = min(range(nparts), key=lambda r: (loads[r], r))
+        parts[k].append(i)
+        loads[k] += costs[i]
+    return [sorted(p) for p in parts], loads
+
+
+def shard(structures, rank, world, cost=structure_cost):
+    """The structures rank ``rank`` of ``world`` optimises (``partition_lpt``
+    on ``cost``), with their indices in the batch.  Structures are
+    independent, so ranks need no collective on the data path; results are
+    gathered by index on the host."""
+    parts, _ = partition_lpt([cost(s) for s in structures], world)
+    idx = parts[int(rank)]
+    return idx, [structures[i] for i in idx]
+
+
 def main():
     import argparse
     import json

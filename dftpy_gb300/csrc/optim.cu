@@ -519,6 +519,12 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     }, S_A, st);
     if (rc) return rc;
     if ((rc = ts_sync(s))) return rc;
+    // a density with NaN/Inf values or without electrons has no solution:
+    // report it instead of iterating on it (the sums are on the host already)
+    if (!isfinite(s.host[S_A]) || !isfinite(s.host[S_B]) || !(s.host[S_A] > 0.0) || !(s.host[S_B] > 0.0))
+      return gb_set_error(GBOFDFT_ERR_NUMERIC,
+                          "optimize_tn: the initial density has non-finite values or no electrons "
+                          "(sum rho = %g, sum phi^2 = %g)", s.host[S_A], s.host[S_B]);
     const T fac = (T)sqrt(s.host[S_A] / s.host[S_B]);
     if (o.precond) {
       // preconditioner of the uniform gas at the mean density
@@ -551,6 +557,9 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
     if ((r = ts_sync(s))) return r;
     energy = s.host[S_EN + GB_E_TOTAL];
     mu = (s.host[S_A] * dV) / (s.host[S_B] * dV);
+    if (!isfinite(energy) || !isfinite(mu))
+      return gb_set_error(GBOFDFT_ERR_NUMERIC, "optimize_tn: non-finite energy (%g) or chemical potential (%g)",
+                          energy, mu);
     const T muT = (T)mu;
     T* res0 = F<T>(s, F_RES0);
     r = launch_mr<1, T>(w, N, [=] __device__(int64_t i, T* c) {

@@ -17,7 +17,7 @@ Hermitian-averaged half spectrum).
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, torch_ops
 from .grid import DirectGrid, ReciprocalGrid
 
 
@@ -91,7 +91,11 @@ def _as_tensor(data, shape, dtype, cplx):
         t = data.to(device="cuda", dtype=dtype)
     else:
         t = torch.as_tensor(np.ascontiguousarray(np.asarray(data)), device="cuda").to(dtype)
-    return t.reshape(tuple(int(x) for x in shape)).contiguous()
+    shape = tuple(int(x) for x in shape)
+    if t.numel() != int(np.prod(shape)):
+        # a buffer of the wrong size never reaches the library
+        raise ValueError("field data has %d values, the grid needs %s = %d" % (t.numel(), shape, int(np.prod(shape))))
+    return t.reshape(shape).contiguous()
 
 
 class DirectField(BaseField):
@@ -138,9 +142,7 @@ class DirectField(BaseField):
             raise NotImplementedError("fft of rank>1 fields")
         plan = g.plan(self.dtype)
         x = self.as_subclass(torch.Tensor).contiguous()
-        cdt = torch.complex128 if self.dtype == torch.float64 else torch.complex64
-        out = torch.empty((int(g.nrR[0]), int(g.nrR[1]), int(g.nrR[2]) // 2 + 1), dtype=cdt, device="cuda")
-        _lib.check(_lib.load().gbofdft_fft_r2c(plan.handle, _lib.ptr(x), _lib.ptr(out), _lib.stream_ptr()), "fft")
+        out = torch.ops.gbofdft.fft_r2c(x, torch_ops.handle(plan))
         if g.full:
             out = _hermitian_extend(out, int(g.nrR[2]))
         return ReciprocalField(g.get_reciprocal(), data=out)
@@ -199,6 +201,5 @@ class ReciprocalField(BaseField):
         X = X.contiguous()
         rdt = torch.float64 if X.dtype == torch.complex128 else torch.float32
         plan = dg.plan(rdt)
-        out = torch.empty(tuple(int(x) for x in dg.nrR), dtype=rdt, device="cuda")
-        _lib.check(_lib.load().gbofdft_fft_c2r(plan.handle, _lib.ptr(X), _lib.ptr(out), _lib.stream_ptr()), "ifft")
+        out = torch.ops.gbofdft.fft_c2r(X, torch_ops.handle(plan), n2)
         return DirectField(dg, data=out)

@@ -3,7 +3,7 @@ import ctypes
 
 import torch
 
-from .. import _lib
+from .. import _lib, torch_ops
 from ..field import DirectField
 
 
@@ -89,12 +89,10 @@ def evaluate(rho, spec, calcType):
     for name, t in (("wt_kernel", spec.wt_kernel), ("vloc", spec.vloc)):
         if t is not None and t.dtype != rho.dtype:
             raise TypeError("%s has dtype %s, density %s" % (name, t.dtype, rho.dtype))
-    pot = torch.empty_like(r)
     want_e = "E" in calcType or "D" in calcType
-    en = torch.empty(_lib.NE, dtype=torch.float64, device="cuda") if want_e else None
     f = spec.ctypes()
     calc = _lib.CALC_V | (_lib.CALC_E if want_e else 0)
-    _lib.check(_lib.load().gbofdft_eval(plan.handle, _lib.ptr(r), f, _lib.ptr(pot), _lib.ptr(en), calc,
-                                        _lib.stream_ptr()), "eval")
+    # torch.ops.gbofdft.eval: the registered operator over gbofdft_eval
+    pot, en = torch.ops.gbofdft.eval(r, torch_ops.handle(plan), ctypes.addressof(f), calc)
     energies = en.cpu().numpy() if want_e else None
     return energies, DirectField(grid, data=pot)

@@ -23,7 +23,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, torch_ops
 from .field import DirectField
 from .functional.output import FunctionalOutput
 from .functional.total_functional import TotalFunctional
@@ -145,15 +145,16 @@ class Optimization:
         nb = ctypes.c_int64()
         _lib.check(L.gbofdft_tn_workspace_bytes(plan.handle, ctypes.byref(nb)))
         ws = _workspace(grid, rho.dtype, int(nb.value))
-        r = rho.as_subclass(torch.Tensor).contiguous().clone()
+        r = rho.as_subclass(torch.Tensor).contiguous()
         res = _lib.TnResult()
         hist = (ctypes.c_double * 4096)()
         res.history = hist
         res.history_cap = 4096
+        # torch.ops.gbofdft.optimize_tn(_split): the registered operators over
+        # gbofdft_optimize_tn(_split); they return the optimised density
         if hess_rho is None:
-            _lib.check(L.gbofdft_optimize_tn(plan.handle, ctypes.byref(f), _lib.ptr(r), ctypes.byref(opts),
-                                             _lib.aligned_ptr(ws, 256), int(nb.value), ctypes.byref(res),
-                                             _lib.stream_ptr()), "optimize_tn")
+            r = torch.ops.gbofdft.optimize_tn(r, torch_ops.handle(plan), ctypes.addressof(f), ctypes.addressof(opts),
+                                              ws, int(nb.value), ctypes.addressof(res))
         else:
             hplan = grid.plan(hess_rho.dtype)
             hf = self.EnergyEvaluator.spec(hess_rho).ctypes()
@@ -164,10 +165,10 @@ class Optimization:
             if dstate is not None:
                 opts.delta = dstate.handle
                 opts.delta_rtol = float(o["delta_rtol"])
-            _lib.check(L.gbofdft_optimize_tn_split(
-                plan.handle, ctypes.byref(f), hplan.handle, ctypes.byref(hf), _lib.ptr(r), ctypes.byref(opts),
-                _lib.aligned_ptr(ws, 256), int(nb.value), _lib.aligned_ptr(hws, 256), int(hb.value),
-                ctypes.byref(res), _lib.stream_ptr()), "optimize_tn_split")
+            r = torch.ops.gbofdft.optimize_tn_split(r, torch_ops.handle(plan), ctypes.addressof(f),
+                                                    torch_ops.handle(hplan), ctypes.addressof(hf),
+                                                    ctypes.addressof(opts), ws, int(nb.value), hws, int(hb.value),
+                                                    ctypes.addressof(res))
         out = dict(energy=res.energy, mu=res.mu, converged=res.converged, n_iter=res.n_iter,
                    n_eval_ev=res.n_eval_ev, n_eval_v=res.n_eval_v, n_eval_hess=res.n_eval_hess,
                    energies=list(res.energies), history=[hist[i] for i in range(res.n_history)],
@@ -290,14 +291,12 @@ class Optimization:
         return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)
 
 
-_WS = {}
-
-
 def _workspace(grid, dtype, nbytes):
-    """Per-(grid, dtype) device workspace for the optimiser (allocated once)."""
-    key = (id(grid), dtype)
-    t = _WS.get(key)
+    """Per-(grid, dtype) device workspace for the optimiser, kept with the
+    grid's plans (allocated once, freed with the grid)."""
+    key = ("tn_workspace", dtype)
+    t = grid._plans.get(key)
     if t is None or t.numel() * 8 < nbytes + 512:
         t = torch.empty(nbytes // 8 + 64, dtype=torch.float64, device="cuda")
-        _WS[key] = t
+        grid._plans[key] = t
     return t

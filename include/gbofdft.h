@@ -453,7 +453,10 @@ int gbofdft_tn_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
  * truncated Newton in phi = sqrt(rho) with the orthogonal rotation line
  * search.  rho_io: initial density in, optimised density out.  workspace:
  * caller-owned device buffer (256-byte aligned) of gbofdft_tn_workspace_bytes.
- * Synchronises the stream (the control flow needs the scalars).
+ * Synchronises the stream (the control flow needs the scalars).  Returns
+ * GBOFDFT_ERR_NUMERIC when the initial density holds NaN/Inf or no
+ * electrons, or an evaluation gives a non-finite energy; GBOFDFT_ERR_ARG for
+ * a workspace smaller than gbofdft_tn_workspace_bytes.
  * Replaces Optimization.optimize_rho with method "TN"
  * (src/dftpy/optimization/optimization.py:281-520).
  */

@@ -52,7 +52,9 @@ BETA = (5.0 - np.sqrt(5.0)) / 6.0
 GAMMA = 2.7
 
 
-ETA_MIN, ETA_MAX, NT = 1e-5, 200.0, 40001
+# RK4 points on ln(eta); the forcing's derivative is singular at eta = 1,
+# which limits the accuracy there to ~7e-7 in Kx at this resolution
+ETA_MIN, ETA_MAX, NT = 1e-5, 200.0, 400001
 
 
 def kernel_shape(alpha=ALPHA, beta=BETA, gamma=GAMMA, x=1.0, order=2):

@@ -94,6 +94,7 @@ int gbofdft_plan_destroy(gbofdft_plan* p) {
   if (p->partials) cudaFree(p->partials);
   if (p->scratch) cudaFree(p->scratch);
   if (p->wt_pm) cudaFree(p->wt_pm);
+  if (p->wgc_pm) cudaFree(p->wgc_pm);
   delete p;
   return GBOFDFT_OK;
 }
@@ -291,16 +292,18 @@ static int eval_descs(const gbofdft_functional* f, EvalDesc& ev, KerDesc& kd, in
   return 0;
 }
 
-// the nonlocal terms evaluated outside the fused passes (added to pot / energies)
+// the nonlocal terms evaluated outside the fused passes (added to pot /
+// energies); wgc_ref: the WGC term also keeps this evaluation as the
+// reference of later WGC delta evaluations
 static int eval_extra(gbofdft_plan* p, const void* rho, const gbofdft_functional* f, void* pot, double* energies,
-                      int calc, cudaStream_t st) {
+                      int calc, cudaStream_t st, int wgc_ref = 0) {
   int rc = 0;
   if (f->lwt)
     rc = gb_lwt_eval(p, rho, f->lwt, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
                      st);
   if (!rc && f->wgc)
     rc = gb_wgc_eval(p, rho, f->wgc, pot, energies, (calc & GBOFDFT_CALC_V) ? 1 : 0, (calc & GBOFDFT_CALC_E) ? 1 : 0,
-                     st);
+                     wgc_ref, st);
   return rc;
 }
 
@@ -348,6 +351,7 @@ struct gbofdft_delta {
   gbofdft_plan* p32;
   double* buf;      // rho_ref [N], pot_ref [N], C_ref [GB_MAX_FIELDS][N], E_ref [GB_NE]
   int valid;
+  int wgc_ref;      // the FP64 WGC term's workspace holds the reference of rho_ref
   int nf;
   int ops[GB_MAX_FIELDS];
   int kind[GB_MAX_FIELDS];
@@ -426,7 +430,10 @@ int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_function
       d->ops[i] = i < nf ? ops[i] : -1;
       d->kind[i] = i < nf ? kd.type[i] : -1;
     }
-    return eval_extra(d->p64, rho, f, pot, energies, calc, st);
+    d->wgc_ref = 0;
+    rc = eval_extra(d->p64, rho, f, pot, energies, calc, st, f->wgc ? 1 : 0);
+    if (!rc && f->wgc) d->wgc_ref = 1;
+    return rc;
   }
   GB_REQUIRE(d->valid, "eval_delta: no reference evaluation yet (call with rebase = 1 first)");
   GB_REQUIRE(d->nf == nf, "eval_delta: functional terms differ from the reference evaluation's");
@@ -440,7 +447,18 @@ int gbofdft_eval_delta(gbofdft_delta* d, const void* rho, const gbofdft_function
   rc = gb_eval_delta_core(d->p64, d->p32, reinterpret_cast<const double*>(rho), rho_ref, pot_ref, eref, cref, nf, ops,
                           f->wt_beta, kd, ev, reinterpret_cast<const double*>(f->vloc),
                           reinterpret_cast<double*>(pot), (calc & GBOFDFT_CALC_E) ? 1 : 0, energies, st);
-  if (!rc) rc = eval_extra(d->p64, rho, f, pot, energies, calc, st);
+  if (rc) return rc;
+  // the WGC term as a change from its reference when the FP32 functional has
+  // one; LWT (and WGC without an FP32 counterpart) in full FP64
+  const bool wgc_delta = f->wgc && d->wgc_ref && hf && hf->wgc &&
+                         fabs(f->wgc->rho0 - hf->wgc->rho0) <= 1e-6 * f->wgc->rho0;
+  gbofdft_functional rest = *f;
+  if (wgc_delta) rest.wgc = nullptr;
+  else d->wgc_ref = 0;   // a full WGC evaluation overwrites the reference's fields
+  rc = eval_extra(d->p64, rho, &rest, pot, energies, calc, st);
+  if (!rc && wgc_delta)
+    rc = gb_wgc_eval_delta(d->p64, d->p32, reinterpret_cast<const double*>(rho), rho_ref, f->wgc, hf->wgc,
+                           reinterpret_cast<double*>(pot), energies, (calc & GBOFDFT_CALC_E) ? 1 : 0, st);
   return rc;
 }
 

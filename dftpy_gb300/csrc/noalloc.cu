@@ -20,9 +20,20 @@
 //    other.  Serialise them.  Each call rewrites everything it reads from the
 //    array (twiddles and the whole spectrum region), so nothing has to be
 //    cleared between calls.
+//  * a call that fails after it has started (a launch error in a later pass)
+//    may already have rewritten the twiddles and part of the spectrum: the
+//    array's contents are never valid across calls anyway.
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture begins.
+//    that first call before any stream capture begins.  The address is kept
+//    per device number for the life of the process: after cudaDeviceReset,
+//    or from a different context on the same device (made through the
+//    driver API), it no longer belongs to the current module -- neither is
+//    supported.
+//  * the twiddle factors are computed on the device (sincospi in double
+//    precision), while gbofdft_plan_create tabulates them on the host in long
+//    double, so the result equals gbofdft_convolve's to rounding, not bit
+//    for bit.
 #include <math.h>
 #include <string.h>
 

@@ -88,9 +88,16 @@ template <typename T> __device__ __forceinline__ T pow_beta_ct(T x, bool b56, T 
 }
 
 template <typename T>
-__device__ __forceinline__ T prologue_ct(int op, T rho, bool b56, T beta) {
+__device__ __forceinline__ T prologue_ct(int op, T rho, bool b56, T beta, T rho0 = (T)0, T inv0 = (T)0) {
   if (op == OP_SQRT) return sqrt_pos<T>(rho > (T)0 ? rho : (T)kZero);
   if (op == OP_POWB) return pow_beta_ct<T>(rho < (T)kZero ? (T)kZero : rho, b56, beta);
+  if (op >= OP_WGC0) {
+    // the WGC transform inputs rho^e u^k, rho clamped at 1e-30 (e = beta)
+    const T rc = rho > (T)kZero ? rho : (T)kZero;
+    const T B = pow_beta_ct<T>(rc, b56, beta);
+    const T u = (rc - rho0) * inv0;
+    return op == OP_WGC0 ? B : (op == OP_WGC1 ? u * B : u * u * B);
+  }
   return rho;
 }
 
@@ -105,6 +112,7 @@ struct CtRowsFwd {
   int op[GB_MAX_FIELDS];
   int b56;            // beta == 5/6
   Sc beta, half;      // half = scale / 2
+  Sc rho0, inv0;      // WGC prologues: expansion density and its inverse
   const void* tw;
 };
 
@@ -144,6 +152,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   __syncthreads();
   const bool b56 = a.b56 != 0;
   const T beta = sc<T>(a.beta);
+  const T rho0 = sc<T>(a.rho0), inv0 = sc<T>(a.inv0);
   // fields in an unrolled outer loop: the field's prologue op is a
   // compile-time parameter index, and every index split below is by a
   // compile-time constant
@@ -154,8 +163,8 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
     for (int idx = tid; idx < RP * N; idx += blockDim.x) {
       const int l2 = idx / N, j = idx % N;
       const int64_t ra = base + 2 * l2;
-      const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], b56, beta) : (T)0;
-      const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], b56, beta) : (T)0;
+      const T x0 = ra < a.nrows ? prologue_ct<T>(op, R[(2 * l2) * N + j], b56, beta, rho0, inv0) : (T)0;
+      const T x1 = ra + 1 < a.nrows ? prologue_ct<T>(op, R[(2 * l2 + 1) * N + j], b56, beta, rho0, inv0) : (T)0;
       A[sw<T, NP>(f * RP + l2, j)] = cpx<T>{x0, x1};
     }
   }
@@ -233,7 +242,7 @@ __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t
   return fft<1, T, N>(A, B, tw, l, lane, true);
 }
 
-template <typename T, int N>
+template <typename T, int N, bool PM = false>
 __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_store(CtRowsInv a) {
   constexpr int RP = RowsCfg<T>::RP, NP = Pad<T, N>::NP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_store(
   const int64_t base = (int64_t)blockIdx.x * 2 * RP;
   const cpx<T>* twg = reinterpret_cast<const cpx<T>*>(a.tw);
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
-  cpx<T>* res = ct_rows_inv_lines<T, N>(a, base, tw, A, B);
+  cpx<T>* res = ct_rows_inv_lines<T, N, PM>(a, base, tw, A, B);
   T* out = reinterpret_cast<T*>(a.out);
   const T s = sc<T>(a.scale);
   for (int idx = tid; idx < a.nf * 2 * RP * N; idx += blockDim.x) {
@@ -577,7 +586,7 @@ template <typename K> inline int ct_smem(K kern, size_t bytes) {
 
 template <typename T, bool PM = false>
 int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, int ld2, int nf, const int* ops,
-                double beta, double scale, cudaStream_t st) {
+                double beta, double scale, cudaStream_t st, double rho0 = 0.0) {
   int rc = 1;
   ct_dispatch(p->n[2], [&](auto nc) {
     constexpr int N = decltype(nc)::value;
@@ -589,6 +598,8 @@ int ct_rows_fwd(gbofdft_plan* p, const void* in, void* spec, int64_t fstride, in
     a.b56 = fabs(beta - 5.0 / 6.0) < 1e-15;
     a.beta.set(beta);
     a.half.set(0.5 * scale);
+    a.rho0.set(rho0);
+    a.inv0.set(rho0 > 0.0 ? 1.0 / rho0 : 0.0);
     a.tw = p->tw[2];
     const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP) + sizeof(T) * 2 * RP * N;
     if ((rc = ct_smem(k_ct_rows_fwd<T, N, PM>, sm))) return;
@@ -635,8 +646,9 @@ int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int
         k_ct_rows_inv_eval<T, N, false, PM><<<nblk, Tpl<N>::value * RP * nfl, sm, st>>>(a);
       }
     } else if constexpr (PM) {
-      rc = gb_set_error(GBOFDFT_ERR_ARG, "ct_rows_inv: plane-major spectra only in the evaluation pass");
-      return;
+      const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP);
+      if ((rc = ct_smem(k_ct_rows_inv_store<T, N, true>, sm))) return;
+      k_ct_rows_inv_store<T, N, true><<<nblk, Tpl<N>::value * RP * nf, sm, st>>>(a);
     } else {
       const size_t sm = sizeof(cpx<T>) * (N + 2 * (size_t)nf * RP * NP);
       if ((rc = ct_smem(k_ct_rows_inv_store<T, N>, sm))) return;
@@ -729,6 +741,73 @@ inline int plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, 
   return rc;
 }
 
+template <typename K> inline void plane_args_common(gbofdft_plan* p, K& a) {
+  a.tw0 = p->tw[0];
+  a.tw1 = p->tw[1];
+}
+
+// forward plane transforms (axis 1 then axis 0) of nf plane-major fields, in place
+inline int plane_fwd_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, cudaStream_t st) {
+  int rc = 1;
+  plane_dispatch(p->n[0], p->n[1], [&](auto a0, auto a1) {
+    constexpr int N0 = decltype(a0)::value, N1 = decltype(a1)::value;
+    PlaneFwdArgs a;
+    a.spec = reinterpret_cast<float2*>(spec);
+    a.fstride = fstride;
+    plane_args_common(p, a);
+    const size_t sm = PlaneCfg<N0, N1>::kSmemXform;
+    auto launch = [&](auto kern) {
+      if ((rc = ct_smem(kern, sm))) return;
+      kern<<<dim3(p->n2h, nf), PlaneCfg<N0, N1>::NT, sm, st>>>(a);
+    };
+    if constexpr (plane_variants<N0, N1>() > 1) {
+      if (p->plane_variant == 1) launch(k_plane_fwd<N0, N1, 1>);
+      else launch(k_plane_fwd<N0, N1, 0>);
+    } else {
+      launch(k_plane_fwd<N0, N1, 0>);
+    }
+    if (rc) return;
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "plane_fwd: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+// WGC kernel combination and inverse plane transforms (axis 0 then axis 1)
+inline int plane_wgc_inv_f32(gbofdft_plan* p, const void* spec, int64_t fstride, void* out, int64_t ostride,
+                             int ngroups, const float* K, double scale, cudaStream_t st) {
+  int rc = 1;
+  plane_dispatch(p->n[0], p->n[1], [&](auto a0, auto a1) {
+    constexpr int N0 = decltype(a0)::value, N1 = decltype(a1)::value;
+    PlaneWgcArgs a;
+    a.in = reinterpret_cast<const float2*>(spec);
+    a.fstride = fstride;
+    a.out = reinterpret_cast<float2*>(out);
+    a.ostride = ostride;
+    a.K = K;
+    a.kstride = p->NG;
+    a.scale = (float)scale;
+    plane_args_common(p, a);
+    const size_t sm = PlaneCfg<N0, N1>::kSmemXform;
+    auto launch = [&](auto kern) {
+      if ((rc = ct_smem(kern, sm))) return;
+      kern<<<dim3(p->n2h, 3, ngroups), PlaneCfg<N0, N1>::NT, sm, st>>>(a);
+    };
+    if constexpr (plane_variants<N0, N1>() > 1) {
+      if (p->plane_variant == 1) launch(k_plane_wgc_inv<N0, N1, 1>);
+      else launch(k_plane_wgc_inv<N0, N1, 0>);
+    } else {
+      launch(k_plane_wgc_inv<N0, N1, 0>);
+    }
+    if (rc) return;
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "plane_wgc_inv: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
 }  // namespace gbct
 
 // Plane-major evaluation pipeline (FP32 only).
@@ -746,6 +825,23 @@ inline int plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, 
   int gb_plane_conv_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, const KerDesc* kd,               \
                         const float* const* pm_arr, double scale, cudaStream_t st) {                          \
     return gbct::plane_conv_f32(p, spec, fstride, nf, *kd, pm_arr, scale, st);                                \
+  }                                                                                                            \
+  int gb_ct_rows_fwd_wgc_pm_f32(gbofdft_plan* p, const void* rho, void* spec, int64_t fstride, double e,        \
+                                double rho0, cudaStream_t st) {                                               \
+    const int ops[3] = {OP_WGC0, OP_WGC1, OP_WGC2};                                                            \
+    return gbct::ct_rows_fwd<float, true>(p, rho, spec, fstride, 0, 3, ops, e, 1.0, st, rho0);                \
+  }                                                                                                            \
+  int gb_ct_rows_inv_store_pm_f32(gbofdft_plan* p, const void* spec, int64_t fstride, int nf, void* out,       \
+                                  int64_t ostride, cudaStream_t st) {                                          \
+    return gbct::ct_rows_inv<float, true>(p, spec, fstride, 0, nf, out, ostride, 1.0, nullptr, nullptr,        \
+                                          nullptr, nullptr, 0, nullptr, nullptr, st);                          \
+  }                                                                                                            \
+  int gb_plane_fwd_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, cudaStream_t st) {                \
+    return gbct::plane_fwd_f32(p, spec, fstride, nf, st);                                                      \
+  }                                                                                                            \
+  int gb_plane_wgc_inv_f32(gbofdft_plan* p, const void* spec, int64_t fstride, void* out, int64_t ostride,     \
+                           int ngroups, const float* K, double scale, cudaStream_t st) {                       \
+    return gbct::plane_wgc_inv_f32(p, spec, fstride, out, ostride, ngroups, K, scale, st);                     \
   }                                                                                                            \
   int gb_plane_supported_f32(int n0, int n1, int n2) {                                                         \
     bool rows = gbct::ct_dispatch(n2, [](auto) {});                                                            \

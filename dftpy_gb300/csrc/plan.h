@@ -36,6 +36,8 @@ struct gbofdft_plan {
   int plane_variant;     // radix-schedule variant of the plane pass (autotuned)
   float* wt_pm;          // plane-major copy of the last WT kernel table built on this plan
   const void* wt_pm_src; // the table that copy belongs to
+  float* wgc_pm;         // plane-major copy of the last WGC kernels (4 x NG) built on this plan
+  const void* wgc_pm_src; // the kernels that copy belongs to
 };
 
 size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
@@ -44,7 +46,9 @@ size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
 unsigned* gb_plan_counter(gbofdft_plan* p);
 
 // ---- pass launchers (passes.cu) -------------------------------------------
-enum { OP_RHO = 0, OP_SQRT = 1, OP_POWB = 2 };           // forward prologues
+// forward prologues; OP_WGC0..2: rho^e u^k (k = 0, 1, 2) of the WGC term,
+// u = (rho - rho0) / rho0, exponent e in the beta argument
+enum { OP_RHO = 0, OP_SQRT = 1, OP_POWB = 2, OP_WGC0 = 3, OP_WGC1 = 4, OP_WGC2 = 5 };
 enum { KER_NONE = 0, KER_HARTREE = 1, KER_G2 = 2, KER_ARRAY = 3 };
 
 struct EvalDesc {
@@ -90,6 +94,18 @@ int gb_ct_rows_inv_eval_pm_f32(gbofdft_plan*, const void*, int64_t, int, const E
                                void*, int, double*, int64_t*, cudaStream_t);
 int gb_plane_conv_f32(gbofdft_plan*, void*, int64_t, int, const KerDesc*, const float* const*, double, cudaStream_t);
 int gb_plane_supported_f32(int n0, int n1, int n2);
+// WGC fields on the plane pipeline (FP32): the forward rows with the WGC
+// prologues (3 fields rho^e u^k from rho), the forward plane transforms of
+// nf fields (in place), the kernel combination and inverse plane transforms
+// of ngroups groups of three fields (K: the plane-major kernels K0, K1, Kq,
+// Kx), and the inverse rows storing real fields
+int gb_ct_rows_fwd_wgc_pm_f32(gbofdft_plan*, const void* rho, void* spec, int64_t fstride, double e, double rho0,
+                              cudaStream_t);
+int gb_plane_fwd_f32(gbofdft_plan*, void* spec, int64_t fstride, int nf, cudaStream_t);
+int gb_plane_wgc_inv_f32(gbofdft_plan*, const void* spec, int64_t fstride, void* out, int64_t ostride, int ngroups,
+                         const float* K, double scale, cudaStream_t);
+int gb_ct_rows_inv_store_pm_f32(gbofdft_plan*, const void* spec, int64_t fstride, int nf, void* out, int64_t ostride,
+                                cudaStream_t);
 int gb_plane_variants_f32(int n0, int n1);
 // the plane-major evaluation (returns 1 when the plan has no plane pipeline
 // or a kernel table has no plane-major copy)
@@ -121,8 +137,15 @@ int gb_use_ct();  // 0 forces the generic passes (GBOFDFT_GENERIC_FFT=1)
 
 int gb_lwt_eval(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double* energies, int calc_v,
                 int calc_e, cudaStream_t st);
+// store_ref (FP64 plans): keep this evaluation as the reference of gb_wgc_eval_delta
 int gb_wgc_eval(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
-                int calc_e, cudaStream_t st);
+                int calc_e, int store_ref, cudaStream_t st);
+// the WGC term at rho from the reference kept by the last store_ref
+// evaluation with d64 (at rho_ref): FP32 transforms of the change with p32 /
+// d32, the NL potential added to pot, the energy to energies (with calc_e)
+int gb_wgc_eval_delta(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
+                      const gbofdft_wgc* d64, const gbofdft_wgc* d32, double* pot, double* energies, int calc_e,
+                      cudaStream_t st);
 
 // phi-space TN preconditioner of the uniform gas rho0 on the half spectrum (real, NG values)
 int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st);

@@ -50,6 +50,8 @@ template <int N0, int N1> struct PlaneCfg {
   static constexpr bool table_smem = kPlaneBytes + kTable + kSmall <= 227 * 1024 && (N0 * N1) % 4 == 0;
   static constexpr size_t kSmem = kPlaneBytes + (table_smem ? kTable : 0) + kSmall;
   static constexpr bool fits = kSmem <= 227 * 1024;
+  // transform-only plane kernels (no kernel table, no G tables): plane + twiddles
+  static constexpr size_t kSmemXform = kPlaneBytes + sizeof(float2) * (N0 + N1);
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -277,6 +279,104 @@ __global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_conv(PlaneArg
   plane_fft<-1, 0, N0, N1, V, PS_SMEM, PS_SMEM>(pl, tw0, nullptr, nullptr, kmul);
   plane_fft<1, 0, N0, N1, V>(pl, tw0);
   // inverse along axis 1, its last stage writing the plane to global memory
+  plane_fft<1, 1, N0, N1, V, PS_SMEM, PS_TO_GLOBAL>(pl, tw1, nullptr, gp);
+}
+
+// ---- plane transforms of the WGC term --------------------------------------------
+// The WGC nonlocal term needs the forward transforms of its transform inputs
+// (three fields per exponent), a pointwise combination ACROSS those fields
+// with four kernels, and the inverse transforms of the three combinations:
+//   X0 = K0 F0 + K1/6 F1 + Kq F2,  X1 = K1/6 F0 + Kx F1,  X2 = Kq F0.
+// A plane of one field fills a CTA's shared memory, so the combination
+// cannot sit between the forward and inverse stages of one CTA: the forward
+// plane pass writes every field's spectrum plane back (in place), and the
+// inverse pass reads the three input planes of its group from global memory
+// (L2), combines them into its own output plane and transforms it back.
+
+struct PlaneFwdArgs {
+  float2* spec;
+  int64_t fstride;
+  const void* tw0;
+  const void* tw1;
+};
+
+template <int N0, int N1, int V>
+__global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_fwd(PlaneFwdArgs a) {
+  constexpr int NT = PlaneCfg<N0, N1>::NT;
+  using Cfg = PlaneCfg<N0, N1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* pl = reinterpret_cast<float2*>(smem_raw);
+  float2* tw0 = reinterpret_cast<float2*>(smem_raw + Cfg::kPlaneBytes);
+  float2* tw1 = tw0 + N0;
+  const int tid = threadIdx.x;
+  const int k2 = blockIdx.x, f = blockIdx.y;
+  float2* gp = a.spec + f * a.fstride + (int64_t)k2 * (N0 * N1);
+  const float2* t0 = reinterpret_cast<const float2*>(a.tw0);
+  const float2* t1 = reinterpret_cast<const float2*>(a.tw1);
+  for (int i = tid; i < N0; i += NT) tw0[i] = t0[i];
+  for (int i = tid; i < N1; i += NT) tw1[i] = t1[i];
+  __syncthreads();
+  plane_fft<-1, 1, N0, N1, V, PS_FROM_GLOBAL>(pl, tw1, gp);
+  plane_fft<-1, 0, N0, N1, V>(pl, tw0);
+  // the spectrum plane back to global memory, row by row (coalesced)
+  for (int idx = tid; idx < N0 * N1; idx += NT) gp[idx] = pl[paddr<N1>(idx / N1, idx % N1)];
+}
+
+struct PlaneWgcArgs {
+  const float2* in;     // forward spectra of the transform inputs, group h at in + 3 h fstride
+  int64_t fstride;
+  float2* out;          // the combinations' planes, transformed back (group h, output j at out + (3 h + j) ostride)
+  int64_t ostride;
+  const float* K;       // plane-major K0, K1, Kq, Kx at K + c kstride
+  int64_t kstride;
+  float scale;          // 1 / N of the inverse transform
+  const void* tw0;
+  const void* tw1;
+};
+
+template <int N0, int N1, int V>
+__global__ void __launch_bounds__(PlaneCfg<N0, N1>::NT, 1) k_plane_wgc_inv(PlaneWgcArgs a) {
+  constexpr int NT = PlaneCfg<N0, N1>::NT;
+  using Cfg = PlaneCfg<N0, N1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* pl = reinterpret_cast<float2*>(smem_raw);
+  float2* tw0 = reinterpret_cast<float2*>(smem_raw + Cfg::kPlaneBytes);
+  float2* tw1 = tw0 + N0;
+  const int tid = threadIdx.x;
+  const int k2 = blockIdx.x, j = blockIdx.y, h = blockIdx.z;
+  const int64_t po = (int64_t)k2 * (N0 * N1);
+  const float2* s0 = a.in + 3 * h * a.fstride + po;
+  const float2* s1 = s0 + a.fstride;
+  const float2* s2 = s1 + a.fstride;
+  const float* K0 = a.K + po;
+  const float* K1 = K0 + a.kstride;
+  const float* Kq = K1 + a.kstride;
+  const float* Kx = Kq + a.kstride;
+  float2* gp = a.out + (3 * h + j) * a.ostride + po;
+  const float2* t0 = reinterpret_cast<const float2*>(a.tw0);
+  const float2* t1 = reinterpret_cast<const float2*>(a.tw1);
+  for (int i = tid; i < N0; i += NT) tw0[i] = t0[i];
+  for (int i = tid; i < N1; i += NT) tw1[i] = t1[i];
+  const float sc = a.scale, sc6 = a.scale * (1.0f / 6.0f);
+  for (int idx = tid; idx < N0 * N1; idx += NT) {
+    const float2 f0 = s0[idx];
+    float2 v;
+    if (j == 0) {
+      const float2 f1 = s1[idx], f2 = s2[idx];
+      const float k0 = __ldg(K0 + idx) * sc, k1 = __ldg(K1 + idx) * sc6, kq = __ldg(Kq + idx) * sc;
+      v = float2{k0 * f0.x + k1 * f1.x + kq * f2.x, k0 * f0.y + k1 * f1.y + kq * f2.y};
+    } else if (j == 1) {
+      const float2 f1 = s1[idx];
+      const float k1 = __ldg(K1 + idx) * sc6, kx = __ldg(Kx + idx) * sc;
+      v = float2{k1 * f0.x + kx * f1.x, k1 * f0.y + kx * f1.y};
+    } else {
+      const float kq = __ldg(Kq + idx) * sc;
+      v = float2{kq * f0.x, kq * f0.y};
+    }
+    pl[paddr<N1>(idx / N1, idx % N1)] = v;
+  }
+  __syncthreads();
+  plane_fft<1, 0, N0, N1, V>(pl, tw0);
   plane_fft<1, 1, N0, N1, V, PS_SMEM, PS_TO_GLOBAL>(pl, tw1, nullptr, gp);
 }
 

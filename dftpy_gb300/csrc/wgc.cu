@@ -31,7 +31,13 @@ struct WgcBufs {
   void* f[6];       // real fields: transform inputs, then X0..X2, Y0..Y2
   void* s[6];       // spectra (internal layout)
   double* part;     // per-CTA energy partials
+  double* vref;     // FP64 plans: the NL potential of the last reference evaluation [N]
+  double* eref;     // FP64 plans: its NL energy [1]
+  void* o[6];       // FP32 plane-pipeline plans: the combinations' spectra (plane-major)
 };
+
+// FP32 plans whose grid has the plane pipeline run the WGC transforms there
+bool wgc_plane(const gbofdft_plan* p) { return p->prec == GBOFDFT_F32 && p->plane_ok && gb_use_ct(); }
 
 constexpr int kBlocks = 1216;
 constexpr int kThreads = 256;
@@ -43,12 +49,29 @@ WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
   for (int i = 0; i < 6; ++i) { W.f[i] = b; b += fb; }
   for (int i = 0; i < 6; ++i) { W.s[i] = b; b += sb; }
   W.part = reinterpret_cast<double*>(b);
+  b += r256(sizeof(double) * kBlocks);
+  W.vref = nullptr;
+  W.eref = nullptr;
+  for (int i = 0; i < 6; ++i) W.o[i] = nullptr;
+  if (p->prec == GBOFDFT_F64) {
+    W.vref = reinterpret_cast<double*>(b);
+    b += r256(sizeof(double) * (size_t)p->N);
+    W.eref = reinterpret_cast<double*>(b);
+  } else if (wgc_plane(p)) {
+    for (int i = 0; i < 6; ++i) { W.o[i] = b; b += sb; }
+  }
   return W;
 }
 
+// FP64 workspaces keep a reference evaluation for the delta evaluations of
+// the mixed-precision refinement: the X / Y fields of the last evaluation
+// (in f[0..5]), its NL potential and energy
 size_t wgc_bytes(const gbofdft_plan* p) {
-  return 6 * r256(gb_elem(p) * (size_t)p->N) + 6 * r256(2 * gb_elem(p) * (size_t)p->NGld) +
-         r256(sizeof(double) * kBlocks);
+  size_t b = 6 * r256(gb_elem(p) * (size_t)p->N) + 6 * r256(2 * gb_elem(p) * (size_t)p->NGld) +
+             r256(sizeof(double) * kBlocks);
+  if (p->prec == GBOFDFT_F64) b += r256(sizeof(double) * (size_t)p->N) + 256;
+  else if (wgc_plane(p)) b += 6 * r256(2 * gb_elem(p) * (size_t)p->NGld);
+  return b;
 }
 
 // Column c of the kernel table at eta: cubic (Catmull-Rom) interpolation in
@@ -89,6 +112,21 @@ __global__ void k_wgc_kernels(GInfo g, double tkf, double C, const double* __res
           g, i0, i1, k2, [&](double gg) { return C * table_at(tab, m, t0, h, c, sqrt(gg) / tkf); });
       out[c * total + id] = (T)v;
     }
+  }
+}
+
+// plane-major copy of the four kernels: element (i0, i1, k2) of kernel c at
+// pm[c NG + (k2 n0 + i0) n1 + i1]
+__global__ void k_wgc_kernels_pm(GInfo g, const float* __restrict__ K, float* __restrict__ pm) {
+  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < 4 * total;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(id / total);
+    const int64_t r = id - c * total;            // plane-major index within kernel c
+    const int64_t plane = (int64_t)g.n0 * g.n1;
+    const int k2 = (int)(r / plane);
+    const int64_t rr = r - k2 * plane;           // i0 n1 + i1
+    pm[id] = K[c * total + rr * g.n2h + k2];
   }
 }
 
@@ -144,7 +182,8 @@ __global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __re
                                                          int two, const T* __restrict__ x0, const T* __restrict__ x1,
                                                          const T* __restrict__ x2, const T* __restrict__ y0,
                                                          const T* __restrict__ y1, const T* __restrict__ y2,
-                                                         T* __restrict__ pot, int calc_v, double* __restrict__ part) {
+                                                         T* __restrict__ pot, int calc_v, double* __restrict__ part,
+                                                         T* __restrict__ vstore) {
   const T inv0 = (T)1 / rho0;
   T es = (T)0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -165,6 +204,7 @@ __global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __re
         v = (T)2 * (a * A / rc * sx + A * inv0 * (X1 + (T)2 * u * X2));
       }
       pot[i] += v;
+      if (vstore) vstore[i] = v;
     }
   }
   if constexpr (!WANT_E) return;
@@ -180,8 +220,10 @@ __global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __re
   }
 }
 
-// energies[NL] and energies[TOTAL] += dV * sum(partials)
-__global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV, double* __restrict__ e) {
+// energies[NL] and energies[TOTAL] += base + dV * sum(partials) (e may be
+// null); eref (may be null) = dV * sum(partials)
+__global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV, double* __restrict__ e,
+                             double* __restrict__ eref, const double* __restrict__ base) {
   __shared__ double red[32];
   KSum s;
   s.init();
@@ -193,23 +235,43 @@ __global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV,
     KSum t;
     t.init();
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t.add(red[w]);
-    const double en = t.value() * dV;
-    e[GB_E_NL] += en;
-    e[GB_E_TOTAL] += en;
+    const double en = t.value() * dV + (base ? *base : 0.0);
+    if (e) {
+      e[GB_E_NL] += en;
+      e[GB_E_TOTAL] += en;
+    }
+    if (eref) *eref = en;
   }
 }
 
-template <typename T>
-int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
-            int calc_e, cudaStream_t st) {
-  WgcBufs W = wgc_layout(p, d->work);
-  const int two = fabs(d->alpha - d->beta) > 1e-12;
+// X0..X2 (and Y0..Y2) into W.f[0..5] on the plane pipeline (FP32): the
+// transform inputs are made from rho in the forward row pass (rho given) or
+// read from W.f[0..5] (rho null); K: the plane-major kernels
+int wgc_xfields_plane(gbofdft_plan* p, const WgcBufs& W, int two, const float* K, const float* rho,
+                      const gbofdft_wgc* d, cudaStream_t st) {
   const int nfield = two ? 6 : 3;
-  const T* r = reinterpret_cast<const T*>(rho);
-  k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],
-                                              (T*)W.f[1], (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
-  GB_CHECK_LAUNCH();
-  gb_count_launch();
+  const int64_t fs = (int64_t)((char*)W.s[1] - (char*)W.s[0]) / (int64_t)sizeof(float2);
+  const int64_t os = (int64_t)((char*)W.o[1] - (char*)W.o[0]) / (int64_t)sizeof(float2);
+  const int64_t rs = (int64_t)((char*)W.f[1] - (char*)W.f[0]) / (int64_t)sizeof(float);
+  int rc = 0;
+  if (rho) {
+    rc = gb_ct_rows_fwd_wgc_pm_f32(p, rho, W.s[0], fs, d->beta, d->rho0, st);
+    if (!rc && two) rc = gb_ct_rows_fwd_wgc_pm_f32(p, rho, W.s[3], fs, d->alpha, d->rho0, st);
+  } else {
+    const int op = OP_RHO;
+    for (int i = 0; i < nfield && !rc; ++i) rc = gb_ct_rows_fwd_pm_f32(p, W.f[i], W.s[i], fs, 1, &op, 1.0, st);
+  }
+  if (!rc) rc = gb_plane_fwd_f32(p, W.s[0], fs, nfield, st);
+  if (!rc) rc = gb_plane_wgc_inv_f32(p, W.s[0], fs, W.o[0], os, two ? 2 : 1, K, 1.0 / (double)p->N, st);
+  for (int h = 0; h < (two ? 2 : 1) && !rc; ++h) rc = gb_ct_rows_inv_store_pm_f32(p, W.o[3 * h], os, 3, W.f[3 * h], rs, st);
+  if (rc == 1) return gb_set_error(GBOFDFT_ERR_STATE, "wgc: plane size without specialisation");
+  return rc;
+}
+
+// X0..X2 (and Y0..Y2) into W.f[0..5] from the transform inputs in W.f[0..5]
+template <typename T>
+int wgc_xfields(gbofdft_plan* p, const WgcBufs& W, int two, const void* kernels, cudaStream_t st) {
+  const int nfield = two ? 6 : 3;
   const int op = OP_RHO;
   for (int i = 0; i < nfield; ++i) {
     int rc = gb_rows_fwd(p, W.f[i], W.s[i], 0, p->ld2, 1, &op, 1.0, 1.0, st);
@@ -217,7 +279,7 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
     if (!rc) rc = gb_cols(p, W.s[i], 0, p->ld2, 1, 0, -1, 1.0, st);
     if (rc) return rc;
   }
-  const T* K = reinterpret_cast<const T*>(d->kernels);
+  const T* K = reinterpret_cast<const T*>(kernels);
   const T scale = (T)(1.0 / (double)p->N);
   for (int h = 0; h < (two ? 2 : 1); ++h) {
     k_wgc_combine<T><<<kBlocks, kThreads, 0, st>>>(p->gi, p->ld2, K, scale, (cpx<T>*)W.s[3 * h],
@@ -233,38 +295,233 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
     if (!rc) rc = gb_rows_inv_store(p, W.s[3 * h], fstride, p->ld2, 3, W.f[3 * h], ostride, 1.0, st);
     if (rc) return rc;
   }
+  return 0;
+}
+
+// store_ref (FP64 plans): also keep the NL potential and energy as the
+// reference of later delta evaluations (the X / Y fields stay in W.f)
+template <typename T>
+int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
+            int calc_e, int store_ref, cudaStream_t st) {
+  WgcBufs W = wgc_layout(p, d->work);
+  const int two = fabs(d->alpha - d->beta) > 1e-12;
+  const T* r = reinterpret_cast<const T*>(rho);
+  int rc;
+  if (wgc_plane(p) && p->wgc_pm && p->wgc_pm_src == d->kernels) {
+    rc = wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st);
+  } else {
+    k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],
+                                                (T*)W.f[1], (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
+    GB_CHECK_LAUNCH();
+    gb_count_launch();
+    rc = wgc_xfields<T>(p, W, two, d->kernels, st);
+  }
+  if (rc) return rc;
+  T* vstore = nullptr;
+  if (store_ref) {
+    calc_v = 1;
+    vstore = reinterpret_cast<T*>(W.vref);
+  }
+  const int want_e = calc_e || store_ref;
   const T* y = reinterpret_cast<const T*>(two ? W.f[3] : W.f[0]);
-  if (calc_e)
+  if (want_e)
     k_wgc_final<T, true><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
                                                        (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
                                                        two ? (const T*)W.f[4] : nullptr,
-                                                       two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part);
+                                                       two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part,
+                                                       vstore);
   else
     k_wgc_final<T, false><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
                                                         (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
                                                         two ? (const T*)W.f[4] : nullptr,
-                                                        two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part);
+                                                        two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part,
+                                                        vstore);
   GB_CHECK_LAUNCH();
   gb_count_launch();
-  if (calc_e) {
-    k_wgc_energy<<<1, 256, 0, st>>>(W.part, kBlocks, p->dV, energies);
+  if (want_e) {
+    k_wgc_energy<<<1, 256, 0, st>>>(W.part, kBlocks, p->dV, calc_e ? energies : nullptr,
+                                    store_ref ? W.eref : nullptr, nullptr);
     GB_CHECK_LAUNCH();
     gb_count_launch();
   }
   return 0;
 }
 
+// ---- delta evaluation (FP64 result from FP32 transforms of the change) -----
+//
+// For a density rho close to the reference rho_r of the last store_ref
+// evaluation, the transform inputs F = {B, uB, u^2 B, A, uA, u^2 A} change by
+// dF, and by linearity X(rho) = X(rho_r) + K * dF.  dF is formed from the
+// two FP64 densities with relative FP32 accuracy in the change (power laws
+// as b^p expm1(p log1p((a - b)/b)), products as d(fg) = df g + f_r dg),
+// transformed by the FP32 plan, and the NL potential and energy are formed
+// as FP32 changes on the stored FP64 reference: the error is ~1e-7 of the
+// change, not of the value.
+
+struct WgcDeltaPt {
+  float dA, A, Ar, dAp, Apr, dB, B, Br, dBp, Bpr, du, u, ur;
+};
+
+// the power-law factors at rho and their changes from rho_r (both clamped at 1e-30)
+__device__ __forceinline__ WgcDeltaPt wgc_delta_point(double rho, double rref, double rho0, float a, float b) {
+  const double rc = rho > kZeroRho ? rho : kZeroRho;
+  const double rr = rref > kZeroRho ? rref : kZeroRho;
+  const float rf = (float)rr;
+  const float d = (float)(rc - rr);
+  const float L = log1pf(d / rf);
+  WgcDeltaPt q;
+  q.Ar = powf(rf, a);
+  q.dA = q.Ar * expm1f(a * L);
+  q.A = q.Ar + q.dA;
+  q.Apr = a * q.Ar / rf;
+  q.dAp = q.Apr * expm1f((a - 1.0f) * L);
+  q.Br = powf(rf, b);
+  q.dB = q.Br * expm1f(b * L);
+  q.B = q.Br + q.dB;
+  q.Bpr = b * q.Br / rf;
+  q.dBp = q.Bpr * expm1f((b - 1.0f) * L);
+  const float inv0 = (float)(1.0 / rho0);
+  q.ur = (float)((rr - rho0) / rho0);
+  q.du = d * inv0;
+  q.u = q.ur + q.du;
+  return q;
+}
+
+// dF (FP32) into f0..f5
+__global__ void k_wgc_delta_prep(int64_t n, const double* __restrict__ rho, const double* __restrict__ rref,
+                                 double rho0, float a, float b, int two, float* __restrict__ f0,
+                                 float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ f3,
+                                 float* __restrict__ f4, float* __restrict__ f5) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const WgcDeltaPt q = wgc_delta_point(rho[i], rref[i], rho0, a, b);
+    const float du2 = q.du * (q.u + q.ur);          // u^2 - u_r^2
+    const float ur2 = q.ur * q.ur;
+    f0[i] = q.dB;
+    f1[i] = q.du * q.B + q.ur * q.dB;
+    f2[i] = du2 * q.B + ur2 * q.dB;
+    if (two) {
+      f3[i] = q.dA;
+      f4[i] = q.du * q.A + q.ur * q.dA;
+      f5[i] = du2 * q.A + ur2 * q.dA;
+    }
+  }
+}
+
+// pot += V_r + dV and per-CTA partials of the energy change; xr: the FP64
+// reference X / Y fields, dx: their FP32 changes
+template <bool WANT_E>
+__global__ void __launch_bounds__(kThreads) k_wgc_delta_final(
+    int64_t n, const double* __restrict__ rho, const double* __restrict__ rref, double rho0, float a, float b,
+    int two, const double* __restrict__ xr0, const double* __restrict__ xr1, const double* __restrict__ xr2,
+    const double* __restrict__ yr0, const double* __restrict__ yr1, const double* __restrict__ yr2,
+    const float* __restrict__ dx0, const float* __restrict__ dx1, const float* __restrict__ dx2,
+    const float* __restrict__ dy0, const float* __restrict__ dy1, const float* __restrict__ dy2,
+    const double* __restrict__ vref, double* __restrict__ pot, double* __restrict__ part) {
+  const float inv0 = (float)(1.0 / rho0);
+  float es = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const WgcDeltaPt q = wgc_delta_point(rho[i], rref[i], rho0, a, b);
+    const float du2 = q.du * (q.u + q.ur);
+    // sx = X0 + u X1 + u^2 X2 and tx = X1 + 2 u X2 at rho, and their changes
+    const float X0 = (float)xr0[i], X1 = (float)xr1[i], X2 = (float)xr2[i];
+    const float d0 = dx0[i], d1 = dx1[i], d2 = dx2[i];
+    const float dsx = d0 + q.u * d1 + q.du * X1 + q.u * q.u * d2 + du2 * X2;
+    const float sx = X0 + q.ur * X1 + q.ur * q.ur * X2 + dsx;
+    const float dtx = d1 + 2.0f * (q.u * d2 + q.du * X2);
+    const float tx = X1 + 2.0f * q.ur * X2 + dtx;
+    float dv = q.dAp * sx + q.Apr * dsx + (q.dA * tx + q.Ar * dtx) * inv0;
+    if (two) {
+      const float Y0 = (float)yr0[i], Y1 = (float)yr1[i], Y2 = (float)yr2[i];
+      const float e0 = dy0[i], e1 = dy1[i], e2 = dy2[i];
+      const float dsy = e0 + q.u * e1 + q.du * Y1 + q.u * q.u * e2 + du2 * Y2;
+      const float sy = Y0 + q.ur * Y1 + q.ur * q.ur * Y2 + dsy;
+      const float dty = e1 + 2.0f * (q.u * e2 + q.du * Y2);
+      const float ty = Y1 + 2.0f * q.ur * Y2 + dty;
+      dv += q.dBp * sy + q.Bpr * dsy + (q.dB * ty + q.Br * dty) * inv0;
+    } else {
+      dv *= 2.0f;
+    }
+    pot[i] += vref[i] + (double)dv;
+    if (WANT_E) es += q.dA * sx + q.Ar * dsx;
+  }
+  if constexpr (!WANT_E) return;
+  __shared__ double red[kThreads / 32];
+  const double v = warp_sum((double)es);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    KSum t;
+    t.init();
+    for (int w = 0; w < kThreads / 32; ++w) t.add(red[w]);
+    part[blockIdx.x] = t.value();
+  }
+}
+
 }  // namespace
 
-int gb_wgc_eval(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
-                int calc_e, cudaStream_t st) {
+static int wgc_check(const gbofdft_plan* p, const gbofdft_wgc* d) {
   GB_REQUIRE(d->kernels && d->work, "wgc: kernels or workspace missing");
   GB_REQUIRE(d->rho0 > 0.0, "wgc: rho0 must be positive (got %g)", d->rho0);
   GB_REQUIRE(d->work_bytes >= (int64_t)wgc_bytes(p), "wgc: workspace %lld < %lld bytes", (long long)d->work_bytes,
              (long long)wgc_bytes(p));
   GB_REQUIRE(((uintptr_t)d->work & 255) == 0, "wgc: workspace must be 256-byte aligned");
-  return p->prec == GBOFDFT_F64 ? wgc_run<double>(p, rho, d, pot, energies, calc_v, calc_e, st)
-                                : wgc_run<float>(p, rho, d, pot, energies, calc_v, calc_e, st);
+  return 0;
+}
+
+int gb_wgc_eval(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, double* energies, int calc_v,
+                int calc_e, int store_ref, cudaStream_t st) {
+  int rc = wgc_check(p, d);
+  if (rc) return rc;
+  GB_REQUIRE(!store_ref || p->prec == GBOFDFT_F64, "wgc: a delta reference needs an FP64 plan");
+  return p->prec == GBOFDFT_F64 ? wgc_run<double>(p, rho, d, pot, energies, calc_v, calc_e, store_ref, st)
+                                : wgc_run<float>(p, rho, d, pot, energies, calc_v, calc_e, 0, st);
+}
+
+int gb_wgc_eval_delta(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, const double* rho_ref,
+                      const gbofdft_wgc* d64, const gbofdft_wgc* d32, double* pot, double* energies, int calc_e,
+                      cudaStream_t st) {
+  int rc = wgc_check(p64, d64);
+  if (!rc) rc = wgc_check(p32, d32);
+  if (rc) return rc;
+  GB_REQUIRE(p64->prec == GBOFDFT_F64 && p32->prec == GBOFDFT_F32, "wgc delta: needs an FP64 and an FP32 plan");
+  GB_REQUIRE(fabs(d64->alpha - d32->alpha) < 1e-12 && fabs(d64->beta - d32->beta) < 1e-12,
+             "wgc delta: the FP64 and FP32 terms have different exponents");
+  GB_REQUIRE(fabs(d64->rho0 - d32->rho0) <= 1e-6 * d64->rho0,
+             "wgc delta: the FP32 kernels were built at another mean density (%g vs %g)", d32->rho0, d64->rho0);
+  WgcBufs W64 = wgc_layout(p64, d64->work);
+  WgcBufs W32 = wgc_layout(p32, d32->work);
+  const int two = fabs(d64->alpha - d64->beta) > 1e-12;
+  const float a = (float)d64->alpha, b = (float)d64->beta;
+  float* f[6];
+  for (int i = 0; i < 6; ++i) f[i] = reinterpret_cast<float*>(W32.f[i]);
+  k_wgc_delta_prep<<<kBlocks, kThreads, 0, st>>>(p64->N, rho, rho_ref, d64->rho0, a, b, two, f[0], f[1], f[2], f[3],
+                                                 f[4], f[5]);
+  GB_CHECK_LAUNCH();
+  gb_count_launch();
+  if (wgc_plane(p32) && p32->wgc_pm && p32->wgc_pm_src == d32->kernels)
+    rc = wgc_xfields_plane(p32, W32, two, p32->wgc_pm, nullptr, d32, st);
+  else
+    rc = wgc_xfields<float>(p32, W32, two, d32->kernels, st);
+  if (rc) return rc;
+  const double* xr[6];
+  for (int i = 0; i < 6; ++i) xr[i] = reinterpret_cast<const double*>(W64.f[two || i < 3 ? i : i - 3]);
+  const float* dy[3] = {f[two ? 3 : 0], f[two ? 4 : 1], f[two ? 5 : 2]};
+  if (calc_e)
+    k_wgc_delta_final<true><<<kBlocks, kThreads, 0, st>>>(p64->N, rho, rho_ref, d64->rho0, a, b, two, xr[0], xr[1],
+                                                          xr[2], xr[3], xr[4], xr[5], f[0], f[1], f[2], dy[0], dy[1],
+                                                          dy[2], W64.vref, pot, W64.part);
+  else
+    k_wgc_delta_final<false><<<kBlocks, kThreads, 0, st>>>(p64->N, rho, rho_ref, d64->rho0, a, b, two, xr[0], xr[1],
+                                                           xr[2], xr[3], xr[4], xr[5], f[0], f[1], f[2], dy[0], dy[1],
+                                                           dy[2], W64.vref, pot, W64.part);
+  GB_CHECK_LAUNCH();
+  gb_count_launch();
+  if (calc_e) {
+    k_wgc_energy<<<1, 256, 0, st>>>(W64.part, kBlocks, p64->dV, energies, nullptr, W64.eref);
+    GB_CHECK_LAUNCH();
+    gb_count_launch();
+  }
+  return 0;
 }
 
 extern "C" {
@@ -294,6 +551,23 @@ int gbofdft_wgc_kernels(gbofdft_plan* p, double rho0, double alpha, double beta,
     k_wgc_kernels<float><<<nblk, 256, 0, st>>>(p->gi, tkf, C, table, m, t0, h, (float*)out);
   GB_CHECK_LAUNCH();
   gb_count_launch();
+  if (wgc_plane(p)) {
+    // plans with the plane pipeline keep a plane-major copy (allocated with
+    // the first kernels built on the plan)
+    if (!p->wgc_pm) {
+      cudaError_t e = cudaMalloc(&p->wgc_pm, sizeof(float) * 4 * (size_t)p->NG);
+      if (e != cudaSuccess) {
+        p->wgc_pm = nullptr;
+        return gb_set_error(GBOFDFT_ERR_ALLOC, "wgc kernels: plane-major copy: %s", cudaGetErrorString(e));
+      }
+    }
+    const int64_t n4 = 4 * total;
+    k_wgc_kernels_pm<<<(int)((n4 + 255) / 256 > 4096 ? 4096 : (n4 + 255) / 256), 256, 0, st>>>(
+        p->gi, reinterpret_cast<const float*>(out), p->wgc_pm);
+    GB_CHECK_LAUNCH();
+    gb_count_launch();
+    p->wgc_pm_src = out;
+  }
   return GBOFDFT_OK;
 }
 

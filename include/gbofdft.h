@@ -110,9 +110,13 @@ int gbofdft_convolve(gbofdft_plan* plan, const void* in, void* out, int kernel, 
  * array inside the library (held by every GPU that loads it, until exit).
  * Grids whose scratch does not fit are rejected (GBOFDFT_ERR_UNSUPPORTED),
  * e.g. 96^3 fits in FP64, 128^3 in FP32 only.  All calls share the array:
- * calls that overlap on the GPU race; serialise them.  The first call on a
- * device looks the array up (cudaGetSymbolAddress): make it before any
- * stream capture.  Same arguments and result as gbofdft_convolve otherwise.
+ * calls that overlap on the GPU race; serialise them (a call that fails part
+ * way may also leave the array rewritten).  The first call on a device looks
+ * the array up (cudaGetSymbolAddress) and keeps the address for the process:
+ * make it before any stream capture; a device reset or another context on
+ * the same device is not supported.  Same arguments as gbofdft_convolve; the
+ * result equals its result to rounding (the twiddles are computed on the
+ * device instead of on the host).
  */
 int gbofdft_convolve_noalloc(const int nr[3], const double lattice[9], int precision, int full, const void* in,
                              void* out, int kernel, const void* kernel_array, double coef, void* stream);
@@ -177,6 +181,8 @@ typedef struct gbofdft_wgc {
   int64_t work_bytes;              /* >= gbofdft_wgc_workspace_bytes */
 } gbofdft_wgc;
 
+/* Bytes of the term's workspace; FP64 plans also hold a delta-evaluation
+ * reference (see gbofdft_eval_delta). */
 int gbofdft_wgc_workspace_bytes(const gbofdft_plan* plan, int64_t* bytes);
 int gbofdft_wgc_kernels(gbofdft_plan* plan, double rho0, double alpha, double beta, const double* table, int m,
                         double t0, double h, void* kernels_out, void* stream);
@@ -219,8 +225,15 @@ int gbofdft_eval(gbofdft_plan* plan, const void* rho, const gbofdft_functional* 
  * and its FP64 C(rho_ref); a delta evaluation transforms the change of g in
  * FP32 (plane pipeline of hplan) and runs the pointwise terms in FP64, so its
  * error is ~1e-7 of the change rather than of C.  rebase = 1 runs the full
- * FP64 evaluation (gbofdft_eval) at rho and makes rho the reference.  The LWT
- * and WGC terms, when present, are always evaluated in full FP64.
+ * FP64 evaluation (gbofdft_eval) at rho and makes rho the reference.  The WGC
+ * term, when f and hf both have one, is evaluated the same way: the rebase
+ * keeps its X / Y fields, NL potential and energy in the FP64 term's
+ * workspace, and a delta evaluation transforms the change of its transform
+ * inputs (rho^b, u rho^b, u^2 rho^b and the same with a) in FP32 and forms
+ * the potential and energy as FP32 changes on that reference (the FP64 WGC
+ * workspace must not be used for other evaluations between a rebase and the
+ * delta evaluations that follow it).  The LWT term is always evaluated in
+ * full FP64.
  * plan: FP64, hplan: FP32 on the same grid (a plane-pipeline size); f: the
  * FP64 functional, hf: the same terms in FP32 (its WT kernel table built on
  * hplan).  Other arguments as gbofdft_eval.

@@ -644,3 +644,20 @@ def test_tn_gaas_recpot_matches_reference_test(api, golden):
     E = total.Energy(rho)
     assert np.isclose(E, -43.3046)
     assert abs(E - float(d["E_final"])) < 1e-6 * len(symbols), (E, float(d["E_final"]))
+
+
+def test_tn_wgc_mixed_delta_refine_matches_full_refine(api):
+    """WGC: the refinement with delta evaluations (the WGC term included)
+    against the same refinement with every FP64 evaluation in full: energies
+    within 1e-9 eV/atom, forces within 1e-6 Ha/Bohr."""
+    from dftpy_gb300 import batch
+    st = systems.config_alloy(2)
+    res = {}
+    for delta in (True, False):
+        r = batch.optimize_batch([st], workers=1, kedf="WGC",
+                                 options={"precision": "mixed", "econv_per_atom": 1e-8, "refine_delta": delta})[0]
+        assert r.converged == 0
+        res[delta] = r
+    assert res[True].stats["stages"][-1]["n_eval_delta"] > 0
+    assert res[False].stats["stages"][-1]["n_eval_delta"] == 0
+    assert abs(res[True].energy - res[False].energy) < 1e-9 / 27.211386 * st.nat

@@ -175,3 +175,57 @@ def test_delta_create_rejects_unspecialised_grid(lib):
     q32 = lib.Plan((64, 64, 64), _lat((64, 64, 64)), precision=lib.F32)
     with pytest.raises(ValueError, match="different grids"):
         lib.Delta(p64, q32)
+
+
+def test_wgc_delta_matches_full_fp64(lib):
+    """The WGC term (second-order density-dependent kernel, alpha != beta, six
+    transformed fields) as a delta evaluation: the rebase keeps its X / Y
+    fields, potential and energy; a delta evaluation at the reference repeats
+    the full result, and at a moved density it matches a full FP64
+    evaluation within the tolerances above."""
+    torch = pytest.importorskip("torch")
+    from dftpy_gb300 import batch, systems
+    from dftpy_gb300.field import DirectField
+    st = systems.fcc_supercell((2, 2, 2), sigma=0.15, seed=4, nr=(64, 64, 64), mg_fraction=0.25, name="wgc_delta")
+    total, rho_u = batch.build_evaluator(st, kedf="WGC")
+    grid = rho_u.grid
+    mean = st.nelec / st.volume
+    base = _density(st.nr, seed=7)
+    ra = base * (mean / base.mean())
+    for eps in (1e-5, 1e-3):
+        rb = ra * (1.0 + _change(st.nr, eps, seed=8))
+        rho_a = torch.tensor(ra, dtype=torch.float64, device="cuda")
+        rho_b = torch.tensor(rb, dtype=torch.float64, device="cuda")
+        f64 = total.spec(DirectField(grid, data=rho_a)).ctypes()
+        f32 = total.spec(DirectField(grid, data=rho_a.to(torch.float32))).ctypes()
+        assert f64.wgc and f32.wgc
+        delta = lib.Delta(grid.plan(torch.float64), grid.plan(torch.float32))
+
+        def run(rho, rebase=None):
+            pot = torch.empty_like(rho)
+            en = torch.zeros(lib.NE, dtype=torch.float64, device="cuda")
+            if rebase is None:
+                lib.check(lib.load().gbofdft_eval(grid.plan(torch.float64).handle, lib.ptr(rho), f64, lib.ptr(pot),
+                                                  lib.ptr(en), lib.CALC_E | lib.CALC_V, lib.stream_ptr()))
+            else:
+                lib.check(lib.load().gbofdft_eval_delta(delta.handle, lib.ptr(rho), f64, f32, lib.ptr(pot),
+                                                        lib.ptr(en), lib.CALC_E | lib.CALC_V, int(rebase),
+                                                        lib.stream_ptr()), "eval_delta")
+            torch.cuda.synchronize()
+            return en.cpu().numpy(), pot.cpu().numpy()
+
+        e_a, v_a = run(rho_a, rebase=True)          # full evaluation, kept as the reference
+        e_0, v_0 = run(rho_a, rebase=False)
+        e_b, v_b = run(rho_b, rebase=False)
+        e_fb, v_fb = run(rho_b)                     # full FP64 (overwrites the reference's fields)
+        e_fa, v_fa = run(rho_a)
+        np.testing.assert_array_equal(e_a, e_fa)
+        np.testing.assert_array_equal(v_a, v_fa)
+        scale_e = np.abs(e_fa[:6]).sum()
+        assert abs(e_0[-1] - e_fa[-1]) <= 1e-12 * scale_e
+        assert np.abs(v_0 - v_fa).max() <= 1e-12 * np.abs(v_fa).max()
+        tol_e = (1e-6 * eps + 1e-12) * scale_e
+        assert np.abs(e_b[:6] - e_fb[:6]).max() <= tol_e, (eps, e_b - e_fb, tol_e)
+        assert abs(e_b[-1] - e_fb[-1]) <= tol_e
+        assert np.abs(v_b - v_fb).max() <= (5e-5 * eps + 1e-12) * np.abs(v_fb).max(), eps
+        assert abs((e_b[-1] - e_a[-1]) - (e_fb[-1] - e_fa[-1])) <= tol_e

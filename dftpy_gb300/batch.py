@@ -109,9 +109,13 @@ def optimize_batch(jobs, workers=None, options=None, kedf="WGC", guess=None, **k
     slots = list(range(workers))
     lock = threading.Lock()
     if guess is not None:
-        # the network's lazily packed weights are made once, here, not by
-        # racing worker threads
-        guess.prepare(prepared[0][0], prepared[0][1].grid)
+        # the network's packed weights and the per-grid-shape feature tables
+        # are made here, once per grid shape, not by racing worker threads
+        shapes = {}
+        for total, rho0, _ in prepared:
+            shapes.setdefault(tuple(int(x) for x in rho0.grid.nrR), (total, rho0.grid))
+        for total, grid in shapes.values():
+            guess.prepare(total, grid)
     # set-up work queued on the default stream (device copies of the inputs)
     # must be complete before other streams read it
     torch.cuda.synchronize()

@@ -49,6 +49,14 @@ _TABLES = {}
 _SMALL = {}
 
 
+def _publish(obj):
+    """A device object about to be shared between threads and streams: wait
+    for the copies that made it on the creating stream, so a solve on another
+    stream never reads it half-written."""
+    torch.cuda.current_stream().synchronize()
+    return obj
+
+
 def _cached(key, make):
     """Small structure-independent device arrays (PME moduli of a grid,
     species indices of a symbol list), kept by key."""
@@ -56,7 +64,7 @@ def _cached(key, make):
     if v is None:
         if len(_SMALL) >= 256:
             _SMALL.clear()
-        v = _SMALL[key] = make()
+        v = _SMALL[key] = _publish(make())
     return v
 
 
@@ -70,7 +78,7 @@ def _radial_table(q, v):
     if t is None:
         if len(_TABLES) >= 64:
             _TABLES.clear()
-        t = _TABLES[key] = _RadialTable(q, v)
+        t = _TABLES[key] = _publish(_RadialTable(q, v))
     return t
 
 

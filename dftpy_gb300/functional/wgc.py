@@ -146,9 +146,10 @@ class WGCTerm:
             t = _DEVICE_TABLES.get(key)
             if t is None:
                 t0, h, cols = kernel_table(self.alpha, self.beta, self.gamma, self.x, self.order)
-                t = _DEVICE_TABLES[key] = (t0, h, cols.shape[1],
-                                           torch.tensor(np.ascontiguousarray(cols), dtype=torch.float64,
-                                                        device="cuda"))
+                dev = torch.tensor(np.ascontiguousarray(cols), dtype=torch.float64, device="cuda")
+                # shared by every thread and stream: complete before publishing
+                torch.cuda.current_stream().synchronize()
+                t = _DEVICE_TABLES[key] = (t0, h, cols.shape[1], dev)
             self._table = t
         return self._table
 

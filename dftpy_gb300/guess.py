@@ -21,6 +21,7 @@ the project's own (``gbofdft_nn_*``).
 """
 import ctypes
 import math
+import threading
 import time
 
 import numpy as np
@@ -29,6 +30,8 @@ import torch
 from . import _lib, systems
 
 SQRT_CLAMP = 1e-30
+
+_PACK_LOCK = threading.Lock()
 
 
 def _L():
@@ -51,16 +54,73 @@ class Conv:
         self.mw, self.vw = torch.zeros_like(self.w), torch.zeros_like(self.w)
         self.mb, self.vb = torch.zeros_like(self.b), torch.zeros_like(self.b)
         self.wtc = None            # BF16 weights packed for the tensor-core kernel (made on first use)
+        self.wtc_t = None          # ... of the input-gradient convolution (training)
         self.sync_bf16()
 
     def sync_bf16(self):
         _lib.check(_L().gbofdft_nn_to_bf16(_lib.ptr(self.w), _lib.ptr(self.wb), self.w.numel(), _lib.stream_ptr()))
         self.wtc = None
+        self.wtc_t = None
 
     def _tc_cout(self):
         """Output width of the tensor-core kernel (a layer narrower than 16
         channels runs 16 wide with zero weights and stores its own)."""
         return 16 if self.cout < 16 else self.cout
+
+    def pack_tc(self, publish=True):
+        """Pack the BF16 weights for the tensor-core kernel.  publish: the
+        packed copy is made visible only once the packing has finished on this
+        stream, so guesses on other threads and streams may use it right away
+        (training, on one stream, skips that wait)."""
+        with _PACK_LOCK:
+            if self.wtc is not None:
+                return
+            cw = self._tc_cout()
+            wb = self.wb
+            if cw != self.cout:
+                wb = torch.zeros((cw, self.cin, 27), dtype=torch.bfloat16, device="cuda")
+                wb[:self.cout] = self.wb
+            wtc = torch.empty(27 * self.cin * cw, dtype=torch.bfloat16, device="cuda")
+            _lib.check(_L().gbofdft_nn_conv3d_tc_pack(_lib.ptr(wb), self.cin, cw, _lib.ptr(wtc),
+                                                      _lib.stream_ptr()), "nn_conv3d_tc_pack")
+            if publish:
+                torch.cuda.current_stream().synchronize()
+            self.wtc = wtc
+
+    def _tc_cin_t(self):
+        """Output width of the transposed convolution on the tensor cores."""
+        return 16 if self.cin < 16 else self.cin
+
+    def pack_tc_t(self):
+        """Packed weights of the input-gradient convolution: the transposed,
+        tap-reversed kernel (C_out -> C_in) of this periodic convolution."""
+        if self.wtc_t is None:
+            cw = self._tc_cin_t()
+            wt = torch.zeros((cw, self.cout, 27), dtype=torch.bfloat16, device="cuda")
+            wt[:self.cin] = self.wb.permute(1, 0, 2).flip(2)
+            wtc = torch.empty(27 * self.cout * cw, dtype=torch.bfloat16, device="cuda")
+            _lib.check(_L().gbofdft_nn_conv3d_tc_pack(_lib.ptr(wt), self.cout, cw, _lib.ptr(wtc),
+                                                      _lib.stream_ptr()), "nn_conv3d_tc_pack")
+            self.wtc_t = wtc
+        return self.wtc_t
+
+    def tc_dgrad_supported(self, shape):
+        D, H, W = shape
+        return bool(_L().gbofdft_nn_conv3d_tc_supported(self.cout, self._tc_cin_t(), D, H, W))
+
+    def forward_z(self, x, shape, err, tc):
+        """conv + bias without activation (the training forward): on the
+        tensor cores (BF16 operands, FP32 accumulation) where the layer shape
+        has a kernel and tc is set, else on the CUDA cores in FP32."""
+        if tc and self.tc_supported(shape):
+            if self.wtc is None:
+                self.pack_tc(publish=False)
+            return self.forward_tc(x, shape, False, err)
+        return self.forward(x, shape)
+
+    def tc_channels(self):
+        """The tensor-core kernel has this layer's channel pair."""
+        return bool(_L().gbofdft_nn_conv3d_tc_supported(self.cin, self._tc_cout(), 16, 16, 16))
 
     def tc_supported(self, shape):
         D, H, W = shape
@@ -73,13 +133,7 @@ class Conv:
         D, H, W = shape
         cw = self._tc_cout()
         if self.wtc is None:
-            wb = self.wb
-            if cw != self.cout:
-                wb = torch.zeros((cw, self.cin, 27), dtype=torch.bfloat16, device="cuda")
-                wb[:self.cout] = self.wb
-            self.wtc = torch.empty(27 * self.cin * cw, dtype=torch.bfloat16, device="cuda")
-            _lib.check(_L().gbofdft_nn_conv3d_tc_pack(_lib.ptr(wb), self.cin, cw, _lib.ptr(self.wtc),
-                                                      _lib.stream_ptr()), "nn_conv3d_tc_pack")
+            self.pack_tc()
         z = torch.empty((self.cout, D, H, W), dtype=torch.float32, device="cuda")
         _lib.check(_L().gbofdft_nn_conv3d_tc(_lib.ptr(x), self.cin, _lib.ptr(self.wtc), _lib.ptr(self.b), _lib.ptr(z),
                                              cw, self.cout, D, H, W, 1 if act else 0,
@@ -107,14 +161,21 @@ class Conv:
                                           self.cout, D, H, W, 0, _lib.stream_ptr()), "nn_conv3d")
         return z
 
-    def backward(self, x, gz, shape, need_input_grad=True):
-        """Weight and bias gradients (overwritten) and the input gradient."""
+    def backward(self, x, gz, shape, need_input_grad=True, tc=False, err=None):
+        """Weight and bias gradients (overwritten) and the input gradient (on
+        the tensor cores where tc is set and the shape has a kernel)."""
         D, H, W = shape
         _lib.check(_L().gbofdft_nn_conv3d_wgrad(_lib.ptr(x), self.cin, _lib.ptr(gz), self.cout, D, H, W,
                                                 _lib.ptr(self.gw), _lib.ptr(self.gb), _lib.stream_ptr()),
                    "nn_conv3d_wgrad")
         if not need_input_grad:
             return None
+        if tc and err is not None and self.tc_dgrad_supported(shape):
+            gx = torch.empty((self.cin, D, H, W), dtype=torch.float32, device="cuda")
+            _lib.check(_L().gbofdft_nn_conv3d_tc(_lib.ptr(gz), self.cout, _lib.ptr(self.pack_tc_t()), None,
+                                                 _lib.ptr(gx), self._tc_cin_t(), self.cin, D, H, W, 0, None, 0,
+                                                 _lib.ptr(err), _lib.stream_ptr()), "nn_conv3d_tc_dgrad")
+            return gx
         gx = torch.empty((self.cin, D, H, W), dtype=torch.float32, device="cuda")
         _lib.check(_L().gbofdft_nn_conv3d(_lib.ptr(gz), self.cout, _lib.ptr(self.wb), None, _lib.ptr(gx), self.cin,
                                           D, H, W, 1, _lib.stream_ptr()), "nn_conv3d_t")
@@ -126,6 +187,7 @@ class Conv:
         _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.w), _lib.ptr(self.gw), _lib.ptr(self.mw), _lib.ptr(self.vw),
                                      _lib.ptr(self.wb), self.w.numel(), lr, b1, b2, eps, step, s))
         self.wtc = None
+        self.wtc_t = None
         _lib.check(L.gbofdft_nn_adam(_lib.ptr(self.b), _lib.ptr(self.gb), _lib.ptr(self.mb), _lib.ptr(self.vb),
                                      None, self.b.numel(), lr, b1, b2, eps, step, s))
 
@@ -211,23 +273,31 @@ class GuessNet:
     def stride(self):
         return 2 ** (len(self.channels) - 1)
 
-    def forward(self, x, keep=False, tc=True):
+    def forward(self, x, keep=False, tc=True, tc_train=False):
         """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward
-        needs (FP32 activations, CUDA-core kernels).  Without keep the inner
-        layers run on the tensor cores (BF16 activations) when tc is set."""
+        needs; its convolutions run in FP32 on the CUDA cores, or with
+        tc_train on the tensor cores where the layer shape has a kernel (BF16
+        operands, FP32 pre-activations kept).  Without keep the inner layers
+        run on the tensor cores (BF16 activations) when tc is set."""
         shape = tuple(x.shape[1:])
         if any(s % self.stride for s in shape):
             raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
         if not keep:
             return self._infer(x, shape, tc)
+        # one device flag of timed-out tensor-core waits for the whole
+        # training run (read once per epoch)
+        if tc_train and getattr(self, "_err_train", None) is None:
+            self._err_train = torch.zeros(1, dtype=torch.int32, device="cuda")
+        err = self._err_train if tc_train else None
+        self._err = err
         tape = []
         skips = []
         h = x
         for lvl, (c1, c2) in enumerate(self.enc):
             sh = tuple(h.shape[1:])
-            z1 = c1.forward(h, sh)
+            z1 = c1.forward_z(h, sh, err, tc_train)
             a1 = silu(z1)
-            z2 = c2.forward(a1, sh)
+            z2 = c2.forward_z(a1, sh, err, tc_train)
             a2 = silu(z2)
             tape.append(("enc", lvl, h, z1, a1, z2))
             skips.append(a2)
@@ -236,10 +306,10 @@ class GuessNet:
             lvl = len(self.channels) - 2 - k
             u = up2(h)
             sh = tuple(u.shape[1:])
-            z1 = c1.forward(u, sh)
+            z1 = c1.forward_z(u, sh, err, tc_train)
             a1 = silu(z1)
             s = add(a1, skips[lvl])
-            z2 = c2.forward(s, sh)
+            z2 = c2.forward_z(s, sh, err, tc_train)
             h = silu(z2)
             tape.append(("dec", lvl, u, z1, s, z2))
         out = self.head.forward(h, shape)
@@ -277,6 +347,8 @@ class GuessNet:
             raise RuntimeError("forward(keep=True) must precede backward")
         _, _, h = tape[-1]
         shape = tuple(h.shape[1:])
+        err = getattr(self, "_err", None)
+        tc = err is not None
         g = self.head.backward(h, gout, shape)
         gskip = {}
         for k in range(len(self.dec) - 1, -1, -1):
@@ -284,10 +356,10 @@ class GuessNet:
             c1, c2 = self.dec[k]
             sh = tuple(u.shape[1:])
             gz2 = silu_bwd(z2, g)
-            gs = c2.backward(s, gz2, sh)
+            gs = c2.backward(s, gz2, sh, tc=tc, err=err)
             gskip[lvl] = gs
             gz1 = silu_bwd(z1, gs)
-            gu = c1.backward(u, gz1, sh)
+            gu = c1.backward(u, gz1, sh, tc=tc, err=err)
             g = up2_bwd(gu)
         for lvl in range(len(self.enc) - 1, -1, -1):
             _, _, hin, z1, a1, z2 = tape[lvl]
@@ -298,9 +370,9 @@ class GuessNet:
             if lvl in gskip:
                 g = add(g, gskip[lvl])
             gz2 = silu_bwd(z2, g)
-            ga1 = c2.backward(a1, gz2, sh)
+            ga1 = c2.backward(a1, gz2, sh, tc=tc, err=err)
             gz1 = silu_bwd(z1, ga1)
-            g = c1.backward(hin, gz1, sh, need_input_grad=lvl > 0)
+            g = c1.backward(hin, gz1, sh, need_input_grad=lvl > 0, tc=tc, err=err)
         self._tape = None
 
     def adam_step(self, lr):
@@ -359,9 +431,14 @@ class LearnedGuess:
         self.net = net
 
     def prepare(self, total, grid=None):
-        """Make the network's packed tensor-core weights (and the cached
-        set-up of the features) by one guess on the current stream; callers
-        that guess from several threads call this first."""
+        """Make the network's packed tensor-core weights (every layer whose
+        channel pair has a tensor-core kernel, whatever the grid) and the
+        cached set-up of the features by one guess on the current stream;
+        callers that guess from several threads call this first, once per
+        grid shape."""
+        for layer in self.net.layers:
+            if layer.wtc is None and layer.tc_channels():
+                layer.pack_tc()
         self.guess(total, grid)
         torch.cuda.synchronize()
 
@@ -413,9 +490,12 @@ def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 6
     return data
 
 
-def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None):
+def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None, tc=True):
     """Adam on the normalised squared error of sqrt(rho) (one cell per step),
-    random periodic translations; cosine learning-rate decay."""
+    random periodic translations; cosine learning-rate decay.  tc: forward and
+    input-gradient convolutions on the tensor cores where a layer's shape has
+    a kernel (BF16 operands, FP32 accumulation); weight gradients on the CUDA
+    cores."""
     L = _L()
     nb = ctypes.c_int64()
     _lib.check(L.gbofdft_nn_sqerr_work_bytes(ctypes.byref(nb)))
@@ -434,7 +514,7 @@ def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None):
             x_ = torch.roll(x, shifts=sh, dims=(1, 2, 3)).contiguous()
             pb = torch.roll(phib, shifts=sh, dims=(0, 1, 2)).contiguous()
             pt = torch.roll(phit, shifts=sh, dims=(0, 1, 2)).contiguous()
-            out = net.forward(x_, keep=True)
+            out = net.forward(x_, keep=True, tc_train=tc)
             s0 = math.sqrt(rho0)
             pred = (pb + s0 * out[0]).contiguous()
             grad = torch.empty_like(pred)
@@ -448,6 +528,9 @@ def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None):
         hist.append(tot / len(data))
         if log:
             log("epoch %d loss %.3e" % (ep, hist[-1]))
+        err = getattr(net, "_err", None)
+        if err is not None and int(err.item()) != 0:
+            raise RuntimeError("tensor-core convolution: a wait timed out (code %d)" % int(err.item()))
     return hist
 
 

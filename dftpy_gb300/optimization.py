@@ -108,14 +108,13 @@ class Optimization:
 
     # ------------------------------------------------------------------------
     def _check(self):
-        if self.optimization_method != "TN":
-            raise NotImplementedError("optimization_method %r: this build implements the truncated-Newton "
-                                      "path (method 'TN')" % self.optimization_method)
+        if self.optimization_method not in FIRST_ORDER and self.optimization_method != "TN":
+            raise AttributeError("The %s direction method not implemented." % self.optimization_method)
         o = self.optimization_options
         if o["algorithm"] != "EMM" or o["vector"] != "Orthogonalization":
             raise NotImplementedError("only algorithm='EMM' with vector='Orthogonalization' is implemented")
         ev = self.EnergyEvaluator
-        if not (isinstance(ev, TotalFunctional) and ev.fusable()):
+        if self.optimization_method == "TN" and not (isinstance(ev, TotalFunctional) and ev.fusable()):
             raise NotImplementedError("the device optimiser needs a TotalFunctional of this package's "
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
@@ -177,7 +176,8 @@ class Optimization:
         return DirectField(grid, data=r), out
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False):
-        """``optimization.py:281-520`` (method TN)."""
+        """``optimization.py:281-520``: the device TN driver, or the first-order
+        methods (``_optimize_first_order``)."""
         if guess_rho is None and self.rho is None:
             raise AttributeError("Must provide a guess density")
         if guess_rho is not None:
@@ -189,6 +189,8 @@ class Optimization:
         rho = self.rho
         if not isinstance(rho, DirectField):
             raise TypeError("guess_rho must be a DirectField")
+        if self.optimization_method in FIRST_ORDER:
+            return self._optimize_first_order(rho)
         prec = o["precision"] or ("fp64" if rho.dtype == torch.float64 else "fp32")
         self.stats = {"stages": []}
         t_start = time.perf_counter()
@@ -245,6 +247,104 @@ class Optimization:
         self._functional = None
         return r
 
+    # ------------------------------------------------------------------------
+    def _optimize_first_order(self, rho):
+        """``optimize_rho`` (``optimization.py:281-520``) with a first-order
+        direction: the conjugate gradients of ``get_direction_CG``
+        (``math_utils.py:396-426``: CG-HS, the reference's default, and CG-PR,
+        CG-DY, CG-CD, CG-LS, CG-FR), ``LBFGS`` (``math_utils.py:374-395,
+        433-455``; ``h0`` in the options, as the reference requires) or ``GD``.
+        The loop is the reference's -- orthogonal rotation of phi, the
+        Moré-Thuente line search (the library's ``gbofdft_dcsrch``) on the
+        rotation angle, energy-change convergence test -- driven from the host
+        with every field on the device: each trial is one evaluation through
+        ``torch.ops.gbofdft.eval``, the field algebra and the FP64 reductions
+        are device operations on the density's tensors."""
+        o = self.optimization_options
+        method = self.optimization_method
+        grid = rho.grid
+        dV = grid.dV
+        ev = self.EnergyEvaluator
+        t_start = time.perf_counter()
+        r = rho.as_subclass(torch.Tensor).to(torch.float64)
+
+        def integral(x):
+            return float(x.sum()) * dV
+
+        def evaluate(phi):
+            out = ev(DirectField(grid, data=phi * phi), calcType={"E", "V"})
+            return float(out.energy), out.potential.as_subclass(torch.Tensor)
+
+        phi = torch.where(r > 0, torch.sqrt(torch.clamp(r, min=0.0)), torch.full_like(r, 1e-300))
+        phi = phi * np.sqrt(float(r.sum()) / float((phi * phi).sum()))
+        energy, pot = evaluate(phi)
+        n_eval = 1
+
+        def mu_of(pot, phi):
+            rr = phi * phi
+            return integral(pot * rr) / integral(rr)
+
+        mu = mu_of(pot, phi)
+        res_a = [(pot - mu) * phi]
+        dir_a = []
+        history = [energy]
+        lbfgs = _Lbfgs(o["h0"], o["maxcor"]) if method == "LBFGS" else None
+        theta = 0.1
+        converged = 1
+        L = _lib.load()
+        it = 0
+        for it in range(1, o["maxiter"]):
+            p = _direction(method, res_a, dir_a, lbfgs)
+            p, theta0 = _orthonormalize(p, phi, dV)
+            if 2.0 * float((pot * phi * p).sum()) > 0:
+                p, theta0 = _orthonormalize(-res_a[-1], phi, dV)   # "Change to steepest descent"
+            theta = min(theta0, theta)
+
+            def value_deriv(t, phi=phi, p=p):
+                newphi = phi * np.cos(t) + p * np.sin(t)
+                e, v = evaluate(newphi)
+                p2 = p * np.cos(t) - phi * np.sin(t)
+                return e, 2.0 * float((v * newphi * p2).sum()) * dV, (newphi, e, v)
+
+            g0 = 2.0 * float((pot * phi * p).sum()) * dV
+            theta, payload, nls = _line_search(L, value_deriv, theta, energy, g0, o["c1"], o["c2"], np.pi, 0.0,
+                                               o["xtol"], o["maxls"])
+            n_eval += nls
+            if theta is None:
+                converged = 1
+                break
+            old_phi = phi
+            phi, energy, pot = payload
+            mu = mu_of(pot, phi)
+            res_a.append((pot - mu) * phi)
+            if lbfgs is not None:
+                lbfgs.update(phi - old_phi, res_a[-1] - res_a[-2])
+            history.append(energy)
+            if len(history) - 1 >= o["ncheck"] and all(abs(history[-2 - i] - energy) <= o["econv"]
+                                                          for i in range(o["ncheck"])):
+                converged = 0
+                break
+            dir_a.append(p)
+            if len(res_a) > 2:
+                res_a.pop(0)
+            if len(dir_a) > 2:
+                dir_a.pop(0)
+        else:
+            converged = 2
+        out_rho = DirectField(grid, data=(phi * phi).to(rho.dtype))
+        self.stats = {"stages": [dict(precision="fp64" if rho.dtype == torch.float64 else "fp32", method=method,
+                                      energy=energy, mu=mu, converged=converged, n_iter=it, n_eval_ev=n_eval,
+                                      n_eval_v=0, n_eval_hess=0, energies=[], history=list(history), n_sync=0,
+                                      t_sync=0.0, t_total=time.perf_counter() - t_start)],
+                      "t_wall": time.perf_counter() - t_start, "t_glue": 0.0}
+        self.converged = converged
+        self.mu = mu
+        self.energy = energy
+        self.history = history
+        self.rho = out_rho
+        self._functional = None
+        return out_rho
+
     def optimize_rho_multistep(self, guess_rho, multistep=2, nr_final=None):
         """Coarse-to-fine optimisation (the multi-step branch of
         ``OptimizeDensityConf``, ``interface.py:160-200``): optimise on the
@@ -289,6 +389,112 @@ class Optimization:
 
     def __call__(self, guess_rho=None, calcType={"E", "V"}, guess_phi=None, lphi=False):
         return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)
+
+
+FIRST_ORDER = ("CG-HS", "CG", "CG-PR", "CG-DY", "CG-CD", "CG-LS", "CG-FR", "LBFGS", "GD")
+
+
+def _dot(a, b):
+    return float((a * b).sum())
+
+
+def _direction(method, res_a, dir_a, lbfgs):
+    """``get_direction`` of the first-order methods (``math_utils.py:396-455``)."""
+    r1 = res_a[-1]
+    if method == "GD":
+        return -r1
+    if method == "LBFGS":
+        q = -r1
+        alphas = [0.0] * len(lbfgs.s)
+        # the reference's loop stops before i = 0
+        for i in range(len(lbfgs.s) - 1, 0, -1):
+            a = lbfgs.rho[i] * _dot(lbfgs.s[i], q)
+            alphas[i] = a
+            q = q - a * lbfgs.y[i]
+        if not lbfgs.H0:
+            gamma = 1.0 if len(lbfgs.s) < 1 else _dot(lbfgs.s[-1], lbfgs.y[-1]) / _dot(lbfgs.y[-1], lbfgs.y[-1])
+            d = gamma * q
+        else:
+            d = lbfgs.H0 * q
+        for i in range(len(lbfgs.s)):
+            b = lbfgs.rho[i] * _dot(lbfgs.y[i], d)
+            d = d + lbfgs.s[i] * (alphas[i] - b)
+        return d
+    if len(res_a) == 1:
+        beta = 0.0
+    else:
+        r0 = res_a[-2]
+        d0 = dir_a[-1] if dir_a else None
+        if method in ("CG-HS", "CG") and d0 is not None:
+            dr = r1 - r0
+            beta = _dot(r1, dr) / _dot(d0, dr)
+        elif method == "CG-PR":
+            beta = max(_dot(r1, r1 - r0) / _dot(r0, r0), 0.0)
+        elif method == "CG-DY" and d0 is not None:
+            beta = _dot(r1, r1) / _dot(d0, r1 - r0)
+        elif method == "CG-CD" and d0 is not None:
+            # kept as the reference has it: -(r1 ** 2) / sum(d0 r0) is a field,
+            # so the update is pointwise
+            beta = -(r1 * r1) / _dot(d0, r0)
+        elif method == "CG-LS" and d0 is not None:
+            beta = _dot(r1, r1 - r0) / _dot(d0, r0)
+        else:
+            beta = _dot(r1, r1) / _dot(r0, r0)
+    if not dir_a:
+        return -r1
+    return -r1 + beta * dir_a[-1]
+
+
+def _orthonormalize(p, phi, dV):
+    """``OrthogonalNormalization`` (``optimization.py:204-225``), vector
+    "Orthogonalization"."""
+    ne = float((phi * phi).sum()) * dV
+    p = p - (float((p * phi).sum()) * dV / ne) * phi
+    pn = float((p * p).sum()) * dV
+    return p * np.sqrt(ne / pn), float(np.sqrt(pn / ne))
+
+
+class _Lbfgs:
+    """``LBFGS`` history (``math_utils.py:374-395``): at most Bound + 1 pairs."""
+
+    def __init__(self, H0=1.0, Bound=5):
+        self.H0, self.Bound = H0, Bound
+        self.s, self.y, self.rho = [], [], []
+
+    def update(self, dx, dg):
+        if len(self.s) > self.Bound:
+            self.s.pop(0)
+            self.y.pop(0)
+            self.rho.pop(0)
+        self.s.append(dx)
+        self.y.append(dg)
+        self.rho.append(1.0 / _dot(dg, dx))
+
+
+def _line_search(L, func, alpha0, f0, g0, c1, c2, amax, amin, xtol, maxiter):
+    """``LineSearchDcsrch2`` (``math_utils.py:76-106``) with the library's
+    More-Thuente state machine; returns (alpha or None, payload, trials)."""
+    state = (ctypes.c_double * 32)()
+    state[0], state[1], state[2], state[3], state[4] = c1, c2, xtol, amin, amax
+    stp = ctypes.c_double(alpha0)
+    f, g = f0, g0
+    task = 0
+    payload = None
+    trials = 0
+    for _ in range(maxiter):
+        task = L.gbofdft_dcsrch(state, 32, ctypes.byref(stp), float(f), float(g), task)
+        if task < 0:
+            raise RuntimeError("gbofdft_dcsrch: %s" % _lib.last_error())
+        if task == 1:
+            f, g, payload = func(stp.value)
+            trials += 1
+        else:
+            break
+    else:
+        return None, payload, trials
+    if task in (3, 4):
+        return None, payload, trials
+    return stp.value, payload, trials
 
 
 def _workspace(grid, dtype, nbytes):

@@ -29,6 +29,8 @@ pseudo_files.npz  reciprocal tables of the reference's example pseudopotential
              stand-in in ``_shims`` for UPF).
 dcsrch.npz   trial-step sequences of the reference's Moré–Thuente line search
              (``LineSearchDcsrch2``) on analytic 1-D functions.
+first_order.npz  the reference's CG-HS, CG-PR and LBFGS solves of the
+             4-atom cell (energies, evaluation counts, forces).
 gaas.npz     the reference's own TN test (GaAs_random, recpot pseudopotentials,
              WT + LDA + Hartree, PME): structure, full reciprocal PP tables,
              converged energy and forces.
@@ -506,7 +508,33 @@ def gen_gaas():
     print("gaas: nr %s E=%.10f (reference test asserts -43.3046), %.1f s" % (list(nr), e_final, time.time() - t0))
 
 
-GENERATORS = {"gaas": gen_gaas, "fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files, "formats": gen_formats, "gridmap": gen_gridmap}
+def gen_first_order():
+    """The reference's first-order optimisers on the 4-atom cell (TFVW + LDA +
+    Hartree + analytic PP, PME, econv 1e-7 Ha, uniform start): CG-HS (its
+    default method), CG-PR and LBFGS (h0 = 1, which LBFGS requires)."""
+    st = systems.config_al4(seed=0)
+    out = {}
+    for name, method, extra in (("cghs", "CG-HS", {}), ("cgpr", "CG-PR", {}), ("lbfgs", "LBFGS", {"h0": 1.0})):
+        grid, ions, pseudo, total, funcs = build_total(st, "TFVW")
+        rho0 = DirectField(grid=grid)
+        rho0[:] = ions.get_ncharges() / ions.cell.volume
+        ev = CountingEvaluator(total)
+        opts = {"econv": 1e-7, "maxiter": 200}
+        opts.update(extra)
+        opt = Optimization(EnergyEvaluator=ev, optimization_method=method, optimization_options=opts)
+        t0 = time.time()
+        rho = opt.optimize_rho(guess_rho=rho0)
+        out[name + "_E_final"] = float(total.Energy(rho))
+        out[name + "_converged"] = int(opt.converged)
+        out[name + "_n_ev"] = ev.n_ev
+        out[name + "_E_history"] = np.array(ev.energies)
+        out[name + "_forces"] = total.get_forces(rho, ions=ions)
+        print("%s: E=%.10f converged %d, %d evaluations, %.1f s" % (method, out[name + "_E_final"],
+                                                                   opt.converged, ev.n_ev, time.time() - t0))
+    np.savez_compressed(HERE / "first_order.npz", **out)
+
+
+GENERATORS = {"first_order": gen_first_order, "gaas": gen_gaas, "fde": gen_fde, "al4": gen_al4, "al256": gen_al256, "dcsrch": gen_dcsrch, "guess": gen_guess, "al256_tight": gen_al256_tight, "stress": gen_stress, "pseudo_files": gen_pseudo_files, "formats": gen_formats, "gridmap": gen_gridmap}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS)

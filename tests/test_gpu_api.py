@@ -661,3 +661,34 @@ def test_tn_wgc_mixed_delta_refine_matches_full_refine(api):
     assert res[True].stats["stages"][-1]["n_eval_delta"] > 0
     assert res[False].stats["stages"][-1]["n_eval_delta"] == 0
     assert abs(res[True].energy - res[False].energy) < 1e-9 / 27.211386 * st.nat
+
+
+@pytest.mark.parametrize("name,method,extra", [("cghs", "CG-HS", {}), ("cgpr", "CG-PR", {}),
+                                               ("lbfgs", "LBFGS", {"h0": 1.0})])
+def test_first_order_methods_match_reference(api, golden, name, method, extra):
+    """The reference's first-order optimisers (CG-HS is its default method) on
+    the 4-atom cell against the reference's own runs: the same starting
+    energy (1e-9 Ha), convergence status, evaluation count within 2, final
+    energy within 1e-6 Ha/atom and forces within 1e-5 Ha/Bohr."""
+    d = golden("first_order")
+    st = systems.config_al4(0)
+    F = api["functional"]
+    grid = api["grid"].DirectGrid(st.lattice, st.nr, full=False)
+    ps = F.LocalPseudo(grid=grid, ions=_ions(api, st), PP_list=_pp(api, st.symbols), PME=True)
+    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="TFVW"),
+                              XCFunctional=F.Functional(type="XC", name="LDA"),
+                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    rho0 = api["field"].DirectField(grid)
+    rho0[:] = st.nelec / st.volume
+    opts = {"econv": 1e-7, "maxiter": 200}
+    opts.update(extra)
+    kw = {} if method == "CG-HS" else {"optimization_method": method}
+    opt = api["opt"].Optimization(EnergyEvaluator=total, optimization_options=opts, **kw)
+    rho = opt.optimize_rho(guess_rho=rho0)
+    h_ref = d[name + "_E_history"]
+    assert opt.converged == int(d[name + "_converged"])
+    assert abs(opt.stats["stages"][0]["n_eval_ev"] - int(d[name + "_n_ev"])) <= 2
+    assert abs(opt.history[0] - h_ref[0]) < 1e-9
+    E = total.Energy(rho)
+    assert abs(E - float(d[name + "_E_final"])) < 1e-6 * st.nat
+    assert np.abs(total.get_forces(rho) - d[name + "_forces"]).max() < 1e-5

@@ -234,3 +234,29 @@ def test_al_network_gain_on_al256(gn):
     n_l = sum(s["n_eval_ev"] + s["n_eval_v"] + s.get("n_eval_hess", 0) for s in o_l.stats["stages"])
     assert n_l < 0.85 * n_u, (n_l, n_u)
     assert abs(o_l.energy - o_u.energy) / st.nat * 27.211386 < 1e-8
+
+
+def test_tensor_core_training_matches_fp32(gn):
+    """Training on the tensor cores (forward and input-gradient convolutions
+    with BF16 operands where a layer's shape has a kernel, weight gradients on
+    the CUDA cores) against the FP32 CUDA-core path on a 32^3 cell with the
+    16-64 channel network: the output within 2e-2 of its norm and every
+    layer's weight gradient within 5e-2 of the FP32 gradient's norm (BF16
+    operands carry 8 mantissa bits)."""
+    import torch
+    net = gn.GuessNet(channels=(16, 32, 48, 64), seed=3)
+    rng = np.random.default_rng(8)
+    x = torch.tensor(rng.standard_normal((2, 32, 32, 32)).astype(np.float32), device="cuda")
+    c = torch.tensor(rng.standard_normal((1, 32, 32, 32)).astype(np.float32), device="cuda")
+    assert any(l.tc_supported((32, 32, 32)) for l in net.layers)
+    res = {}
+    for tc in (False, True):
+        out = net.forward(x, keep=True, tc_train=tc)
+        net.backward(c)
+        res[tc] = (out.clone(), [l.gw.clone() for l in net.layers])
+    o32, g32 = res[False]
+    otc, gtc = res[True]
+    assert float((otc - o32).norm() / o32.norm()) < 2e-2
+    for i, (a, b) in enumerate(zip(gtc, g32)):
+        assert float((a - b).norm() / b.norm()) < 5e-2, i
+    assert int(net._err_train.item()) == 0

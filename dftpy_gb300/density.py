@@ -101,13 +101,20 @@ def get_3d_value_recipe(r, arho, ions, grid, ncharge=None, rho=None, dtol=0.0, d
     plan = grid.plan(dtype)
     tables = [_radial_table(r[k], arho[k]) for k in keys]
     tabs = (_lib.VTable * len(keys))(*[t.ctypes() for t in tables])
-    # one host-to-device copy per call (each pageable copy waits for the
-    # stream); the species indices and the PME moduli are cached
+    # positions and species indices: copies on this stream; the PME moduli of
+    # the grid shape and the radial tables are cached and shared by every
+    # stream, so this stream is recorded on them: should a cache drop one,
+    # its memory is not reused before this stream's kernels have read it
     spos = torch.from_numpy(np.ascontiguousarray(ions.get_scaled_positions(), dtype=np.float64)).to("cuda")
-    species = _cached(("species", tuple(keys), tuple(ions.symbols)),
-                      lambda: torch.tensor([keys.index(s) for s in ions.symbols], dtype=torch.int32, device="cuda"))
+    species = torch.tensor([keys.index(s) for s in ions.symbols], dtype=torch.int32, device="cuda")
     bm = _cached(("bm", tuple(int(x) for x in grid.nrR), int(order)),
                  lambda: torch.tensor(pme_bm(grid.nrR, order).view(np.float64), device="cuda")) if pme else None
+    cur = torch.cuda.current_stream()
+    for t in tables:
+        t.x.record_stream(cur)
+        t.c.record_stream(cur)
+    if bm is not None:
+        bm.record_stream(cur)
     nb = _lib.setup_workspace_bytes(plan, ions.nat)
     work = torch.empty(nb // 8 + 64, dtype=torch.float64, device="cuda")
     n0, n1, n2 = (int(x) for x in grid.nrR)

@@ -1,10 +1,13 @@
-"""Repeat the functional evaluation of the 256-atom / 128^3 WT workload.
+"""Repeat the functional evaluation of the 256-atom / 128^3 WT workload (or
+of one Al/Mg alloy snapshot of the batched WGC workload, ``--workload alloy
+--seed S``).
 
 ``python -m dftpy_gb300.profile_eval --precision fp32 --calc V --reps 3``
 sets the structure up, runs warm-up evaluations, then ``reps`` evaluations
 inside an NVTX range named ``eval`` (so a profiler can select exactly those
 launches with ``--nvtx --nvtx-include eval/``) and prints the CUDA-event
-time per evaluation.
+time per evaluation.  ``--solve mixed`` runs whole TN solves instead (NVTX
+range ``solve``), on this thread and stream.
 """
 import argparse
 import os
@@ -17,7 +20,8 @@ def main():
     p.add_argument("--calc", default="V", choices=["V", "EV"])
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--workload", default="al256", choices=["al256", "al4"])
+    p.add_argument("--workload", default="al256", choices=["al256", "al4", "alloy"])
+    p.add_argument("--seed", type=int, default=0, help="alloy snapshot seed")
     p.add_argument("--solve", default=None, choices=["mixed", "fp64", "fp32"],
                    help="instead of single evaluations, run whole TN solves (NVTX range 'solve')")
     a = p.parse_args()
@@ -27,13 +31,21 @@ def main():
     from .field import DirectField
     from .grid import DirectGrid
     from .ions import Ions
-    st = systems.config_al256(0) if a.workload == "al256" else systems.config_al4(0)
-    grid = DirectGrid(st.lattice, st.nr, full=False)
-    ions = Ions(st.symbols, positions=st.positions, cell=st.lattice)
-    ps = F.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": F.AnalyticPP(3.0, 1.0)}, PME=True)
-    total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="WT"),
-                              XCFunctional=F.Functional(type="XC", name="LDA"),
-                              HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+    if a.workload == "alloy":
+        from .batch import build_evaluator
+        st = systems.config_alloy(a.seed)
+        total, _ = build_evaluator(st, kedf="WGC")
+        grid = total.PSEUDO.grid
+        econv = 1e-8 * st.nat
+    else:
+        st = systems.config_al256(0) if a.workload == "al256" else systems.config_al4(0)
+        grid = DirectGrid(st.lattice, st.nr, full=False)
+        ions = Ions(st.symbols, positions=st.positions, cell=st.lattice)
+        ps = F.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": F.AnalyticPP(3.0, 1.0)}, PME=True)
+        total = F.TotalFunctional(KineticEnergyFunctional=F.Functional(type="KEDF", name="WT"),
+                                  XCFunctional=F.Functional(type="XC", name="LDA"),
+                                  HARTREE=F.Functional(type="HARTREE"), PSEUDO=ps)
+        econv = 1e-7
     if a.solve:
         from .optimization import Optimization
         rho0 = DirectField(grid)
@@ -41,7 +53,7 @@ def main():
 
         def run():
             o = Optimization(EnergyEvaluator=total, optimization_method="TN",
-                             optimization_options={"econv": 1e-7, "maxfun": 50, "maxiter": 100,
+                             optimization_options={"econv": econv, "maxfun": 50, "maxiter": 100,
                                                    "precision": a.solve})
             o.optimize_rho(guess_rho=rho0)
             return o

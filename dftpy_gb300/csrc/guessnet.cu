@@ -129,7 +129,18 @@ __global__ void __launch_bounds__(kWgThreads) k_conv3d_wgrad(const float* __rest
 }
 
 // pointwise operations
-enum { PW_SILU = 0, PW_SILU_BWD = 1, PW_ADD = 2, PW_POOL2 = 3, PW_POOL2_BWD = 4, PW_UP2 = 5, PW_UP2_BWD = 6 };
+enum { PW_SILU = 0, PW_SILU_BWD = 1, PW_ADD = 2, PW_POOL2 = 3, PW_POOL2_BWD = 4, PW_UP2 = 5, PW_UP2_BWD = 6,
+       PW_UPLIN = 7, PW_UPLIN_BWD = 8 };
+
+// Periodic 2x linear upsampling in cell-centred coordinates (the inverse
+// pairing of the 2x average pool): fine point i of an axis sits at coarse
+// coordinate i/2 - 1/4, so it takes 3/4 of coarse point i/2 and 1/4 of its
+// neighbour on the side of i (i/2 - 1 for even i, i/2 + 1 for odd i),
+// periodically; trilinear = the product over the three axes.
+__device__ __forceinline__ void uplin_axis(int i, int n2, int& j0, int& j1) {
+  j0 = i >> 1;
+  j1 = (i & 1) ? (j0 + 1 == n2 ? 0 : j0 + 1) : (j0 == 0 ? n2 - 1 : j0 - 1);
+}
 
 __global__ void k_pointwise(int op, int64_t n, const float* __restrict__ a, const float* __restrict__ b,
                             float* __restrict__ out, int C, int D, int H, int W) {
@@ -170,6 +181,46 @@ __global__ void k_pointwise(int op, int64_t n, const float* __restrict__ a, cons
         const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)((i / ((int64_t)W * H)) % D);
         const int64_t c = i / ((int64_t)W * H * D);
         out[i] = a[((c * (D / 2) + z / 2) * (H / 2) + y / 2) * (W / 2) + x / 2];
+        break;
+      }
+      case PW_UPLIN: {  // out (C, D, H, W) from a (C, D/2, H/2, W/2), periodic trilinear
+        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)((i / ((int64_t)W * H)) % D);
+        const int64_t c = i / ((int64_t)W * H * D);
+        const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
+        int x0, x1, y0, y1, z0, z1;
+        uplin_axis(x, w2, x0, x1);
+        uplin_axis(y, h2, y0, y1);
+        uplin_axis(z, d2, z0, z1);
+        const float* s = a + c * (int64_t)d2 * h2 * w2;
+        const int zz[2] = {z0, z1}, yy[2] = {y0, y1}, xx[2] = {x0, x1};
+        const float wt[2] = {0.75f, 0.25f};
+        float acc = 0.0f;
+        for (int dz = 0; dz < 2; ++dz)
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx)
+              acc += wt[dz] * wt[dy] * wt[dx] * s[((int64_t)zz[dz] * h2 + yy[dy]) * w2 + xx[dx]];
+        out[i] = acc;
+        break;
+      }
+      case PW_UPLIN_BWD: {  // out (C, D/2, H/2, W/2): the adjoint of PW_UPLIN applied to a (C, D, H, W)
+        const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
+        const int x = (int)(i % w2), y = (int)((i / w2) % h2), z = (int)((i / ((int64_t)w2 * h2)) % d2);
+        const int64_t c = i / ((int64_t)w2 * h2 * d2);
+        const float* s = a + c * (int64_t)D * H * W;
+        // coarse j feeds fine 2j and 2j+1 (3/4), 2j-1 and 2j+2 (1/4), periodically
+        const float wt[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+        float acc = 0.0f;
+        for (int dz = 0; dz < 4; ++dz) {
+          const int fz = (2 * z - 1 + dz + D) % D;
+          for (int dy = 0; dy < 4; ++dy) {
+            const int fy = (2 * y - 1 + dy + H) % H;
+            for (int dx = 0; dx < 4; ++dx) {
+              const int fx = (2 * x - 1 + dx + W) % W;
+              acc += wt[dz] * wt[dy] * wt[dx] * s[((int64_t)fz * H + fy) * W + fx];
+            }
+          }
+        }
+        out[i] = acc;
         break;
       }
       case PW_UP2_BWD: {  // out (C, D/2, H/2, W/2) = sum of the 8 children in a (C, D, H, W)
@@ -293,9 +344,9 @@ int gbofdft_nn_conv3d_wgrad(const float* in, int cin, const float* gout, int cou
 
 int gbofdft_nn_pointwise(int op, const float* a, const float* b, float* out, int C, int D, int H, int W,
                          void* stream) {
-  GB_REQUIRE(a && out && op >= PW_SILU && op <= PW_UP2_BWD, "nn_pointwise: bad arguments");
+  GB_REQUIRE(a && out && op >= PW_SILU && op <= PW_UPLIN_BWD, "nn_pointwise: bad arguments");
   GB_REQUIRE(!(op == PW_SILU_BWD || op == PW_ADD) || b, "nn_pointwise: second operand missing");
-  const bool half_out = op == PW_POOL2 || op == PW_UP2_BWD;
+  const bool half_out = op == PW_POOL2 || op == PW_UP2_BWD || op == PW_UPLIN_BWD;
   GB_REQUIRE(!(op >= PW_POOL2) || (D % 2 == 0 && H % 2 == 0 && W % 2 == 0),
              "nn_pointwise: pooling needs even extents (got %d %d %d)", D, H, W);
   // (D, H, W) are the fine extents for the resampling operations

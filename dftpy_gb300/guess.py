@@ -199,7 +199,7 @@ def _pw(op, a, b, out, C, shape):
     return out
 
 
-SILU, SILU_BWD, ADD, POOL2, POOL2_BWD, UP2, UP2_BWD = range(7)
+SILU, SILU_BWD, ADD, POOL2, POOL2_BWD, UP2, UP2_BWD, UPLIN, UPLIN_BWD = range(9)
 
 
 def silu(z):
@@ -233,6 +233,19 @@ def up2_bwd(g):
                (D, H, W))
 
 
+def uplin(x):
+    """Periodic 2x trilinear upsampling (cell-centred)."""
+    C, D, H, W = x.shape
+    fine = (2 * D, 2 * H, 2 * W)
+    return _pw(UPLIN, x, None, torch.empty((C,) + fine, dtype=x.dtype, device="cuda"), C, fine)
+
+
+def uplin_bwd(g):
+    C, D, H, W = g.shape
+    return _pw(UPLIN_BWD, g, None, torch.empty((C, D // 2, H // 2, W // 2), dtype=g.dtype, device="cuda"), C,
+               (D, H, W))
+
+
 def add(a, b):
     return _pw(ADD, a, b, torch.empty_like(a), a.shape[0], tuple(a.shape[1:]))
 
@@ -242,7 +255,12 @@ class GuessNet:
 
     IN_CHANNELS = 2
 
-    def __init__(self, channels=(16, 32, 48, 64), seed=0):
+    def __init__(self, channels=(16, 32, 48, 64), seed=0, res=1):
+        """res 2: the network runs on the 2x average-pooled features and its
+        output is upsampled back (periodic trilinear) -- 8x less work."""
+        if int(res) not in (1, 2):
+            raise ValueError("res must be 1 or 2")
+        self.res = int(res)
         rng = np.random.default_rng(seed)
         self.channels = tuple(int(c) for c in channels)
         c = self.channels
@@ -271,17 +289,25 @@ class GuessNet:
 
     @property
     def stride(self):
-        return 2 ** (len(self.channels) - 1)
+        return 2 ** (len(self.channels) - 1) * self.res
 
     def forward(self, x, keep=False, tc=True, tc_train=False):
+        """x: (2, D, H, W) FP32 -> (1, D, H, W) (see ``_forward``); with res 2
+        the network sees pool2(x) and its output is upsampled."""
+        shape = tuple(x.shape[1:])
+        if any(s % self.stride for s in shape):
+            raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
+        if self.res == 1:
+            return self._forward(x, keep, tc, tc_train)
+        return uplin(self._forward(pool2(x), keep, tc, tc_train))
+
+    def _forward(self, x, keep=False, tc=True, tc_train=False):
         """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward
         needs; its convolutions run in FP32 on the CUDA cores, or with
         tc_train on the tensor cores where the layer shape has a kernel (BF16
         operands, FP32 pre-activations kept).  Without keep the inner layers
         run on the tensor cores (BF16 activations) when tc is set."""
         shape = tuple(x.shape[1:])
-        if any(s % self.stride for s in shape):
-            raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
         if not keep:
             return self._infer(x, shape, tc)
         # one device flag of timed-out tensor-core waits for the whole
@@ -345,6 +371,8 @@ class GuessNet:
         tape = self._tape
         if tape is None:
             raise RuntimeError("forward(keep=True) must precede backward")
+        if self.res == 2:
+            gout = uplin_bwd(gout.contiguous())
         _, _, h = tape[-1]
         shape = tuple(h.shape[1:])
         err = getattr(self, "_err", None)
@@ -381,7 +409,7 @@ class GuessNet:
             l.adam(lr, self.step_count)
 
     def state(self):
-        return {"channels": np.array(self.channels),
+        return {"channels": np.array(self.channels), "res": np.array(self.res),
                 **{"w%d" % i: l.w.cpu().numpy() for i, l in enumerate(self.layers)},
                 **{"b%d" % i: l.b.cpu().numpy() for i, l in enumerate(self.layers)}}
 
@@ -391,7 +419,7 @@ class GuessNet:
     @classmethod
     def load(cls, path):
         d = np.load(path)
-        net = cls(channels=tuple(int(c) for c in d["channels"]))
+        net = cls(channels=tuple(int(c) for c in d["channels"]), res=int(d["res"]) if "res" in d.files else 1)
         for i, l in enumerate(net.layers):
             l.w.copy_(torch.tensor(d["w%d" % i]))
             l.b.copy_(torch.tensor(d["b%d" % i]))

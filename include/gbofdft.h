@@ -533,7 +533,8 @@ int gbofdft_nn_conv3d(const float* in, int cin, const void* w_bf16, const float*
 int gbofdft_nn_conv3d_wgrad(const float* in, int cin, const float* gout, int cout, int D, int H, int W, float* gw,
                             float* gb, void* stream);
 /* op: 0 SiLU(a), 1 b * SiLU'(a), 2 a + b, 3 2x average pool, 4 its adjoint, 5 2x nearest upsample, 6 its
- * adjoint; (C, D, H, W) are the fine-grid extents for ops 3-6. */
+ * adjoint, 7 2x periodic trilinear upsample (cell-centred: fine point i at coarse i/2 - 1/4), 8 its
+ * adjoint; (C, D, H, W) are the fine-grid extents for ops 3-8. */
 int gbofdft_nn_pointwise(int op, const float* a, const float* b, float* out, int C, int D, int H, int W,
                          void* stream);
 /* loss = sum (pred - target)^2 / sum target^2 (device double), grad = d loss / d pred (may be NULL). */

@@ -68,6 +68,39 @@ def up2_adjoint(g):
     return g.reshape(C, D // 2, 2, H // 2, 2, W // 2, 2).sum(axis=(2, 4, 6))
 
 
+def uplin(x):
+    """Periodic 2x linear upsampling, cell-centred: fine point i of an axis
+    takes 3/4 of coarse point i // 2 and 1/4 of its neighbour on the side
+    of i (the inverse pairing of the average pool)."""
+    out = x
+    for ax in (1, 2, 3):
+        even = 0.75 * out + 0.25 * np.roll(out, 1, axis=ax)     # 2j: j and j - 1
+        odd = 0.75 * out + 0.25 * np.roll(out, -1, axis=ax)     # 2j + 1: j and j + 1
+        shape = list(out.shape)
+        shape[ax] *= 2
+        new = np.empty(shape)
+        sl_e = [slice(None)] * 4
+        sl_o = [slice(None)] * 4
+        sl_e[ax] = slice(0, None, 2)
+        sl_o[ax] = slice(1, None, 2)
+        new[tuple(sl_e)] = even
+        new[tuple(sl_o)] = odd
+        out = new
+    return out
+
+
+def uplin_adjoint(g):
+    out = g
+    for ax in (1, 2, 3):
+        sl_e = [slice(None)] * 4
+        sl_o = [slice(None)] * 4
+        sl_e[ax] = slice(0, None, 2)
+        sl_o[ax] = slice(1, None, 2)
+        e, o = out[tuple(sl_e)], out[tuple(sl_o)]
+        out = 0.75 * (e + o) + 0.25 * (np.roll(e, -1, axis=ax) + np.roll(o, 1, axis=ax))
+    return out
+
+
 def net_forward(x, enc, dec, head):
     """The encoder-decoder of the product (weights as lists of (w, b) pairs
     per level; enc: [(w1, b1, w2, b2)], dec: the same from the deepest

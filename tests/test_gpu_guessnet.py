@@ -130,6 +130,9 @@ def test_pointwise_kernels(gn):
     np.testing.assert_allclose(gn.pool2_bwd(cd, (4, 6, 8)).cpu().numpy(), G.pool2_adjoint(c), rtol=1e-6, atol=1e-7)
     np.testing.assert_allclose(gn.up2(cd).cpu().numpy(), G.up2(c), rtol=0, atol=0)
     np.testing.assert_allclose(gn.up2_bwd(xd).cpu().numpy(), G.up2_adjoint(x), rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(gn.uplin(cd).cpu().numpy(), G.uplin(c.astype(np.float64)), rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(gn.uplin_bwd(xd).cpu().numpy(), G.uplin_adjoint(x.astype(np.float64)), rtol=1e-5,
+                               atol=1e-5)
 
 
 def _oracle_weights(net):
@@ -260,3 +263,38 @@ def test_tensor_core_training_matches_fp32(gn):
     for i, (a, b) in enumerate(zip(gtc, g32)):
         assert float((a - b).norm() / b.norm()) < 5e-2, i
     assert int(net._err_train.item()) == 0
+
+
+def test_half_resolution_network_gradients(gn):
+    """res 2: the network on the pooled features, its output upsampled back;
+    the weight gradients of sum(out * c) equal central differences of the
+    oracle's composition pool2 -> network -> uplin (FP64)."""
+    import torch
+    net = gn.GuessNet(channels=(4, 6), seed=2, res=2)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((2, 8, 8, 12)).astype(np.float32)
+    c = rng.standard_normal((1, 8, 8, 12)).astype(np.float32)
+    out = net.forward(torch.tensor(x, device="cuda"), keep=True).cpu().numpy()
+    enc, dec, head = _oracle_weights(net)
+
+    def full(enc2, dec2, head2):
+        return G.uplin(G.net_forward(G.pool2(x.astype(np.float64)), enc2, dec2, head2))
+    ref = full(enc, dec, head)
+    assert out.shape == (1, 8, 8, 12)
+    assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max()
+    net.backward(torch.tensor(c, device="cuda"))
+    e = 1e-4
+    for lvl, which, idx in [(0, 0, (1, 0, 13)), (1, 2, (3, 5, 0))]:
+        layer = net.enc[lvl][which // 2]
+        g_gpu = float(layer.gw.cpu().numpy()[idx])
+
+        def loss(delta):
+            enc2, dec2, head2 = _oracle_weights(net)
+            t = list(enc2[lvl])
+            w = t[which].copy()
+            w[idx] += delta
+            t[which] = w
+            enc2[lvl] = tuple(t)
+            return float((full(enc2, dec2, head2) * c).sum())
+        fd = (loss(e) - loss(-e)) / (2 * e)
+        assert abs(g_gpu - fd) <= 2e-3 * max(1.0, abs(fd)), (lvl, which, idx, g_gpu, fd)

@@ -34,6 +34,12 @@ def test_resampling_adjoints():
     c = rng.standard_normal((2, 2, 3, 4))
     assert abs(float((G.pool2(x) * c).sum()) - float((x * G.pool2_adjoint(c)).sum())) < 1e-12
     assert abs(float((G.up2(c) * x).sum()) - float((c * G.up2_adjoint(x)).sum())) < 1e-12
+    assert abs(float((G.uplin(c) * x).sum()) - float((c * G.uplin_adjoint(x)).sum())) < 1e-12
+    # linear upsampling keeps constants and linear-in-index ramps (away from the wrap)
+    np.testing.assert_allclose(G.uplin(np.full((1, 2, 3, 4), 1.5)), 1.5)
+    ramp = np.arange(4.0)[None, None, None, :] * np.ones((1, 2, 2, 4))
+    up = G.uplin(ramp)[0, 0, 0]
+    np.testing.assert_allclose(up[1:-1], (np.arange(1, 7) - 0.5) / 2.0)
     z = np.linspace(-4, 4, 101)
     fd = (G.silu(z + 1e-6) - G.silu(z - 1e-6)) / 2e-6
     np.testing.assert_allclose(G.silu_grad(z), fd, rtol=1e-6, atol=1e-9)

@@ -720,11 +720,17 @@ int gb_eval_delta_core(gbofdft_plan* p64, gbofdft_plan* p32, const double* rho, 
 
 int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
   GB_REQUIRE(rho0 > 0.0, "preconditioner: rho0 must be positive (got %g)", rho0);
+  // the optimiser's workspace keeps it between solves of the same grid: the
+  // table depends on the grid and the mean density only (stream order makes
+  // the earlier build complete before any later reader on the plan's stream)
+  if (p->precond_buf == out && p->precond_rho0 == rho0) return 0;
   const int64_t total = p->NG;
   const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
   if (p->prec == GBOFDFT_F64) k_precond<double><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<double*>(out));
   else k_precond<float><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<float*>(out));
   GB_CHECK_LAUNCH();
+  p->precond_buf = out;
+  p->precond_rho0 = rho0;
   return 0;
 }
 

@@ -213,7 +213,7 @@ struct CtRowsInv {
 
 // irfftn line build (all fields) + inverse FFT; result line (f * RP + pair)
 // holds row 2 pair in .x and row 2 pair + 1 in .y.
-template <typename T, int N, bool PM = false>
+template <typename T, int N, bool PM = false, int NFMAX = GB_MAX_FIELDS>
 __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t base, cpx<T>* tw, cpx<T>* A,
                                                      cpx<T>* B) {
   constexpr int RP = RowsCfg<T>::RP, TPL = Tpl<N>::value, NP = Pad<T, N>::NP, NH = N / 2 + 1;
@@ -221,7 +221,7 @@ __device__ __forceinline__ cpx<T>* ct_rows_inv_lines(const CtRowsInv& a, int64_t
   const int nl = a.nf * RP;
   const cpx<T>* src0 = reinterpret_cast<const cpx<T>*>(a.in);
 #pragma unroll
-  for (int f = 0; f < GB_MAX_FIELDS; ++f) {
+  for (int f = 0; f < NFMAX; ++f) {
     if (f >= a.nf) break;
     const cpx<T>* src = src0 + f * a.fstride;
     for (int idx = tid; idx < RP * NH; idx += blockDim.x) {
@@ -264,6 +264,61 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>()) k_ct_rows_inv_store(
     if (row >= a.nrows) continue;
     const cpx<T> z = res[sw<T, NP>(f * RP + (rr >> 1), j)];
     out[f * a.ostride + row * N + j] = ((rr & 1) ? z.y : z.x) * s;
+  }
+}
+
+// WGC nonlocal potential from its six real-space fields (X0..X2 from rho^b,
+// Y0..Y2 from rho^a): the inverse row pass of the combined spectra with the
+// potential added to pot in the same kernel (FP32, potential only), instead
+// of storing the six fields and reading them back.
+struct CtRowsInvWgc {
+  CtRowsInv r;          // spectra (plane-major), nf = 6 (3 when a == b), twiddles
+  const float* rho;
+  float rho0, inv0, ea, eb;
+  int two;
+  float* pot;
+};
+
+template <int N>
+__global__ void __launch_bounds__(Tpl<N>::value * RowsCfg<float>::RP * 6) k_ct_rows_inv_wgc(CtRowsInvWgc a) {
+  constexpr int RP = RowsCfg<float>::RP, NP = Pad<float, N>::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nl = a.r.nf * RP;
+  cpx<float>* tw = reinterpret_cast<cpx<float>*>(smem_raw);
+  cpx<float>* A = tw + N;
+  cpx<float>* B = A + nl * NP;
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * 2 * RP;
+  const cpx<float>* twg = reinterpret_cast<const cpx<float>*>(a.r.tw);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
+  cpx<float>* res = ct_rows_inv_lines<float, N, true, 6>(a.r, base, tw, A, B);
+  const int gy = a.two ? 3 : 0;
+  for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
+    const int rr = idx / N, j = idx % N;
+    const int64_t row = base + rr;
+    if (row >= a.r.nrows) continue;
+    const int64_t g = row * N + j;
+    const int pr = rr >> 1;
+    auto fld = [&](int f) {
+      const cpx<float> z = res[sw<float, NP>(f * RP + pr, j)];
+      return (rr & 1) ? z.y : z.x;
+    };
+    const float X0 = fld(0), X1 = fld(1), X2 = fld(2);
+    const float Y0 = fld(gy), Y1 = fld(gy + 1), Y2 = fld(gy + 2);
+    const float r = __ldg(a.rho + g);
+    const float rc = r > (float)kZero ? r : (float)kZero;
+    const float u = (rc - a.rho0) * a.inv0;
+    const float Aa = powf(rc, a.ea);
+    const float sx = X0 + u * X1 + u * u * X2;
+    float v;
+    if (a.two) {
+      const float Bb = powf(rc, a.eb);
+      v = a.ea * Aa / rc * sx + Aa * a.inv0 * (X1 + 2.0f * u * X2) + a.eb * Bb / rc * (Y0 + u * Y1 + u * u * Y2) +
+          Bb * a.inv0 * (Y1 + 2.0f * u * Y2);
+    } else {
+      v = 2.0f * (a.ea * Aa / rc * sx + Aa * a.inv0 * (X1 + 2.0f * u * X2));
+    }
+    a.pot[g] += v;
   }
 }
 
@@ -661,6 +716,29 @@ int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int
   return rc;
 }
 
+inline int ct_rows_inv_wgc(gbofdft_plan* p, const void* spec, int64_t fstride, int two, const float* rho, double rho0,
+                           double ea, double eb, float* pot, cudaStream_t st) {
+  int rc = 1;
+  ct_dispatch(p->n[2], [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    constexpr int RP = RowsCfg<float>::RP, NP = Pad<float, N>::NP;
+    CtRowsInvWgc a;
+    memset(&a, 0, sizeof(a));
+    a.r.in = spec; a.r.fstride = fstride; a.r.nrows = p->n[0] * p->n[1]; a.r.ld2 = 0; a.r.nf = two ? 6 : 3;
+    a.r.tw = p->tw[2];
+    a.rho = rho; a.rho0 = (float)rho0; a.inv0 = (float)(1.0 / rho0); a.ea = (float)ea; a.eb = (float)eb;
+    a.two = two; a.pot = pot;
+    const int nblk = (a.r.nrows + 2 * RP - 1) / (2 * RP);
+    const size_t sm = sizeof(cpx<float>) * (N + 2 * (size_t)a.r.nf * RP * NP);
+    if ((rc = ct_smem(k_ct_rows_inv_wgc<N>, sm))) return;
+    k_ct_rows_inv_wgc<N><<<nblk, Tpl<N>::value * RP * a.r.nf, sm, st>>>(a);
+    gb_count_launch();
+    cudaError_t e = cudaGetLastError();
+    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "ct_rows_inv_wgc: %s", cudaGetErrorString(e));
+  });
+  return rc;
+}
+
 template <typename T, int DIR, bool CONV>
 int ct_cols_t(gbofdft_plan* p, void* spec, int64_t fstride, int ld2, int nf, int axis, double scale,
               const KerDesc* kd, cudaStream_t st) {
@@ -835,6 +913,10 @@ inline int plane_wgc_inv_f32(gbofdft_plan* p, const void* spec, int64_t fstride,
                                   int64_t ostride, cudaStream_t st) {                                          \
     return gbct::ct_rows_inv<float, true>(p, spec, fstride, 0, nf, out, ostride, 1.0, nullptr, nullptr,        \
                                           nullptr, nullptr, 0, nullptr, nullptr, st);                          \
+  }                                                                                                            \
+  int gb_ct_rows_inv_wgc_pm_f32(gbofdft_plan* p, const void* spec, int64_t fstride, int two, const float* rho,   \
+                                double rho0, double ea, double eb, float* pot, cudaStream_t st) {             \
+    return gbct::ct_rows_inv_wgc(p, spec, fstride, two, rho, rho0, ea, eb, pot, st);                          \
   }                                                                                                            \
   int gb_plane_fwd_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, cudaStream_t st) {                \
     return gbct::plane_fwd_f32(p, spec, fstride, nf, st);                                                      \

@@ -38,6 +38,8 @@ struct gbofdft_plan {
   const void* wt_pm_src; // the table that copy belongs to
   float* wgc_pm;         // plane-major copy of the last WGC kernels (4 x NG) built on this plan
   const void* wgc_pm_src; // the kernels that copy belongs to
+  const void* precond_buf;  // the buffer the last TN preconditioner was built into ...
+  double precond_rho0;      // ... and its mean density (a rebuild is skipped when both match)
 };
 
 size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar
@@ -106,6 +108,10 @@ int gb_plane_wgc_inv_f32(gbofdft_plan*, const void* spec, int64_t fstride, void*
                          const float* K, double scale, cudaStream_t);
 int gb_ct_rows_inv_store_pm_f32(gbofdft_plan*, const void* spec, int64_t fstride, int nf, void* out, int64_t ostride,
                                 cudaStream_t);
+// the inverse rows of the six (three when a == b) combined WGC spectra with
+// the NL potential added to pot (potential-only FP32 evaluations)
+int gb_ct_rows_inv_wgc_pm_f32(gbofdft_plan*, const void* spec, int64_t fstride, int two, const float* rho, double rho0,
+                              double ea, double eb, float* pot, cudaStream_t);
 int gb_plane_variants_f32(int n0, int n1);
 // the plane-major evaluation (returns 1 when the plan has no plane pipeline
 // or a kernel table has no plane-major copy)

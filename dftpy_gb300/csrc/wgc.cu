@@ -220,6 +220,50 @@ __global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __re
   }
 }
 
+// The FP32 potential-only final pass, four points per thread with 16-byte
+// loads and stores (n % 4 == 0; the fields are 16-byte aligned): the
+// per-point pass is latency-bound on its seven input streams otherwise.
+__global__ void __launch_bounds__(kThreads) k_wgc_final_v4(int64_t n4, const float4* __restrict__ rho, float rho0,
+                                                            float a, float b, int two, const float4* __restrict__ x0,
+                                                            const float4* __restrict__ x1,
+                                                            const float4* __restrict__ x2,
+                                                            const float4* __restrict__ y0,
+                                                            const float4* __restrict__ y1,
+                                                            const float4* __restrict__ y2,
+                                                            float4* __restrict__ pot) {
+  const float inv0 = 1.0f / rho0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 r4 = rho[i], X04 = x0[i], X14 = x1[i], X24 = x2[i];
+    float4 Y04 = X04, Y14 = X14, Y24 = X24;
+    if (two) {
+      Y04 = y0[i];
+      Y14 = y1[i];
+      Y24 = y2[i];
+    }
+    float4 p4 = pot[i];
+    const float* rr = &r4.x;
+    const float *X0 = &X04.x, *X1 = &X14.x, *X2 = &X24.x, *Y0 = &Y04.x, *Y1 = &Y14.x, *Y2 = &Y24.x;
+    float* pp = &p4.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float rc = rr[k] > (float)kZeroRho ? rr[k] : (float)kZeroRho;
+      const float u = (rc - rho0) * inv0;
+      const float A = powf(rc, a);
+      const float sx = X0[k] + u * X1[k] + u * u * X2[k];
+      float v;
+      if (two) {
+        const float B = powf(rc, b);
+        v = a * A / rc * sx + A * inv0 * (X1[k] + 2.0f * u * X2[k]) +
+            b * B / rc * (Y0[k] + u * Y1[k] + u * u * Y2[k]) + B * inv0 * (Y1[k] + 2.0f * u * Y2[k]);
+      } else {
+        v = 2.0f * (a * A / rc * sx + A * inv0 * (X1[k] + 2.0f * u * X2[k]));
+      }
+      pp[k] += v;
+    }
+    pot[i] = p4;
+  }
+}
+
 // energies[NL] and energies[TOTAL] += base + dV * sum(partials) (e may be
 // null); eref (may be null) = dV * sum(partials)
 __global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV, double* __restrict__ e,
@@ -246,9 +290,11 @@ __global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV,
 
 // X0..X2 (and Y0..Y2) into W.f[0..5] on the plane pipeline (FP32): the
 // transform inputs are made from rho in the forward row pass (rho given) or
-// read from W.f[0..5] (rho null); K: the plane-major kernels
+// read from W.f[0..5] (rho null); K: the plane-major kernels.  pot given
+// (potential-only evaluations): the inverse row pass adds the NL potential
+// to pot directly instead of storing the fields.
 int wgc_xfields_plane(gbofdft_plan* p, const WgcBufs& W, int two, const float* K, const float* rho,
-                      const gbofdft_wgc* d, cudaStream_t st) {
+                      const gbofdft_wgc* d, cudaStream_t st, float* pot = nullptr) {
   const int nfield = two ? 6 : 3;
   const int64_t fs = (int64_t)((char*)W.s[1] - (char*)W.s[0]) / (int64_t)sizeof(float2);
   const int64_t os = (int64_t)((char*)W.o[1] - (char*)W.o[0]) / (int64_t)sizeof(float2);
@@ -263,6 +309,11 @@ int wgc_xfields_plane(gbofdft_plan* p, const WgcBufs& W, int two, const float* K
   }
   if (!rc) rc = gb_plane_fwd_f32(p, W.s[0], fs, nfield, st);
   if (!rc) rc = gb_plane_wgc_inv_f32(p, W.s[0], fs, W.o[0], os, two ? 2 : 1, K, 1.0 / (double)p->N, st);
+  if (!rc && pot && rho) {
+    rc = gb_ct_rows_inv_wgc_pm_f32(p, W.o[0], os, two, rho, d->rho0, d->alpha, d->beta, pot, st);
+    if (rc == 1) return gb_set_error(GBOFDFT_ERR_STATE, "wgc: plane size without specialisation");
+    return rc;
+  }
   for (int h = 0; h < (two ? 2 : 1) && !rc; ++h) rc = gb_ct_rows_inv_store_pm_f32(p, W.o[3 * h], os, 3, W.f[3 * h], rs, st);
   if (rc == 1) return gb_set_error(GBOFDFT_ERR_STATE, "wgc: plane size without specialisation");
   return rc;
@@ -308,6 +359,10 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
   const T* r = reinterpret_cast<const T*>(rho);
   int rc;
   if (wgc_plane(p) && p->wgc_pm && p->wgc_pm_src == d->kernels) {
+    if (!calc_e && calc_v && !store_ref)
+      // potential only: the inverse rows add the potential themselves
+      return wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st,
+                               reinterpret_cast<float*>(pot));
     rc = wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st);
   } else {
     k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],
@@ -324,6 +379,23 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
   }
   const int want_e = calc_e || store_ref;
   const T* y = reinterpret_cast<const T*>(two ? W.f[3] : W.f[0]);
+  auto a16 = [](const void* q) { return ((uintptr_t)q & 15) == 0; };
+  if constexpr (sizeof(T) == 4) {
+    if (!want_e && calc_v && p->N % 4 == 0 && a16(rho) && a16(pot) && a16(W.f[0]) && a16(W.f[1]) && a16(W.f[2]) &&
+        a16(y) && (!two || (a16(W.f[4]) && a16(W.f[5])))) {
+      const int64_t n4 = p->N / 4;
+      const int nb = (int)((n4 + kThreads - 1) / kThreads < 4 * kBlocks ? (n4 + kThreads - 1) / kThreads : 4 * kBlocks);
+      k_wgc_final_v4<<<nb, kThreads, 0, st>>>(
+          n4, reinterpret_cast<const float4*>(rho), (float)d->rho0, (float)d->alpha, (float)d->beta, two,
+          reinterpret_cast<const float4*>(W.f[0]), reinterpret_cast<const float4*>(W.f[1]),
+          reinterpret_cast<const float4*>(W.f[2]), reinterpret_cast<const float4*>(y),
+          two ? reinterpret_cast<const float4*>(W.f[4]) : nullptr,
+          two ? reinterpret_cast<const float4*>(W.f[5]) : nullptr, reinterpret_cast<float4*>(pot));
+      GB_CHECK_LAUNCH();
+      gb_count_launch();
+      return 0;
+    }
+  }
   if (want_e)
     k_wgc_final<T, true><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
                                                        (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,

@@ -336,6 +336,13 @@ def test_wgc_eval_matches_oracle(lib, prec, ab, nr, full, skew):
         assert abs(float(en[lib.E_TOTAL]) - e) <= 1e-12 * max(1.0, abs(e))
         p = pot.cpu().numpy()
         assert np.abs(p - v_ref).max() <= tol * 5 * np.abs(v_ref).max(), order
+        # potential only: on plane-pipeline grids (FP32) the inverse row pass
+        # adds the potential itself; the same potential to FP32 rounding
+        pv = torch.empty_like(rd)
+        lib.check(lib.load().gbofdft_eval(plan.handle, lib.ptr(rd), f, lib.ptr(pv), None, lib.CALC_V,
+                                          lib.stream_ptr()))
+        torch.cuda.synchronize()
+        assert np.abs(pv.cpu().numpy() - p).max() <= (1e-12 if prec == 1 else 2e-6) * np.abs(p).max(), order
         if order == 0 and ab == "equal":
             e_wt, v_wt = O.WTNL()(rho, g)
             assert abs(e - e_wt) <= tol * abs(e_wt)

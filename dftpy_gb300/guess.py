@@ -261,6 +261,7 @@ class GuessNet:
         if int(res) not in (1, 2):
             raise ValueError("res must be 1 or 2")
         self.res = int(res)
+        self.mix = 1.0          # the LearnedGuess mixing factor this network was evaluated with
         rng = np.random.default_rng(seed)
         self.channels = tuple(int(c) for c in channels)
         c = self.channels
@@ -409,7 +410,7 @@ class GuessNet:
             l.adam(lr, self.step_count)
 
     def state(self):
-        return {"channels": np.array(self.channels), "res": np.array(self.res),
+        return {"channels": np.array(self.channels), "res": np.array(self.res), "mix": np.array(self.mix),
                 **{"w%d" % i: l.w.cpu().numpy() for i, l in enumerate(self.layers)},
                 **{"b%d" % i: l.b.cpu().numpy() for i, l in enumerate(self.layers)}}
 
@@ -420,6 +421,7 @@ class GuessNet:
     def load(cls, path):
         d = np.load(path)
         net = cls(channels=tuple(int(c) for c in d["channels"]), res=int(d["res"]) if "res" in d.files else 1)
+        net.mix = float(d["mix"]) if "mix" in d.files else 1.0
         for i, l in enumerate(net.layers):
             l.w.copy_(torch.tensor(d["w%d" % i]))
             l.b.copy_(torch.tensor(d["b%d" % i]))
@@ -453,10 +455,13 @@ def features(total, grid):
 
 
 class LearnedGuess:
-    """Starting density from a trained ``GuessNet``."""
+    """Starting density from a trained ``GuessNet``: the network's density,
+    mixed with the uniform density when ``mix`` < 1 (rho0 + mix (rho_net -
+    rho0); None: the value saved with the network, else 1)."""
 
-    def __init__(self, net):
+    def __init__(self, net, mix=None):
         self.net = net
+        self.mix = float(mix) if mix is not None else float(getattr(net, "mix", 1.0))
 
     def prepare(self, total, grid=None):
         """Make the network's packed tensor-core weights (every layer whose
@@ -479,6 +484,9 @@ class LearnedGuess:
         rho = (phi * phi).to(torch.float64)
         nel = float(total.PSEUDO.ions.get_ncharges())
         rho = rho * (nel / (float(rho.sum()) * grid.dV))
+        if self.mix != 1.0:
+            rho0_u = nel / grid.volume
+            rho = rho0_u + self.mix * (rho - rho0_u)
         return DirectField(grid, data=rho.to(dtype))
 
 
@@ -502,16 +510,22 @@ def training_cell(seed, reps=(2, 2, 2), nr=(64, 64, 64), mg_max=0.3, sigmas=(0.1
 
 
 def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 64, 64), workers=16, chunk=64,
-                 mg_max=0.3, sigmas=(0.15,)):
+                 mg_max=0.3, sigmas=(0.15,), cells="small"):
     """(x, sqrt(rho_atom), sqrt(rho converged), rho0) per seed from the
-    solver's own converged densities (solved as batches)."""
+    solver's own converged densities (solved as batches).  cells "small":
+    ``training_cell`` (2x2x2 cells at 64^3); "alloy": the batched workload's
+    own generator (``systems.config_alloy``, 108-500 atoms, 96^3-160^3)."""
     from .batch import build_evaluator, optimize_batch
     data = []
     seeds = list(seeds)
     for c0 in range(0, len(seeds), chunk):
-        jobs = [build_evaluator(training_cell(s, reps, nr, mg_max, sigmas), kedf=kedf) for s in seeds[c0:c0 + chunk]]
+        make = (lambda s: systems.config_alloy(s)) if cells == "alloy" else \
+            (lambda s: training_cell(s, reps, nr, mg_max, sigmas))
+        jobs = [build_evaluator(make(s), kedf=kedf) for s in seeds[c0:c0 + chunk]]
         res = optimize_batch(jobs, workers=workers, options={"precision": precision})
         for (total, rho_u), r in zip(jobs, res):
+            if r.converged != 0:
+                continue
             x, phib, rho0 = features(total, rho_u.grid)
             phit = torch.sqrt(torch.clamp(r.rho.as_subclass(torch.Tensor).to(torch.float32), min=SQRT_CLAMP))
             data.append((x, phib, phit, rho0))
@@ -595,6 +609,37 @@ def evaluate_guesses(net, structures, kedf="WGC", precision="mixed"):
     return rows
 
 
+def evaluate_batched(net, structures, kedf="WGC", chunk=64, workers=16, mix=None):
+    """Mixed-precision batches of ``structures`` from the uniform density and
+    from the learned guess: per start the wall time, TN iterations and
+    evaluations, converged count and the largest energy difference to the
+    uniform start (eV/atom)."""
+    from .batch import build_evaluator, optimize_batch
+    lg = LearnedGuess(net, mix=mix)
+    out = {}
+    energies = {}
+    for mode, guess in (("uniform", None), ("learned", lg)):
+        wall, iters, evals, conv, es = 0.0, 0, 0, 0, []
+        for c0 in range(0, len(structures), chunk):
+            jobs = [build_evaluator(st, kedf=kedf) for st in structures[c0:c0 + chunk]]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = optimize_batch(jobs, workers=workers, options={"precision": "mixed"}, guess=guess)
+            torch.cuda.synchronize()
+            wall += time.perf_counter() - t0
+            for r in res:
+                iters += sum(st_["n_iter"] for st_ in r.stats["stages"])
+                evals += sum(st_["n_eval_ev"] + st_["n_eval_v"] + st_.get("n_eval_hess", 0) for st_ in r.stats["stages"])
+                conv += int(r.converged == 0)
+                es.append(float(r.energy))
+        energies[mode] = np.array(es)
+        out[mode] = {"wall_s": wall, "iters": iters, "evals": evals, "converged": conv}
+    nat = np.array([st.nat for st in structures])
+    out["learned"]["max_dE_eV_per_atom_vs_uniform"] = float(
+        np.max(np.abs(energies["learned"] - energies["uniform"]) / nat * 27.211386024367243))
+    return out
+
+
 def main():
     import argparse
     import json
@@ -603,8 +648,12 @@ def main():
     p.add_argument("--epochs", type=int, default=8)
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--channels", default="16,32,48,64")
+    p.add_argument("--res", type=int, default=1, help="2: the network runs on 2x pooled features")
+    p.add_argument("--mix", type=float, default=1.0, help="mixing factor with the uniform density saved with the "
+                                                           "network")
+    p.add_argument("--cells", default="small", choices=["small", "alloy"],
+                   help="training cells: small 2x2x2 cells at 64^3, or the batched workload's snapshots")
     p.add_argument("--eval", type=int, default=8, help="held-out cells (seeds 5000 ...)")
-    p.add_argument("--eval-large", type=int, default=4, help="held-out batched-workload snapshots")
     p.add_argument("--out", default=None)
     p.add_argument("--kedf", default="WGC", help="KEDF of the training solves (WGC: the batched workload's; "
                                                   "WT: the 256-atom benchmark's)")
@@ -613,42 +662,28 @@ def main():
     a = p.parse_args()
     sigmas = tuple(float(v) for v in a.sigma.split(","))
     t0 = time.perf_counter()
-    data = make_dataset(range(1000, 1000 + a.train), kedf=a.kedf, mg_max=a.mg_max, sigmas=sigmas)
+    data = make_dataset(range(1000, 1000 + a.train), kedf=a.kedf, mg_max=a.mg_max, sigmas=sigmas, cells=a.cells)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
-    net = GuessNet(channels=tuple(int(c) for c in a.channels.split(",")), seed=0)
+    net = GuessNet(channels=tuple(int(c) for c in a.channels.split(",")), seed=0, res=a.res)
+    net.mix = float(a.mix)
     t1 = time.perf_counter()
     hist = train(net, data, epochs=a.epochs, lr=a.lr, log=lambda s: print(s, flush=True))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
     if a.out:
         net.save(a.out)
-    held = [training_cell(s, mg_max=a.mg_max, sigmas=sigmas) for s in range(5000, 5000 + a.eval)]
-    rows = evaluate_guesses(net, held, kedf=a.kedf)
-    large = [systems.config_alloy(5000 + s) for s in range(a.eval_large)] if a.kedf == "WGC" else \
-        [systems.config_al256(s) for s in range(a.eval_large)]
-    rows_l = evaluate_guesses(net, large, kedf=a.kedf)
-
-    def summary(rs):
-        out = {}
-        for m in ("uniform", "atomic", "learned"):
-            out[m] = {"evals": sum(r[m]["evals"] for r in rs), "iters": sum(r[m]["iters"] for r in rs),
-                      "wall_s": sum(r[m]["wall_s"] for r in rs),
-                      "converged": sum(r[m]["converged"] == 0 for r in rs),
-                      "max_dE_eV_per_atom_vs_uniform": max(abs(r[m]["energy"] - r["uniform"]["energy"]) / r["nat"]
-                                                           * 27.211386024367243 for r in rs)}
-        return out
-    x, phib, phit, rho0 = data[0]
-    t2 = time.perf_counter()
-    for _ in range(10):
-        net.forward(x)
-    torch.cuda.synchronize()
-    t_inf = (time.perf_counter() - t2) / 10
-    print(json.dumps({"params": net.nparams, "channels": list(net.channels), "train_cells": a.train,
-                      "epochs": a.epochs, "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
-                      "data_s": t_data, "train_s": t_train, "inference_64cubed_s": t_inf,
-                      "heldout_64": summary(rows), "heldout_batched": summary(rows_l),
-                      "rows": rows + rows_l}))
+    report = {"params": net.nparams, "channels": list(net.channels), "res": net.res, "mix": net.mix,
+              "cells": a.cells, "train_cells": len(data), "epochs": a.epochs, "loss": hist,
+              "data_s": t_data, "train_s": t_train}
+    del data
+    if a.cells == "alloy":
+        held = [systems.config_alloy(s) for s in range(5000, 5000 + a.eval)]
+        report["heldout"] = evaluate_batched(net, held, kedf=a.kedf)
+    else:
+        held = [training_cell(s, mg_max=a.mg_max, sigmas=sigmas) for s in range(5000, 5000 + a.eval)]
+        report["rows"] = evaluate_guesses(net, held, kedf=a.kedf)
+    print(json.dumps(report))
 
 
 if __name__ == "__main__":

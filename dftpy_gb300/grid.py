@@ -10,6 +10,7 @@ precision (FFT schedule, twiddle tables, workspaces).
 import math
 
 import os
+import weakref
 
 import numpy as np
 
@@ -191,9 +192,14 @@ class DirectGrid(BaseGrid):
         return self._plans["delta"]
 
     def get_reciprocal(self):
-        if self._reciprocal is None:
-            self._reciprocal = ReciprocalGrid(self)
-        return self._reciprocal
+        """The reciprocal grid (cached weakly: it refers to this grid, and a
+        strong reference both ways would keep the pair -- with its plans and
+        device workspaces -- alive until Python's cycle collector runs)."""
+        r = self._reciprocal() if self._reciprocal is not None else None
+        if r is None:
+            r = ReciprocalGrid(self)
+            self._reciprocal = weakref.ref(r)
+        return r
 
     def guess_ecut(self):
         """``DirectGrid.guess_ecut`` (``grid.py:477-480``)."""

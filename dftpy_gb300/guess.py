@@ -20,6 +20,7 @@ Weights are BF16 for the arithmetic with FP32 master copies; every kernel
 the project's own (``gbofdft_nn_*``).
 """
 import ctypes
+import gc
 import math
 import threading
 import time
@@ -529,6 +530,9 @@ def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 6
             x, phib, rho0 = features(total, rho_u.grid)
             phit = torch.sqrt(torch.clamp(r.rho.as_subclass(torch.Tensor).to(torch.float32), min=SQRT_CLAMP))
             data.append((x, phib, phit, rho0))
+        # the chunk's evaluators (plans, workspaces) go before the next chunk's
+        del jobs, res
+        gc.collect()
     return data
 
 

@@ -194,11 +194,12 @@ def alloy_jobs(seeds):
     return jobs
 
 
-def batch_step(jobs, precision, guess, workers):
+def batch_step(jobs, precision, guess, workers, extra=None):
     """One step: optimise every job; returns (wall s, results)."""
     import torch
     from dftpy_gb300 import batch
     opts = {"precision": precision, "econv_per_atom": ECONV_PER_ATOM}
+    opts.update(extra or {})
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -211,10 +212,10 @@ def batch_step(jobs, precision, guess, workers):
     return max(wall, e0.elapsed_time(e1) / 1000.0), res
 
 
-def timed_batches(jobs, precision, guess, steps, warmup, flush, world, workers):
+def timed_batches(jobs, precision, guess, steps, warmup, flush, world, workers, extra=None):
     from dftpy_gb300 import _lib
     for _ in range(warmup):
-        batch_step(jobs, precision, guess, workers)
+        batch_step(jobs, precision, guess, workers, extra)
     times, last = [], None
     l0 = _lib.launch_count()
     for _ in range(steps):
@@ -222,7 +223,7 @@ def timed_batches(jobs, precision, guess, steps, warmup, flush, world, workers):
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
-        t, last = batch_step(jobs, precision, guess, workers)
+        t, last = batch_step(jobs, precision, guess, workers, extra)
         times.append(t)
     return times, last, _lib.launch_count() - l0
 
@@ -647,6 +648,12 @@ def main():
         plain = {"value": max_over_ranks(pt[0], world), "evaluations": sum(n_evals(r) for r in pres),
                  "converged": sum(r.converged == 0 for r in pres), "guess": "uniform",
                  "method": "FP64 TN, unpreconditioned inner CG, the reference's line search (its method)"}
+        # the same FP64 solves with the mixed path's preconditioner: how much of
+        # the speed-up is the preconditioner and how much the precision split
+        qt, qres, _ = timed_batches(jobs, "fp64", None, 1, 0, flush, world, args.workers, {"precond": True})
+        plain["fp64_preconditioned"] = {"value": max_over_ranks(qt[0], world),
+                                        "evaluations": sum(n_evals(r) for r in qres),
+                                        "converged": sum(r.converged == 0 for r in qres)}
     acc = {"tolerance_ev_per_atom": TOL_EV_PER_ATOM}
     if e_plain is not None:
         err = [abs(a - b) * HA_EV / n for a, b, n in zip(energies, e_plain, nat)]
@@ -663,8 +670,13 @@ def main():
     j128 = [j for j in jobs if tuple(int(x) for x in j[1].grid.nrR) == (128, 128, 128)]
     if j128:
         t_w = eval_roofline_wgc(*j128[0])
-        roof_wgc = {"t_eval_us": t_w * 1e6, "grid": [128, 128, 128],
-                    "functional": "TF+vW+WGC+LDA+Hartree+PP, FP32 potential only, isolated loop"}
+        # s N (R + W + 2 F): R = 2 (rho, v_loc), W = 1, F = 16 transforms (vW 2, Hartree 2, WGC 6 + 6: the
+        # WGC term has no reference, so this is this implementation's own count)
+        b_w = 4 * 128 ** 3 * (2 + 1 + 2 * 16)
+        peak_w, _ = measured_peaks()
+        roof_wgc = {"t_eval_us": t_w * 1e6, "grid": [128, 128, 128], "algorithmic_bytes": b_w,
+                    "achieved_gbs": b_w / t_w / 1e9, "frac": b_w / t_w / 1e9 / peak_w,
+                    "functional": "TF+vW+WGC+LDA+Hartree+PP, FP32 potential only, isolated loop (one stream)"}
     e2e_v, h2d, d2h, _ = e2e_batch(seeds, jobs, args.precision, guess, args.workers, 1 if args.steps < 2 else 2, 1)
     al = None
     live, t_iso, b_eval = (0.0, 0), None, None

@@ -68,6 +68,9 @@ DEFAULTS = {
     "refine_cg_rtol": 0.01,
     # preconditioned inner CG in the stages of "mixed" (uniform-gas Hessian)
     "mixed_precond": True,
+    # preconditioned inner CG for precision "fp64" / "fp32" too (off: the
+    # reference's plain CG); for attributing the mixed path's speed-up
+    "precond": False,
     # CUDA-event timing of the FP32 potential-only evaluations (stats
     # t_eval_timed / n_eval_timed per stage)
     "time_evals": False,
@@ -197,7 +200,8 @@ class Optimization:
         if prec in ("fp64", "fp32"):
             dt = torch.float64 if prec == "fp64" else torch.float32
             eps = o["eps"] if o["eps"] is not None else (1e-9 if dt == torch.float64 else o["fp32_eps"])
-            r, out = self._run(rho.to(dt) if rho.dtype != dt else rho, o["econv"], eps, o["maxiter"])
+            r, out = self._run(rho.to(dt) if rho.dtype != dt else rho, o["econv"], eps, o["maxiter"],
+                               precond=bool(o["precond"]))
             self.stats["stages"].append(dict(precision=prec, **out))
         elif prec == "mixed":
             # FP32 until its energy changes by less than fp32_econv (default:

@@ -200,6 +200,25 @@ def check(rc, what=""):
         raise exc("gbofdft%s: %s (status %d)" % ((" " + what) if what else "", msg, rc))
 
 
+def check_alloc(call, what=""):
+    """``check(call())`` for calls whose only side effect before a failed
+    allocation can be repeated (creating a plan or delta state, building a
+    kernel table).  The library allocates with ``cudaMalloc`` beside
+    PyTorch's caching allocator, which keeps freed blocks reserved: on
+    ``GBOFDFT_ERR_ALLOC`` the cache (and unreachable Python objects holding
+    device memory) is released and the call made once more."""
+    rc = call()
+    if rc == 4:
+        import gc
+        import torch
+        gc.collect()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+        rc = call()
+    check(rc, what)
+
+
 def require_cuda():
     import torch
     if not torch.cuda.is_available():
@@ -262,8 +281,8 @@ class Plan:
         nr = [int(x) for x in nr]
         lat = [float(x) for x in list(_flat(lattice))]
         h = ctypes.c_void_p()
-        check(L.gbofdft_plan_create((ctypes.c_int * 3)(*nr), (ctypes.c_double * 9)(*lat), int(precision),
-                                    1 if full else 0, ctypes.byref(h)), "plan_create")
+        check_alloc(lambda: L.gbofdft_plan_create((ctypes.c_int * 3)(*nr), (ctypes.c_double * 9)(*lat),
+                                                  int(precision), 1 if full else 0, ctypes.byref(h)), "plan_create")
         self.handle = h
         self.nr = tuple(nr)
         self.precision = precision
@@ -290,7 +309,7 @@ class Delta:
     def __init__(self, plan64, plan32):
         L = load()
         h = ctypes.c_void_p()
-        check(L.gbofdft_delta_create(plan64.handle, plan32.handle, ctypes.byref(h)), "delta_create")
+        check_alloc(lambda: L.gbofdft_delta_create(plan64.handle, plan32.handle, ctypes.byref(h)), "delta_create")
         self.handle = h
         self._plans = (plan64, plan32)   # the state refers to both plans
 

@@ -69,7 +69,7 @@ class KEDF(AbstractFunctional):
             g = rho.grid
             plan = g.plan(rho.dtype)
             k = torch.empty((int(g.nrR[0]), int(g.nrR[1]), int(g.nrR[2]) // 2 + 1), dtype=rho.dtype, device="cuda")
-            _lib.check(_lib.load().gbofdft_wt_kernel(
+            _lib.check_alloc(lambda: _lib.load().gbofdft_wt_kernel(
                 plan.handle, float(rho0), float(self.options.get("x", 1.0)), float(self.alpha),
                 float(self.beta), _lib.ptr(k), _lib.stream_ptr()), "wt_kernel")
             s.update(Kernel=k, rho0=rho0, shape=shape)

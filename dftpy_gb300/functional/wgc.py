@@ -175,8 +175,8 @@ class WGCTerm:
         d = st["d"]
         if abs(d.rho0 - rho0) > 1e-6:
             t0, h, m, tab = self.table()
-            _lib.check(_lib.load().gbofdft_wgc_kernels(plan.handle, rho0, self.alpha, self.beta, _lib.ptr(tab),
-                                                       int(m), t0, h, _lib.ptr(st["K"]), _lib.stream_ptr()),
-                       "wgc_kernels")
+            _lib.check_alloc(lambda: _lib.load().gbofdft_wgc_kernels(
+                plan.handle, rho0, self.alpha, self.beta, _lib.ptr(tab), int(m), t0, h, _lib.ptr(st["K"]),
+                _lib.stream_ptr()), "wgc_kernels")
             d.rho0 = rho0
         return d

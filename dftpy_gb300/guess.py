@@ -511,11 +511,13 @@ def training_cell(seed, reps=(2, 2, 2), nr=(64, 64, 64), mg_max=0.3, sigmas=(0.1
 
 
 def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 64, 64), workers=16, chunk=64,
-                 mg_max=0.3, sigmas=(0.15,), cells="small"):
+                 mg_max=0.3, sigmas=(0.15,), cells="small", store="cuda"):
     """(x, sqrt(rho_atom), sqrt(rho converged), rho0) per seed from the
     solver's own converged densities (solved as batches).  cells "small":
     ``training_cell`` (2x2x2 cells at 64^3); "alloy": the batched workload's
-    own generator (``systems.config_alloy``, 108-500 atoms, 96^3-160^3)."""
+    own generator (``systems.config_alloy``, 108-500 atoms, 96^3-160^3).
+    store "cpu" keeps the samples in pinned host memory (``train`` copies
+    each to the device when it is used)."""
     from .batch import build_evaluator, optimize_batch
     data = []
     seeds = list(seeds)
@@ -529,6 +531,8 @@ def make_dataset(seeds, kedf="WGC", precision="mixed", reps=(2, 2, 2), nr=(64, 6
                 continue
             x, phib, rho0 = features(total, rho_u.grid)
             phit = torch.sqrt(torch.clamp(r.rho.as_subclass(torch.Tensor).to(torch.float32), min=SQRT_CLAMP))
+            if store == "cpu":
+                x, phib, phit = (t.cpu().pin_memory() for t in (x, phib, phit))
             data.append((x, phib, phit, rho0))
         # the chunk's evaluators (plans, workspaces) go before the next chunk's
         del jobs, res
@@ -556,6 +560,8 @@ def train(net, data, epochs=10, lr=1e-3, lr_min=1e-5, seed=0, log=None, tc=True)
         tot = 0.0
         for i in order:
             x, phib, phit, rho0 = data[i]
+            if not x.is_cuda:
+                x, phib, phit = (t.to("cuda", non_blocking=True) for t in (x, phib, phit))
             sh = [int(rng.integers(n)) for n in x.shape[1:]]
             x_ = torch.roll(x, shifts=sh, dims=(1, 2, 3)).contiguous()
             pb = torch.roll(phib, shifts=sh, dims=(0, 1, 2)).contiguous()
@@ -657,6 +663,8 @@ def main():
                                                            "network")
     p.add_argument("--cells", default="small", choices=["small", "alloy"],
                    help="training cells: small 2x2x2 cells at 64^3, or the batched workload's snapshots")
+    p.add_argument("--store", default=None, choices=["cuda", "cpu"],
+                   help="where the training samples are kept (default: host memory for alloy cells)")
     p.add_argument("--eval", type=int, default=8, help="held-out cells (seeds 5000 ...)")
     p.add_argument("--out", default=None)
     p.add_argument("--kedf", default="WGC", help="KEDF of the training solves (WGC: the batched workload's; "
@@ -666,7 +674,9 @@ def main():
     a = p.parse_args()
     sigmas = tuple(float(v) for v in a.sigma.split(","))
     t0 = time.perf_counter()
-    data = make_dataset(range(1000, 1000 + a.train), kedf=a.kedf, mg_max=a.mg_max, sigmas=sigmas, cells=a.cells)
+    store = a.store or ("cpu" if a.cells == "alloy" else "cuda")
+    data = make_dataset(range(1000, 1000 + a.train), kedf=a.kedf, mg_max=a.mg_max, sigmas=sigmas, cells=a.cells,
+                        store=store)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     net = GuessNet(channels=tuple(int(c) for c in a.channels.split(",")), seed=0, res=a.res)

@@ -46,6 +46,22 @@ def test_error_path_without_device_work(lib):
         lib.check(rc)
 
 
+def test_allocation_failure_retried_once(lib):
+    """An allocation status makes ``check_alloc`` release PyTorch's cache and
+    call once more; a second failure (or any other status) raises."""
+    rcs = [4, 0]
+    lib.check_alloc(lambda: rcs.pop(0), "create")
+    assert rcs == []
+    rcs = [4, 4, 0]
+    with pytest.raises(MemoryError):
+        lib.check_alloc(lambda: rcs.pop(0), "create")
+    assert rcs == [0]
+    rcs = [1, 0]
+    with pytest.raises(ValueError):
+        lib.check_alloc(lambda: rcs.pop(0), "create")
+    assert rcs == [0]
+
+
 LS_CASES = {
     "quad": lambda a: ((a - 0.7) ** 2, 2.0 * (a - 0.7)),
     "cos": lambda a: (-np.cos(a - 0.3) + 0.01 * a ** 4, np.sin(a - 0.3) + 0.04 * a ** 3),

@@ -32,6 +32,22 @@ from .optimization import Optimization
 # (3.7e-7 Ha/atom) accuracy the mixed-precision solves are held to
 DEFAULT_OPTIONS = {"econv_per_atom": 1e-8, "maxfun": 50, "maxiter": 100, "precision": "mixed"}
 
+# worker streams, kept from batch to batch: PyTorch's caching allocator
+# reuses a freed block only on the stream it was allocated on, so new streams
+# per batch would leave every earlier batch's blocks reserved and unused
+_STREAMS = {}
+_STREAMS_LOCK = threading.Lock()
+
+
+def worker_streams(n):
+    """``n`` CUDA streams of the current device, the same ones on every call."""
+    dev = torch.cuda.current_device()
+    with _STREAMS_LOCK:
+        pool = _STREAMS.setdefault(dev, [])
+        while len(pool) < n:
+            pool.append(torch.cuda.Stream(device=dev))
+        return pool[:n]
+
 
 @dataclass
 class BatchResult:
@@ -105,7 +121,7 @@ def optimize_batch(jobs, workers=None, options=None, kedf="WGC", guess=None, **k
         return []
     n = len(prepared)
     workers = min(n, 16) if workers is None else max(1, min(int(workers), n))
-    streams = [torch.cuda.Stream() for _ in range(workers)]
+    streams = worker_streams(workers)
     slots = list(range(workers))
     lock = threading.Lock()
     if guess is not None:

@@ -455,14 +455,36 @@ def features(total, grid):
     return x, phib, rho0
 
 
+def residual(total, rho):
+    """||(V - mu) sqrt(rho)|| (L2 over the cell) of the FP32 potential at
+    ``rho``, mu = int V rho / int rho: the square root of the residual norm
+    the reference TN prints at its first step (``optimization.py:318-340``,
+    residual = (V - mu) phi)."""
+    from .field import DirectField
+    grid = rho.grid
+    x = DirectField(grid, data=rho.as_subclass(torch.Tensor).to(torch.float32))
+    v = total(x, calcType={"V"}).potential.as_subclass(torch.Tensor).to(torch.float64)
+    r = x.as_subclass(torch.Tensor).to(torch.float64)
+    mu = (v * r).sum() / r.sum()
+    return float(torch.sqrt(((v - mu) ** 2 * r.clamp(min=0.0)).sum() * grid.dV))
+
+
 class LearnedGuess:
     """Starting density from a trained ``GuessNet``: the network's density,
     mixed with the uniform density when ``mix`` < 1 (rho0 + mix (rho_net -
-    rho0); None: the value saved with the network, else 1)."""
+    rho0); None: the value saved with the network, else 1).
 
-    def __init__(self, net, mix=None):
+    fallback: compare the FP32 residual (``residual``) of the network's
+    density with the uniform density's and start from the uniform density
+    when the network's is not below ``fallback_ratio`` times it (two FP32
+    potential evaluations per guess); ``last_choice`` records the pick."""
+
+    def __init__(self, net, mix=None, fallback=True, fallback_ratio=1.0):
         self.net = net
         self.mix = float(mix) if mix is not None else float(getattr(net, "mix", 1.0))
+        self.fallback = bool(fallback)
+        self.fallback_ratio = float(fallback_ratio)
+        self.last_choice = None
 
     def prepare(self, total, grid=None):
         """Make the network's packed tensor-core weights (every layer whose
@@ -485,10 +507,17 @@ class LearnedGuess:
         rho = (phi * phi).to(torch.float64)
         nel = float(total.PSEUDO.ions.get_ncharges())
         rho = rho * (nel / (float(rho.sum()) * grid.dV))
+        rho0_u = nel / grid.volume
         if self.mix != 1.0:
-            rho0_u = nel / grid.volume
             rho = rho0_u + self.mix * (rho - rho0_u)
-        return DirectField(grid, data=rho.to(dtype))
+        out = DirectField(grid, data=rho.to(dtype))
+        choice = "network"
+        if self.fallback:
+            uni = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
+            if not residual(total, out) < self.fallback_ratio * residual(total, uni):
+                out, choice = uni, "uniform"
+        self.last_choice = choice
+        return out
 
 
 def _solve(total, guess, precision="mixed", econv_per_atom=1e-8):

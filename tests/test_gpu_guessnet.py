@@ -239,6 +239,38 @@ def test_al_network_gain_on_al256(gn):
     assert abs(o_l.energy - o_u.energy) / st.nat * 27.211386 < 1e-8
 
 
+def test_fallback_to_uniform_when_the_network_is_worse(gn):
+    """``LearnedGuess`` keeps the network's density when its FP32 residual is
+    below the uniform density's and starts from the uniform density
+    otherwise: the trained WT network on the 256-atom cell is kept, an
+    untrained network (random weights, head scaled 50x) is replaced.
+    ``residual`` equals a float64 numpy restatement of ||(V - mu) phi||."""
+    import torch
+    from dftpy_gb300 import systems
+    from dftpy_gb300.batch import build_evaluator
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    st = systems.config_al256(0)
+    total, rho_u = build_evaluator(st, kedf="WT")
+    good = gn.LearnedGuess(gn.GuessNet.load(os.path.join(here, "dftpy_gb300", "data", "guessnet_al_wt.npz")))
+    g = good.guess(total, rho_u.grid)
+    assert good.last_choice == "network"
+    r_net, r_uni = gn.residual(total, g), gn.residual(total, rho_u)
+    assert r_net < r_uni
+    v = total(g.to(torch.float32), calcType={"V"}).potential.as_subclass(torch.Tensor).double().cpu().numpy()
+    r = g.as_subclass(torch.Tensor).float().double().cpu().numpy()
+    mu = (v * r).sum() / r.sum()
+    ref = np.sqrt(((v - mu) ** 2 * np.maximum(r, 0)).sum() * rho_u.grid.dV)
+    assert abs(r_net - ref) <= 1e-9 * ref
+    bad_net = gn.GuessNet(channels=(16, 32, 48, 64), seed=11)
+    bad_net.head.w.mul_(50.0)
+    bad_net.head.sync_bf16()
+    bad = gn.LearnedGuess(bad_net)
+    b = bad.guess(total, rho_u.grid)
+    assert bad.last_choice == "uniform"
+    assert torch.allclose(b.as_subclass(torch.Tensor), rho_u.as_subclass(torch.Tensor).to(b.dtype), rtol=1e-13,
+                          atol=0.0)
+
+
 def test_tensor_core_training_matches_fp32(gn):
     """Training on the tensor cores (forward and input-gradient convolutions
     with BF16 operands where a layer's shape has a kernel, weight gradients on

@@ -158,6 +158,8 @@ class WGCTerm:
         key = (id(rho.grid), rho.dtype)
         st = self._state.get(key)
         rho0 = self.fixed_rho0 or float(rho.as_subclass(torch.Tensor).to(torch.float64).mean())
+        if not (math.isfinite(rho0) and rho0 > 0.0):
+            raise ValueError("WGC: the mean density must be positive and finite (got %r)" % rho0)
         plan = rho.grid.plan(rho.dtype)
         if st is None:
             nb = ctypes.c_int64()

@@ -257,10 +257,11 @@ class GuessNet:
     IN_CHANNELS = 2
 
     def __init__(self, channels=(16, 32, 48, 64), seed=0, res=1):
-        """res 2: the network runs on the 2x average-pooled features and its
-        output is upsampled back (periodic trilinear) -- 8x less work."""
-        if int(res) not in (1, 2):
-            raise ValueError("res must be 1 or 2")
+        """res 2 (4): the network runs on the 2x (twice 2x) average-pooled
+        features and its output is upsampled back by periodic trilinear 2x
+        steps -- 8x (64x) less work."""
+        if int(res) not in (1, 2, 4):
+            raise ValueError("res must be 1, 2 or 4")
         self.res = int(res)
         self.mix = 1.0          # the LearnedGuess mixing factor this network was evaluated with
         rng = np.random.default_rng(seed)
@@ -295,13 +296,20 @@ class GuessNet:
 
     def forward(self, x, keep=False, tc=True, tc_train=False):
         """x: (2, D, H, W) FP32 -> (1, D, H, W) (see ``_forward``); with res 2
-        the network sees pool2(x) and its output is upsampled."""
+        (4) the network sees pool2(x) (twice) and its output is upsampled."""
         shape = tuple(x.shape[1:])
         if any(s % self.stride for s in shape):
             raise ValueError("grid %s not divisible by %d" % (shape, self.stride))
-        if self.res == 1:
-            return self._forward(x, keep, tc, tc_train)
-        return uplin(self._forward(pool2(x), keep, tc, tc_train))
+        for _ in range(self._halvings):
+            x = pool2(x)
+        out = self._forward(x, keep, tc, tc_train)
+        for _ in range(self._halvings):
+            out = uplin(out)
+        return out
+
+    @property
+    def _halvings(self):
+        return {1: 0, 2: 1, 4: 2}[self.res]
 
     def _forward(self, x, keep=False, tc=True, tc_train=False):
         """x: (2, D, H, W) FP32 -> (1, D, H, W).  keep: record what backward
@@ -373,7 +381,7 @@ class GuessNet:
         tape = self._tape
         if tape is None:
             raise RuntimeError("forward(keep=True) must precede backward")
-        if self.res == 2:
+        for _ in range(self._halvings):
             gout = uplin_bwd(gout.contiguous())
         _, _, h = tape[-1]
         shape = tuple(h.shape[1:])
@@ -476,8 +484,9 @@ class LearnedGuess:
 
     fallback: compare the FP32 residual (``residual``) of the network's
     density with the uniform density's and start from the uniform density
-    when the network's is not below ``fallback_ratio`` times it (two FP32
-    potential evaluations per guess); ``last_choice`` records the pick."""
+    when the network's is not below ``fallback_ratio`` times it, or is not
+    finite (two FP32 potential evaluations per guess); ``last_choice``
+    records the pick."""
 
     def __init__(self, net, mix=None, fallback=True, fallback_ratio=1.0):
         self.net = net
@@ -514,7 +523,8 @@ class LearnedGuess:
         choice = "network"
         if self.fallback:
             uni = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
-            if not residual(total, out) < self.fallback_ratio * residual(total, uni):
+            if not bool(torch.isfinite(rho).all()) or \
+                    not residual(total, out) < self.fallback_ratio * residual(total, uni):
                 out, choice = uni, "uniform"
         self.last_choice = choice
         return out
@@ -687,7 +697,8 @@ def main():
     p.add_argument("--epochs", type=int, default=8)
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--channels", default="16,32,48,64")
-    p.add_argument("--res", type=int, default=1, help="2: the network runs on 2x pooled features")
+    p.add_argument("--res", type=int, default=1, choices=[1, 2, 4],
+                   help="2 (4): the network runs on 2x (4x) pooled features")
     p.add_argument("--mix", type=float, default=1.0, help="mixing factor with the uniform density saved with the "
                                                            "network")
     p.add_argument("--cells", default="small", choices=["small", "alloy"],

@@ -1,6 +1,6 @@
 """Repeat the functional evaluation of the 256-atom / 128^3 WT workload (or
 of one Al/Mg alloy snapshot of the batched WGC workload, ``--workload alloy
---seed S``).
+--seed S``, or of the 4000-atom 360^3 LMGP cell, ``--workload al4000``).
 
 ``python -m dftpy_gb300.profile_eval --precision fp32 --calc V --reps 3``
 sets the structure up, runs warm-up evaluations, then ``reps`` evaluations
@@ -20,7 +20,7 @@ def main():
     p.add_argument("--calc", default="V", choices=["V", "EV"])
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--workload", default="al256", choices=["al256", "al4", "alloy"])
+    p.add_argument("--workload", default="al256", choices=["al256", "al4", "alloy", "al4000"])
     p.add_argument("--seed", type=int, default=0, help="alloy snapshot seed")
     p.add_argument("--solve", default=None, choices=["mixed", "fp64", "fp32"],
                    help="instead of single evaluations, run whole TN solves (NVTX range 'solve')")
@@ -36,6 +36,10 @@ def main():
         st = systems.config_alloy(a.seed)
         total, _ = build_evaluator(st, kedf="WGC")
         grid = total.PSEUDO.grid
+        econv = 1e-8 * st.nat
+    elif a.workload == "al4000":
+        from .large import build
+        st, grid, total, _, _ = build()
         econv = 1e-8 * st.nat
     else:
         st = systems.config_al256(0) if a.workload == "al256" else systems.config_al4(0)
@@ -77,6 +81,15 @@ def main():
     g = torch.Generator(device="cuda").manual_seed(0)
     base = st.nelec / st.volume
     x = (base * (1.0 + 0.05 * torch.randn(tuple(st.nr), generator=g, device="cuda", dtype=torch.float64))).to(dt)
+    if a.workload == "al4000":
+        # the superposed atomic densities: the k_F range (and the LMGP knot
+        # count) of a real solve, not of a near-uniform noise field
+        from .density import DensityGenerator
+        from .ions import Ions
+        r_, a_ = systems.atomic_density_table(3.0, systems.ATOMIC_SIGMA["Al"])
+        ions = Ions(st.symbols, positions=st.positions, cell=st.lattice)
+        x = DensityGenerator(r={"Al": r_}, arho={"Al": a_}).guess_rho(ions, grid=grid).as_subclass(
+            torch.Tensor).to(dt)
     rho = DirectField(grid, data=x)
     f = total.spec(rho).ctypes()
     plan = grid.plan(dt)
@@ -98,8 +111,10 @@ def main():
     e1.record()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
-    print("eval %s %s %s: %.1f us per evaluation" % (a.workload, a.precision, a.calc,
-                                                     e0.elapsed_time(e1) * 1000.0 / a.reps))
+    kd = getattr(getattr(total, "KineticEnergyFunctional", None), "_lwt", None)
+    knots = "" if kd is None else ", %d k_F knots" % kd.prepare(rho).nknots
+    print("eval %s %s %s: %.1f us per evaluation%s" % (a.workload, a.precision, a.calc,
+                                                       e0.elapsed_time(e1) * 1000.0 / a.reps, knots))
     return 0
 
 

@@ -5,8 +5,11 @@ its convolution layers, for profiling.
 tensor-core convolution C_in -> C_out on an n^3 grid (SiLU fused) ``reps``
 times after two warm-up calls and prints the CUDA-event time per call;
 ``python -m dftpy_gb300.profile_guess`` computes the learned guess (features,
-network, normalisation) after two warm-up guesses, once inside an NVTX
-range named ``guess`` (select it with ``--nvtx --nvtx-include guess/``).
+network, normalisation, the fallback's two residuals) after two warm-up
+guesses, once inside an NVTX range named ``guess`` (select it with ``--nvtx
+--nvtx-include guess/``), then times its parts one by one
+(``--workload alloy --seed S``: the alloy network on one snapshot of the
+batched workload).
 """
 import argparse
 import os
@@ -17,6 +20,10 @@ def main():
     p.add_argument("--conv", default=None, help="C_in,C_out,n: time one tensor-core layer on an n^3 grid")
     p.add_argument("--up", action="store_true", help="with --conv: the input is the n/2 grid, read upsampled")
     p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--workload", default="al256", choices=["al256", "alloy"],
+                   help="al256: the WT network on the 256-atom cell; alloy: the alloy network on one snapshot")
+    p.add_argument("--seed", type=int, default=0, help="alloy snapshot seed")
+    p.add_argument("--net", default=None, help="network file (default: the workload's committed network)")
     a = p.parse_args()
     import numpy as np
     import torch
@@ -45,22 +52,44 @@ def main():
         return
     from . import systems
     from .batch import build_evaluator
-    st = systems.config_al256(0)
-    total, rho_u = build_evaluator(st, kedf="WT")
     here = os.path.dirname(os.path.abspath(__file__))
-    lg = G.LearnedGuess(G.GuessNet.load(os.path.join(here, "data", "guessnet_al_wt.npz")))
+    if a.workload == "alloy":
+        st = systems.config_alloy(a.seed)
+        total, rho_u = build_evaluator(st, kedf="WGC")
+        net = a.net or os.path.join(here, "data", "guessnet.npz")
+    else:
+        st = systems.config_al256(0)
+        total, rho_u = build_evaluator(st, kedf="WT")
+        net = a.net or os.path.join(here, "data", "guessnet_al_wt.npz")
+    lg = G.LearnedGuess(G.GuessNet.load(net))
+    grid = rho_u.grid
     for _ in range(2):
-        lg.guess(total, rho_u.grid)
+        lg.guess(total, grid)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("guess")
     e0.record()
-    g = lg.guess(total, rho_u.grid)
+    g = lg.guess(total, grid)
     e1.record()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    print("learned guess al256 128^3: %.3f ms, integral %.6f" % (e0.elapsed_time(e1),
-                                                                 float(g.as_subclass(torch.Tensor).sum()) * rho_u.grid.dV))
+    # the parts of one guess, each timed alone
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev[0].record()
+    x, phib, rho0 = G.features(total, grid)
+    ev[1].record()
+    out = lg.net.forward(x)
+    ev[2].record()
+    r1 = G.residual(total, g)
+    ev[3].record()
+    r2 = G.residual(total, rho_u)
+    ev[4].record()
+    torch.cuda.synchronize()
+    parts = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    print("learned guess %s %s: %.3f ms (choice %s), integral %.6f; features %.3f ms, network %.3f ms, "
+          "residual of the guess %.3f ms, of the uniform density %.3f ms (residuals %.3e / %.3e)"
+          % (a.workload, "x".join(str(int(n)) for n in grid.nrR), e0.elapsed_time(e1), lg.last_choice,
+             float(g.as_subclass(torch.Tensor).sum()) * grid.dV, *parts, r1, r2))
 
 
 if __name__ == "__main__":

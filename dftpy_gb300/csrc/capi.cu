@@ -135,6 +135,23 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   p->NGld = (int64_t)nr[0] * nr[1] * p->ld2;
   p->dV = p->volume / (double)p->N;
   const size_t cs = 2 * gb_elem(p);
+  // The plan's initial device contents (twiddles, the zeroed counter) are
+  // written on a stream of its own and complete before plan_create returns:
+  // cudaMemcpy from pageable memory and cudaMemset return before the device
+  // has finished, on the legacy stream, which the callers' non-blocking
+  // streams do not wait for -- a first transform on such a stream could read
+  // a half-written table.
+  cudaStream_t init_st = nullptr;
+  {
+    cudaError_t e = cudaStreamCreateWithFlags(&init_st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete p; return gb_set_error(GBOFDFT_ERR_CUDA, "plan_create: %s", cudaGetErrorString(e)); }
+  }
+  auto fail = [&](int code, const char* what, cudaError_t e) {
+    cudaStreamSynchronize(init_st);
+    cudaStreamDestroy(init_st);
+    gbofdft_plan_destroy(p);
+    return gb_set_error(code, "plan_create: %s%s", what, cudaGetErrorString(e));
+  };
   for (int a = 0; a < 3; ++a) {
     factorize(nr[a], p->ax[a]);
     std::vector<double> t(2 * (size_t)nr[a]);
@@ -145,14 +162,16 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
       t[2 * m + 1] = (double)sinl(ang);
     }
     cudaError_t e = cudaMalloc(&p->tw[a], cs * nr[a]);
-    if (e != cudaSuccess) { gbofdft_plan_destroy(p); return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) return fail(GBOFDFT_ERR_ALLOC, "", e);
+    // from pageable memory the copy returns once the host buffer is staged,
+    // so t / tf may go out of scope before the stream has run it
     if (precision == GBOFDFT_F64) {
-      e = cudaMemcpy(p->tw[a], t.data(), cs * nr[a], cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(p->tw[a], t.data(), cs * nr[a], cudaMemcpyHostToDevice, init_st);
     } else {
       std::vector<float> tf(t.begin(), t.end());
-      e = cudaMemcpy(p->tw[a], tf.data(), cs * nr[a], cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(p->tw[a], tf.data(), cs * nr[a], cudaMemcpyHostToDevice, init_st);
     }
-    if (e != cudaSuccess) { gbofdft_plan_destroy(p); return gb_set_error(GBOFDFT_ERR_CUDA, "plan_create: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) return fail(GBOFDFT_ERR_CUDA, "", e);
   }
   // column tile: keep (n + 2 n tb) complex elements within ~96 KB
   for (int a = 0; a < 3; ++a) {
@@ -166,6 +185,8 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   const size_t rows_sm = cs * ((size_t)nr[2] + 2 * (size_t)GB_MAX_FIELDS * p->pairs * nr[2]);
   if (rows_sm > 200 * 1024 || cs * ((size_t)nr[0] * (1 + 2 * p->tb[0])) > 220 * 1024 ||
       cs * ((size_t)nr[1] * (1 + 2 * p->tb[1])) > 220 * 1024) {
+    cudaStreamSynchronize(init_st);
+    cudaStreamDestroy(init_st);
     gbofdft_plan_destroy(p);
     return gb_set_error(GBOFDFT_ERR_UNSUPPORTED, "plan_create: grid %dx%dx%d too large for the line passes",
                         nr[0], nr[1], nr[2]);
@@ -175,10 +196,14 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   p->max_partials = (nrows + 2 * p->pairs - 1) / (2 * p->pairs) + 1;
   if (e == cudaSuccess) e = cudaMalloc(&p->partials, sizeof(double) * GB_NE * p->max_partials);
   if (e == cudaSuccess) e = cudaMalloc(&p->scratch, sizeof(double) * 4096);
-  if (e == cudaSuccess) e = cudaMemset(p->scratch, 0, sizeof(double) * 4096);  // the counter slot starts at 0
+  // the counter slot starts at 0
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->scratch, 0, sizeof(double) * 4096, init_st);
+  if (e != cudaSuccess) return fail(GBOFDFT_ERR_ALLOC, "workspace: ", e);
+  e = cudaStreamSynchronize(init_st);
+  cudaStreamDestroy(init_st);
   if (e != cudaSuccess) {
     gbofdft_plan_destroy(p);
-    return gb_set_error(GBOFDFT_ERR_ALLOC, "plan_create: workspace: %s", cudaGetErrorString(e));
+    return gb_set_error(GBOFDFT_ERR_CUDA, "plan_create: initial copies: %s", cudaGetErrorString(e));
   }
   memcpy(p->gi.bg, p->bg, sizeof(p->bg));
   p->gi.n0 = nr[0]; p->gi.n1 = nr[1]; p->gi.n2 = nr[2]; p->gi.n2h = p->n2h; p->gi.ld2 = p->ld2;

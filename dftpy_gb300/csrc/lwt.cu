@@ -88,26 +88,26 @@ __device__ __forceinline__ A lwt_kval(const GInfo& g, const BG<A>& bg, const UTa
   }
 }
 
+// Spectral kernels walk the half spectrum row by row: one CTA per (i0, i1)
+// row at a time, its threads over k2, so no per-element index division.
 // dst[f] = coef_f * K_f(q / kf) * src   (f = 0: kernel table, f = 1: derivative table)
 template <typename T>
 __global__ void k_lwt_kmul(GInfo g, BG<T> bg, const cpx<T>* __restrict__ src, int64_t sld, cpx<T>* __restrict__ dst,
                            int64_t dfs, int nf, UTable<T> tk, UTable<T> td, double kf, double scale) {
-  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  const int nrow = g.n0 * g.n1;
   const T inv_kf = (T)(1.0 / kf), kfT = (T)kf, scT = (T)scale;
-  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
-       id += (int64_t)gridDim.x * blockDim.x) {
-    const int k2 = (int)(id % g.n2h);
-    const int64_t r = id / g.n2h;
-    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
-    const int64_t row = (int64_t)i0 * g.n1 + i1;
-    const cpx<T> s = src[row * sld + k2];
-    for (int f = 0; f < nf; ++f) {
-      const UTable<T>& t = f == 0 ? tk : td;
-      T kv = (T)0;
-      if (!(i0 == 0 && i1 == 0 && k2 == 0)) kv = lwt_kval<T>(g, bg, t, inv_kf, i0, i1, k2);
-      if (f == 1) kv /= kfT;
-      const T c = kv * scT;
-      dst[f * dfs + row * g.ld2 + k2] = cpx<T>{s.x * c, s.y * c};
+  for (int row = blockIdx.x; row < nrow; row += gridDim.x) {
+    const int i0 = row / g.n1, i1 = row - i0 * g.n1;
+    for (int k2 = threadIdx.x; k2 < g.n2h; k2 += blockDim.x) {
+      const cpx<T> s = src[(int64_t)row * sld + k2];
+      for (int f = 0; f < nf; ++f) {
+        const UTable<T>& t = f == 0 ? tk : td;
+        T kv = (T)0;
+        if (!(i0 == 0 && i1 == 0 && k2 == 0)) kv = lwt_kval<T>(g, bg, t, inv_kf, i0, i1, k2);
+        if (f == 1) kv /= kfT;
+        const T c = kv * scT;
+        dst[f * dfs + (int64_t)row * g.ld2 + k2] = cpx<T>{s.x * c, s.y * c};
+      }
     }
   }
 }
@@ -116,14 +116,12 @@ __global__ void k_lwt_kmul(GInfo g, BG<T> bg, const cpx<T>* __restrict__ src, in
 template <typename T>
 __global__ void k_lwt_acc(GInfo g, BG<T> bg, const cpx<T>* __restrict__ U, int64_t ufs, int nf, UTable<T> tk,
                           UTable<T> td, double kf, double scale, cpx<T>* __restrict__ acc, int first) {
-  const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
+  const int nrow = g.n0 * g.n1;
   const T inv_kf = (T)(1.0 / kf), kfT = (T)kf, scT = (T)scale;
-  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
-       id += (int64_t)gridDim.x * blockDim.x) {
-    const int k2 = (int)(id % g.n2h);
-    const int64_t r = id / g.n2h;
-    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
-    const int64_t o = ((int64_t)i0 * g.n1 + i1) * g.ld2 + k2;
+  for (int row = blockIdx.x; row < nrow; row += gridDim.x)
+  for (int k2 = threadIdx.x; k2 < g.n2h; k2 += blockDim.x) {
+    const int i0 = row / g.n1, i1 = row - i0 * g.n1;
+    const int64_t o = (int64_t)row * g.ld2 + k2;
     T ax = (T)0, ay = (T)0;
     if (!(i0 == 0 && i1 == 0 && k2 == 0)) {
       for (int f = 0; f < nf; ++f) {
@@ -354,6 +352,18 @@ int blocks_for(int64_t n) {
 
 size_t r256(size_t x) { return (x + 255) / 256 * 256; }
 
+// launch shape of the row-wise spectral kernels: threads cover one half
+// row (k2 = 0 .. n2h-1) in whole warps, CTAs stride over the rows
+struct RowLaunch {
+  int blocks, threads;
+};
+RowLaunch row_launch(const gbofdft_plan* p) {
+  const int nrow = p->gi.n0 * p->gi.n1;
+  int th = (p->gi.n2h + 31) / 32 * 32;
+  if (th > 256) th = 256;
+  return RowLaunch{nrow < 4096 ? nrow : 4096, th};
+}
+
 constexpr int kMaxNetaF32 = 200001;   // FP32 table copies: coefficients of at most this many points
 
 struct LwtBufs {
@@ -370,7 +380,9 @@ LwtBufs lwt_layout(const gbofdft_plan* p, void* work) {
   char* b = reinterpret_cast<char*>(work);
   const size_t fb = lwt_field_bytes(p), sb = lwt_spec_bytes(p);
   LwtBufs L;
-  void** fields[] = {&L.p[0], &L.p[1], &L.m[0], &L.m[1], &L.w[0], &L.w[1], &L.wd[0], &L.wd[1],
+  // p[c] and m[c] adjacent: the inverse transforms of a knot's two spectra
+  // are one launch sequence with a field stride of one field
+  void** fields[] = {&L.p[0], &L.m[0], &L.p[1], &L.m[1], &L.w[0], &L.w[1], &L.wd[0], &L.wd[1],
                      &L.pot1, &L.pot2, &L.pot3, &L.kf, &L.ra};
   for (int i = 0; i < 13; ++i) { *fields[i] = b; b += fb; }
   L.ktab_f = reinterpret_cast<float*>(b); b += r256(sizeof(float) * 4 * (size_t)kMaxNetaF32);
@@ -490,6 +502,7 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   k_lwt_pre<T><<<nb, 256, 0, st>>>(N, rhoT, kfmax, d->alpha, reinterpret_cast<T*>(L.kf), reinterpret_cast<T*>(L.ra));
   GB_CHECK_LAUNCH();
   const double invN = 1.0 / (double)N;
+  const RowLaunch rl = row_launch(p);
   const size_t fb = lwt_field_bytes(p), sb = lwt_spec_bytes(p);
   const int64_t sfs = (int64_t)(sb / (2 * gb_elem(p)));  // complex elements per spectrum slot
   // shared forward transform of rho^beta (rho clamped to 1e-30 below)
@@ -503,15 +516,11 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   int cur = 0;
   for (int k = 0; k < nsp; ++k) {
     // p_k (and m_k) from the shared spectrum
-    k_lwt_kmul<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs, nkf, tk, td, kfl[k],
-                                       invN);
+    k_lwt_kmul<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs, nkf,
+                                                     tk, td, kfl[k], invN);
     GB_CHECK_LAUNCH();
-    // pm slots: p[cur], m[cur] must be adjacent for one inverse with nf = 2:
-    // inverse into p[cur] then copy to m[cur] when needed (p and m are separate fields)
-    if ((rc = inv3d(p, L.T, sfs, 1, L.p[cur], 0, st))) return rc;
-    if (mcalc) {
-      if ((rc = inv3d(p, (char*)L.T + sb, sfs, 1, L.m[cur], 0, st))) return rc;
-    }
+    // p[cur] (and m[cur], the next field) from the knot's spectra in T
+    if ((rc = inv3d(p, L.T, sfs, mcalc ? 2 : 1, L.p[cur], (int64_t)(fb / gb_elem(p)), st))) return rc;
     if (k >= 1) {
       const int prv = cur ^ 1;
       IntervalArgs a;
@@ -531,8 +540,8 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
         // weights of knot k-1 are complete: pot2G += K_{k-1} fft(w) (+ D_{k-1} fft(wd))
         if ((rc = fwd3d(p, L.w[prv], L.U, OP_RHO, 1.0, st))) return rc;
         if (hermite && (rc = fwd3d(p, L.wd[prv], (char*)L.U + sb, OP_RHO, 1.0, st))) return rc;
-        k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[k - 1], invN,
-                                          (cpx<T>*)L.G, k == 1);
+        k_lwt_acc<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[k - 1],
+                                                        invN, (cpx<T>*)L.G, k == 1);
         GB_CHECK_LAUNCH();
       }
     }
@@ -542,8 +551,8 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   if (kdd > 1) {
     if ((rc = fwd3d(p, L.w[last], L.U, OP_RHO, 1.0, st))) return rc;
     if (hermite && (rc = fwd3d(p, L.wd[last], (char*)L.U + sb, OP_RHO, 1.0, st))) return rc;
-    k_lwt_acc<T><<<nb, 256, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[nsp - 1], invN,
-                                      (cpx<T>*)L.G, 0);
+    k_lwt_acc<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[nsp - 1],
+                                                    invN, (cpx<T>*)L.G, 0);
     GB_CHECK_LAUNCH();
     if (calc_v && (rc = inv3d(p, L.G, sfs, 1, L.pot2, 0, st))) return rc;
   }

@@ -477,16 +477,35 @@ def residual(total, rho):
     return float(torch.sqrt(((v - mu) ** 2 * r.clamp(min=0.0)).sum() * grid.dV))
 
 
+def uniform_residual(total, grid):
+    """``residual`` at the uniform density.  When every member of ``total``
+    is one of this package's functionals the potential there is a constant
+    plus v_loc (the semilocal terms are constant, vW and Hartree vanish, the
+    nonlocal kernels act on a constant), so the residual is
+    sqrt(rho0) ||v_loc - <v_loc>||, a reduction without an evaluation."""
+    from .field import DirectField
+    nel = float(total.PSEUDO.ions.get_ncharges())
+    rho0 = nel / grid.volume
+    fusable = getattr(total, "fusable", None)
+    if fusable is not None and fusable():
+        v = total.PSEUDO.vreal_of(torch.float64)
+        dv = v - v.mean()
+        return float(torch.sqrt((dv * dv).sum() * (rho0 * grid.dV)))
+    uni = DirectField(grid, data=torch.full(tuple(int(n) for n in grid.nrR), rho0, dtype=torch.float64,
+                                            device="cuda"))
+    return residual(total, uni)
+
+
 class LearnedGuess:
     """Starting density from a trained ``GuessNet``: the network's density,
     mixed with the uniform density when ``mix`` < 1 (rho0 + mix (rho_net -
     rho0); None: the value saved with the network, else 1).
 
     fallback: compare the FP32 residual (``residual``) of the network's
-    density with the uniform density's and start from the uniform density
-    when the network's is not below ``fallback_ratio`` times it, or is not
-    finite (two FP32 potential evaluations per guess); ``last_choice``
-    records the pick."""
+    density with the uniform density's (``uniform_residual``) and start from
+    the uniform density when the network's is not below ``fallback_ratio``
+    times it, or is not finite (one FP32 potential evaluation per guess);
+    ``last_choice`` records the pick."""
 
     def __init__(self, net, mix=None, fallback=True, fallback_ratio=1.0):
         self.net = net
@@ -522,10 +541,10 @@ class LearnedGuess:
         out = DirectField(grid, data=rho.to(dtype))
         choice = "network"
         if self.fallback:
-            uni = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
             if not bool(torch.isfinite(rho).all()) or \
-                    not residual(total, out) < self.fallback_ratio * residual(total, uni):
-                out, choice = uni, "uniform"
+                    not residual(total, out) < self.fallback_ratio * uniform_residual(total, grid):
+                out = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
+                choice = "uniform"
         self.last_choice = choice
         return out
 

@@ -82,12 +82,12 @@ def main():
     ev[2].record()
     r1 = G.residual(total, g)
     ev[3].record()
-    r2 = G.residual(total, rho_u)
+    r2 = G.uniform_residual(total, grid)
     ev[4].record()
     torch.cuda.synchronize()
     parts = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
     print("learned guess %s %s: %.3f ms (choice %s), integral %.6f; features %.3f ms, network %.3f ms, "
-          "residual of the guess %.3f ms, of the uniform density %.3f ms (residuals %.3e / %.3e)"
+          "residual of the guess %.3f ms, of the uniform density (from v_loc) %.3f ms (residuals %.3e / %.3e)"
           % (a.workload, "x".join(str(int(n)) for n in grid.nrR), e0.elapsed_time(e1), lg.last_choice,
              float(g.as_subclass(torch.Tensor).sum()) * grid.dV, *parts, r1, r2))
 

@@ -244,7 +244,8 @@ def test_fallback_to_uniform_when_the_network_is_worse(gn):
     below the uniform density's and starts from the uniform density
     otherwise: the trained WT network on the 256-atom cell is kept, an
     untrained network (random weights, head scaled 50x) is replaced.
-    ``residual`` equals a float64 numpy restatement of ||(V - mu) phi||."""
+    ``residual`` equals a float64 numpy restatement of ||(V - mu) phi||, and
+    ``uniform_residual`` (from v_loc alone) the evaluated one."""
     import torch
     from dftpy_gb300 import systems
     from dftpy_gb300.batch import build_evaluator
@@ -256,6 +257,8 @@ def test_fallback_to_uniform_when_the_network_is_worse(gn):
     assert good.last_choice == "network"
     r_net, r_uni = gn.residual(total, g), gn.residual(total, rho_u)
     assert r_net < r_uni
+    # at the uniform density the potential is a constant plus v_loc
+    assert abs(gn.uniform_residual(total, rho_u.grid) - r_uni) <= 1e-4 * r_uni
     v = total(g.to(torch.float32), calcType={"V"}).potential.as_subclass(torch.Tensor).double().cpu().numpy()
     r = g.as_subclass(torch.Tensor).float().double().cpu().numpy()
     mu = (v * r).sum() / r.sum()

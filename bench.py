@@ -9,10 +9,12 @@ Bohr spacing, Mg fraction U(0, 0.3), jitter 0.15 Bohr), KEDF TF + vW + WGC
 (second-order density-dependent kernel) + LDA + Hartree + analytic local
 pseudopotentials (PME), econv 1e-8 Ha/atom.  One "step" optimises all 64:
 each structure's starting density comes from the guess network
-(``dftpy_gb300/data/guessnet.npz``, trained on the solver's own converged
-densities of held-apart snapshots; tensor-core inference inside the step),
-then FP32 truncated Newton and the FP64 refinement, 16 structures in flight on
-their own streams.  The evaluators' set-up (pseudopotentials, Ewald, kernel
+(``dftpy_gb300/data/guessnet.npz``: 4-level encoder-decoder, 32-128 channels,
+1.5 M parameters, run on 4x pooled features; trained on the solver's own
+converged densities of 2000 other snapshots, seeds 1000-2999; inference on the
+tensor cores inside the step, with the fallback check against the uniform
+density's residual), then FP32 truncated Newton and the FP64 refinement, 16
+structures in flight on their own streams.  The evaluators' set-up (pseudopotentials, Ewald, kernel
 tables, plans) is done before the timed steps, as the reference's timing
 excludes it.  ``value`` is the wall time of one step.  Beside it: the plain
 FP64 batch (the reference's method: uniform start, unpreconditioned TN, FP64
@@ -724,8 +726,9 @@ def main():
                    "natoms_range": [min(nat), max(nat)], "grids": sorted({tuple(j[1].grid.nrR) for j in jobs}),
                    "functional": "TF+vW+WGC(second order)+LDA+Hartree+analytic PP (PME order 10)",
                    "method": "TN econv 1e-8 Ha/atom, maxfun 50", "precision": args.precision,
-                   "guess": ("learned (BF16 tcgen05 network dftpy_gb300/data/guessnet.npz; inference inside the "
-                             "step)") if guess is not None else "uniform",
+                   "guess": ("learned (BF16 tcgen05 network dftpy_gb300/data/guessnet.npz, 1.5 M parameters on "
+                             "4x pooled features; inference and its fallback check inside the step)")
+                            if guess is not None else "uniform",
                    "in_flight": args.workers, "l2": "512 MB buffer written between timed steps",
                    "sharding": "longest-processing-time on grid points over ranks"},
         "converged": n_conv,

@@ -45,6 +45,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HA_EV = 27.211386024367243
+
+
+def _plain(o):
+    """json.dumps default: numpy scalars and arrays as Python numbers and lists."""
+    if hasattr(o, "tolist"):
+        return o.tolist()
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError("%s is not JSON serializable" % type(o).__name__)
 TOL_EV_PER_ATOM = 1e-5
 METRIC = "wall-s to converged OFDFT energy (<=1e-5 eV/atom vs FP64), learned+mixed vs plain"
 ECONV_PER_ATOM = 1e-8
@@ -507,7 +516,8 @@ def run_reference(args):
     from dftpy_gb300 import batch, systems
     fix = oracle_fixture()
     if fix is None:
-        print(json.dumps({"impl": "reference", "unavailable": "tests/golden/alloy64_oracle.npz is missing"}))
+        print(json.dumps({"impl": "reference", "unavailable": "tests/golden/alloy64_oracle.npz is missing"},
+                         default=_plain))
         return 0
     seeds = list(range(args.n))
     cores = os.cpu_count() or 1
@@ -574,7 +584,7 @@ def run_reference(args):
                                    "set-up excluded" % (workers, statistics.mean(walls), len(seeds), workers)},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_plain), flush=True)
     return 0
 
 
@@ -602,7 +612,7 @@ def main_al256(args):
                       "config": {"workload": "al256_128_wt"}, "evaluations": evals[-1],
                       "roofline": {"bound": "hbm", "achieved": b_eval / t_eval / 1e9, "peak": peak, "unit": "GB/s",
                                    "frac": b_eval / t_eval / 1e9 / peak, "peak_kind": peak_kind},
-                      "clocks": clk}), flush=True)
+                      "clocks": clk}, default=_plain), flush=True)
     return 0
 
 
@@ -744,7 +754,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_plain), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

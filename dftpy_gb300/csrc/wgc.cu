@@ -33,6 +33,7 @@ struct WgcBufs {
   double* part;     // per-CTA energy partials
   double* vref;     // FP64 plans: the NL potential of the last reference evaluation [N]
   double* eref;     // FP64 plans: its NL energy [1]
+  double* pw[2];    // FP64 plans: rho^a and rho^b of the current evaluation [N] each
   void* o[6];       // FP32 plane-pipeline plans: the combinations' spectra (plane-major)
 };
 
@@ -52,11 +53,17 @@ WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
   b += r256(sizeof(double) * kBlocks);
   W.vref = nullptr;
   W.eref = nullptr;
+  W.pw[0] = W.pw[1] = nullptr;
   for (int i = 0; i < 6; ++i) W.o[i] = nullptr;
   if (p->prec == GBOFDFT_F64) {
     W.vref = reinterpret_cast<double*>(b);
     b += r256(sizeof(double) * (size_t)p->N);
     W.eref = reinterpret_cast<double*>(b);
+    b += 256;
+    for (int i = 0; i < 2; ++i) {
+      W.pw[i] = reinterpret_cast<double*>(b);
+      b += r256(sizeof(double) * (size_t)p->N);
+    }
   } else if (wgc_plane(p)) {
     for (int i = 0; i < 6; ++i) { W.o[i] = b; b += sb; }
   }
@@ -69,7 +76,7 @@ WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
 size_t wgc_bytes(const gbofdft_plan* p) {
   size_t b = 6 * r256(gb_elem(p) * (size_t)p->N) + 6 * r256(2 * gb_elem(p) * (size_t)p->NGld) +
              r256(sizeof(double) * kBlocks);
-  if (p->prec == GBOFDFT_F64) b += r256(sizeof(double) * (size_t)p->N) + 256;
+  if (p->prec == GBOFDFT_F64) b += 3 * r256(sizeof(double) * (size_t)p->N) + 256;
   else if (wgc_plane(p)) b += 6 * r256(2 * gb_elem(p) * (size_t)p->NGld);
   return b;
 }
@@ -134,22 +141,37 @@ __global__ void k_wgc_kernels_pm(GInfo g, const float* __restrict__ K, float* __
 __device__ __forceinline__ float wpow(float x, float y) { return powf(x, y); }
 __device__ __forceinline__ double wpow(double x, double y) { return pow(x, y); }
 
-// transform inputs: F0 = B, F1 = u B, F2 = u^2 B (and A, u A, u^2 A)
+// A = rc^a and B = rc^b.  FP64: one logarithm and two exponentials instead
+// of two pow calls (the FP64 pipe of this part is slow and these powers
+// dominated the FP64 pointwise passes); exp(a ln rc) carries a relative error
+// of about |a ln rc| ulp, below 1e-14 for rc >= 1e-30.
+__device__ __forceinline__ void wpow2(float rc, float a, float b, int two, float& A, float& B) {
+  B = powf(rc, b);
+  A = two ? powf(rc, a) : B;
+}
+__device__ __forceinline__ void wpow2(double rc, double a, double b, int two, double& A, double& B) {
+  const double L = log(rc);
+  B = exp(b * L);
+  A = two ? exp(a * L) : B;
+}
+
+// transform inputs: F0 = B, F1 = u B, F2 = u^2 B (and A, u A, u^2 A); pa / pb
+// (optional) keep A and B for the final pass
 template <typename T>
 __global__ void k_wgc_prep(int64_t n, const T* __restrict__ rho, T rho0, T a, T b, int two, T* __restrict__ f0,
                            T* __restrict__ f1, T* __restrict__ f2, T* __restrict__ f3, T* __restrict__ f4,
-                           T* __restrict__ f5) {
+                           T* __restrict__ f5, T* __restrict__ pa, T* __restrict__ pb) {
   const T inv0 = (T)1 / rho0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const T rc = rho[i] > (T)kZeroRho ? rho[i] : (T)kZeroRho;
     const T u = (rc - rho0) * inv0;
-    const T B = wpow(rc, b);
+    T A, B;
+    wpow2(rc, a, b, two, A, B);
+    if (pa) { pa[i] = A; pb[i] = B; }
     f0[i] = B;
     f1[i] = u * B;
     f2[i] = u * u * B;
     if (two) {
-      const T A = wpow(rc, a);
-      f3[i] = A;
       f4[i] = u * A;
       f5[i] = u * u * A;
     }
@@ -183,20 +205,21 @@ __global__ void __launch_bounds__(kThreads) k_wgc_final(int64_t n, const T* __re
                                                          const T* __restrict__ x2, const T* __restrict__ y0,
                                                          const T* __restrict__ y1, const T* __restrict__ y2,
                                                          T* __restrict__ pot, int calc_v, double* __restrict__ part,
-                                                         T* __restrict__ vstore) {
+                                                         T* __restrict__ vstore, const T* __restrict__ pa,
+                                                         const T* __restrict__ pb) {
   const T inv0 = (T)1 / rho0;
   T es = (T)0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const T rc = rho[i] > (T)kZeroRho ? rho[i] : (T)kZeroRho;
     const T u = (rc - rho0) * inv0;
-    const T A = wpow(rc, a);
+    const T A = pa ? pa[i] : wpow(rc, a);
     const T X0 = x0[i], X1 = x1[i], X2 = x2[i];
     const T sx = X0 + u * X1 + u * u * X2;
     if (WANT_E) es += A * sx;
     if (calc_v) {
       T v;
       if (two) {
-        const T B = wpow(rc, b);
+        const T B = pb ? pb[i] : wpow(rc, b);
         const T Y0 = y0[i], Y1 = y1[i], Y2 = y2[i];
         v = a * A / rc * sx + A * inv0 * (X1 + (T)2 * u * X2) + b * B / rc * (Y0 + u * Y1 + u * u * Y2) +
             B * inv0 * (Y1 + (T)2 * u * Y2);
@@ -366,7 +389,8 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
     rc = wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st);
   } else {
     k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],
-                                                (T*)W.f[1], (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5]);
+                                                (T*)W.f[1], (T*)W.f[2], (T*)W.f[3], (T*)W.f[4], (T*)W.f[5],
+                                                (T*)W.pw[0], (T*)W.pw[1]);
     GB_CHECK_LAUNCH();
     gb_count_launch();
     rc = wgc_xfields<T>(p, W, two, d->kernels, st);
@@ -401,13 +425,13 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
                                                        (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
                                                        two ? (const T*)W.f[4] : nullptr,
                                                        two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part,
-                                                       vstore);
+                                                       vstore, (const T*)W.pw[0], (const T*)W.pw[1]);
   else
     k_wgc_final<T, false><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two,
                                                         (const T*)W.f[0], (const T*)W.f[1], (const T*)W.f[2], y,
                                                         two ? (const T*)W.f[4] : nullptr,
                                                         two ? (const T*)W.f[5] : nullptr, (T*)pot, calc_v, W.part,
-                                                        vstore);
+                                                        vstore, (const T*)W.pw[0], (const T*)W.pw[1]);
   GB_CHECK_LAUNCH();
   gb_count_launch();
   if (want_e) {

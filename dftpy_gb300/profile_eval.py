@@ -85,10 +85,8 @@ def main():
         # the superposed atomic densities: the k_F range (and the LMGP knot
         # count) of a real solve, not of a near-uniform noise field
         from .density import DensityGenerator
-        from .ions import Ions
         r_, a_ = systems.atomic_density_table(3.0, systems.ATOMIC_SIGMA["Al"])
-        ions = Ions(st.symbols, positions=st.positions, cell=st.lattice)
-        x = DensityGenerator(r={"Al": r_}, arho={"Al": a_}).guess_rho(ions, grid=grid).as_subclass(
+        x = DensityGenerator(r={"Al": r_}, arho={"Al": a_}).guess_rho(total.PSEUDO.ions, grid=grid).as_subclass(
             torch.Tensor).to(dt)
     rho = DirectField(grid, data=x)
     f = total.spec(rho).ctypes()

@@ -172,6 +172,7 @@ __global__ void k_wgc_prep(int64_t n, const T* __restrict__ rho, T rho0, T a, T 
     f1[i] = u * B;
     f2[i] = u * u * B;
     if (two) {
+      f3[i] = A;
       f4[i] = u * A;
       f5[i] = u * u * A;
     }

@@ -153,12 +153,34 @@ __global__ void __launch_bounds__(rows_threads_max<T, N>(), GB_CT_ROWS_MINB) k_c
   const bool b56 = a.b56 != 0;
   const T beta = sc<T>(a.beta);
   const T rho0 = sc<T>(a.rho0), inv0 = sc<T>(a.inv0);
+  // the three WGC inputs rho^e u^k (k = 0, 1, 2) of one exponent share the
+  // power: computed once per point (the same arithmetic as prologue_ct)
+  const bool wgc3 = a.nf == 3 && a.op[0] == OP_WGC0 && a.op[1] == OP_WGC1 && a.op[2] == OP_WGC2;
+  if (wgc3) {
+    for (int idx = tid; idx < RP * N; idx += blockDim.x) {
+      const int l2 = idx / N, j = idx % N;
+      const int64_t ra = base + 2 * l2;
+      T B[2] = {(T)0, (T)0}, u[2] = {(T)0, (T)0};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (ra + h < a.nrows) {
+          const T rho = R[(2 * l2 + h) * N + j];
+          const T rc = rho > (T)kZero ? rho : (T)kZero;
+          B[h] = pow_beta_ct<T>(rc, b56, beta);
+          u[h] = (rc - rho0) * inv0;
+        }
+      }
+      A[sw<T, NP>(0 * RP + l2, j)] = cpx<T>{B[0], B[1]};
+      A[sw<T, NP>(1 * RP + l2, j)] = cpx<T>{u[0] * B[0], u[1] * B[1]};
+      A[sw<T, NP>(2 * RP + l2, j)] = cpx<T>{u[0] * u[0] * B[0], u[1] * u[1] * B[1]};
+    }
+  }
   // fields in an unrolled outer loop: the field's prologue op is a
   // compile-time parameter index, and every index split below is by a
   // compile-time constant
 #pragma unroll
   for (int f = 0; f < GB_MAX_FIELDS; ++f) {
-    if (f >= a.nf) break;
+    if (wgc3 || f >= a.nf) break;
     const int op = a.op[f];
     for (int idx = tid; idx < RP * N; idx += blockDim.x) {
       const int l2 = idx / N, j = idx % N;

@@ -270,6 +270,10 @@ def test_fallback_to_uniform_when_the_network_is_worse(gn):
     bad = gn.LearnedGuess(bad_net)
     b = bad.guess(total, rho_u.grid)
     assert bad.last_choice == "uniform"
+    # a ratio below the network's own residual ratio rejects even the good guess
+    strict = gn.LearnedGuess(good.net, fallback_ratio=0.5 * r_net / r_uni)
+    strict.guess(total, rho_u.grid)
+    assert strict.last_choice == "uniform"
     assert torch.allclose(b.as_subclass(torch.Tensor), rho_u.as_subclass(torch.Tensor).to(b.dtype), rtol=1e-13,
                           atol=0.0)
 

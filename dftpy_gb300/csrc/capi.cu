@@ -94,6 +94,7 @@ int gbofdft_plan_destroy(gbofdft_plan* p) {
   if (p->partials) cudaFree(p->partials);
   if (p->scratch) cudaFree(p->scratch);
   if (p->wt_pm) cudaFree(p->wt_pm);
+  if (p->precond_pm) cudaFree(p->precond_pm);
   if (p->wgc_pm) cudaFree(p->wgc_pm);
   delete p;
   return GBOFDFT_OK;
@@ -214,6 +215,11 @@ int gbofdft_plan_create(const int nr[3], const double lattice[9], int precision,
   p->plane_ok = precision == GBOFDFT_F32 && gb_plane_supported_f32(nr[0], nr[1], nr[2]);
   p->plane = p->plane_ok && !(pe && pe[0] == '0');
   p->plane_variant = 0;
+  // GBOFDFT_PLANE_PRECOND=1: the TN preconditioner's convolutions through the
+  // plane pipeline too (one field: fills fewer SMs than the column passes, so
+  // it pays only when other streams run beside it)
+  const char* pp = getenv("GBOFDFT_PLANE_PRECOND");
+  p->plane_precond = p->plane && pp && pp[0] == '1';
   *out = p;
   return GBOFDFT_OK;
 }
@@ -284,6 +290,15 @@ int gbofdft_convolve(gbofdft_plan* p, const void* in, void* out, int kernel, con
   kd.type[0] = kernel;
   kd.arr[0] = karr;
   kd.coef[0] = coef;
+  if (p->plane_precond && kernel == GBOFDFT_KER_ARRAY && karr == p->precond_buf && p->precond_pm && gb_use_ct()) {
+    // the preconditioner: rows forward, one plane convolution, rows inverse
+    const float* pm_arr[GB_MAX_FIELDS] = {p->precond_pm, nullptr, nullptr, nullptr};
+    const int64_t fs = p->NG;
+    int rc = gb_ct_rows_fwd_pm_f32(p, in, p->spec, fs, 1, &op, 1.0, st);
+    if (!rc) rc = gb_plane_conv_f32(p, p->spec, fs, 1, &kd, pm_arr, 1.0 / (double)p->N, st);
+    if (!rc) rc = gb_ct_rows_inv_store_pm_f32(p, p->spec, fs, 1, out, 0, st);
+    if (rc != 1) return rc;
+  }
   int rc = gb_rows_fwd(p, in, p->spec, 0, p->ld2, 1, &op, 1.0, 1.0, st);
   if (!rc) rc = gb_cols(p, p->spec, 0, p->ld2, 1, 1, -1, 1.0, st);
   if (!rc) rc = gb_cols_conv(p, p->spec, 0, p->ld2, 1, kd, 1.0 / (double)p->N, st);

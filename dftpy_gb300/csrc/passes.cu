@@ -442,7 +442,7 @@ __global__ void k_wt_kernel(GInfo g, double tkf, double factor, double x, T* __r
 // the inverse of the kinetic (Lindhard) plus Hartree curvature of the
 // uniform electron gas; 0 at G = 0.
 template <typename T>
-__global__ void k_precond(GInfo g, double rho0, T* __restrict__ out) {
+__global__ void k_precond(GInfo g, double rho0, T* __restrict__ out, float* __restrict__ out_pm) {
   const double kf = cbrt(3.0 * kPi * kPi * rho0);
   const double ckin = 2.0 / 3.0 * kf * kf, tkf = 2.0 * kf, ch = 8.0 * kPi * rho0;
   const int64_t total = (int64_t)g.n0 * g.n1 * g.n2h;
@@ -455,6 +455,7 @@ __global__ void k_precond(GInfo g, double rho0, T* __restrict__ out) {
       return gg > 0.0 ? 1.0 / (ckin * lindhard_inv(sqrt(gg) / tkf, 0.0, 0.0) + ch / gg) : 0.0;
     });
     out[id] = (T)v;
+    if (out_pm) out_pm[(int64_t)k2 * g.n0 * g.n1 + r] = (float)v;
   }
 }
 
@@ -726,8 +727,18 @@ int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
   if (p->precond_buf == out && p->precond_rho0 == rho0) return 0;
   const int64_t total = p->NG;
   const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
-  if (p->prec == GBOFDFT_F64) k_precond<double><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<double*>(out));
-  else k_precond<float><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<float*>(out));
+  // plans that convolve with it on the plane pipeline keep a plane-major copy
+  if (p->plane_precond && p->plane_ok && !p->precond_pm) {
+    cudaError_t e = cudaMalloc(&p->precond_pm, sizeof(float) * (size_t)p->NG);
+    if (e != cudaSuccess) {
+      p->precond_pm = nullptr;
+      return gb_set_error(GBOFDFT_ERR_ALLOC, "preconditioner: plane-major copy: %s", cudaGetErrorString(e));
+    }
+  }
+  float* pm = p->plane_precond && p->plane_ok ? p->precond_pm : nullptr;
+  if (p->prec == GBOFDFT_F64)
+    k_precond<double><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<double*>(out), nullptr);
+  else k_precond<float><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<float*>(out), pm);
   GB_CHECK_LAUNCH();
   p->precond_buf = out;
   p->precond_rho0 = rho0;

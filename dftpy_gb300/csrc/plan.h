@@ -40,6 +40,8 @@ struct gbofdft_plan {
   const void* wgc_pm_src; // the kernels that copy belongs to
   const void* precond_buf;  // the buffer the last TN preconditioner was built into ...
   double precond_rho0;      // ... and its mean density (a rebuild is skipped when both match)
+  float* precond_pm;        // FP32 plane-pipeline plans: plane-major copy of that preconditioner
+  int plane_precond;        // 1: preconditioner convolutions through the plane pipeline
 };
 
 size_t gb_elem(const gbofdft_plan* p);  // bytes per real scalar

@@ -36,6 +36,9 @@ __host__ inline bool ct_dispatch(int n, F&& f) {
 #ifndef GB_CT_TB_F32
 #define GB_CT_TB_F32 16
 #endif
+#ifndef GB_CT_TB_F32_LARGE
+#define GB_CT_TB_F32_LARGE 8   // FP32 column tiles of lines longer than 256
+#endif
 #ifndef GB_CT_ROWS_MINB
 #define GB_CT_ROWS_MINB 1
 #endif
@@ -55,7 +58,7 @@ template <> struct RowsCfg<double> { static constexpr int RP = 4; };
 // threads of a row-pass CTA: TPL per line, one line per (field, row pair)
 template <typename T, int N> constexpr int rows_threads_max() { return Tpl<N>::value * RowsCfg<T>::RP * GB_MAX_FIELDS; }
 template <typename T, int N> struct ColsCfg {     // columns per tile
-  static constexpr int TB = (sizeof(T) == 4 && N <= 256) ? GB_CT_TB_F32 : 8;
+  static constexpr int TB = sizeof(T) == 4 ? (N <= 256 ? GB_CT_TB_F32 : GB_CT_TB_F32_LARGE) : 8;
 };
 // minimum resident CTAs per SM for the column passes (caps registers)
 template <typename T, int N, bool CONV> constexpr int cols_minb() {

@@ -11,6 +11,7 @@
 // interval weights) is regrouped by linearity into one forward transform per
 // knot of the accumulated weight field.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
@@ -221,7 +222,12 @@ __global__ void __launch_bounds__(gbct::Tpl<N>::value * gbct::ColsCfg<T, N>::TB)
 // compile-time specialisation (the caller then runs the separate kernels).
 template <typename T, int DIR>
 int lwt_cols(gbofdft_plan* p, const LwtColsArgs<T>& args, cudaStream_t st) {
-  if (!gb_use_ct()) return 1;
+  // GBOFDFT_LWT_FUSED=0: the separate kernel-multiply / accumulation kernels
+  static const bool off = [] {
+    const char* e = getenv("GBOFDFT_LWT_FUSED");
+    return e && e[0] == '0';
+  }();
+  if (off || !gb_use_ct()) return 1;
   int rc = 1;
   gbct::ct_dispatch(p->n[0], [&](auto ncst) {
     constexpr int N = decltype(ncst)::value;

@@ -24,8 +24,12 @@ def _bf16_round(a):
     return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).to(torch.float64).numpy()
 
 
-@pytest.mark.parametrize("shape,cin,cout", [((4, 6, 8), 3, 37), ((8, 8, 8), 16, 32), ((2, 4, 2), 5, 1)])
+@pytest.mark.parametrize("shape,cin,cout", [((4, 6, 8), 3, 37), ((8, 8, 8), 16, 32), ((2, 4, 2), 5, 1),
+                                             ((16, 32, 160), 3, 37)])
 def test_conv_kernels(gn, shape, cin, cout):
+    """The CUDA-core convolution against the oracle: small grids run one thread
+    per (voxel, channel) (``k_conv3d_vc``), the 81920-voxel grid the voxel-tile
+    kernel (``k_conv3d``); both sum in the same order."""
     import torch
     rng = np.random.default_rng(2)
     layer = gn.Conv(cin, cout, rng)

@@ -290,7 +290,7 @@ int gbofdft_convolve(gbofdft_plan* p, const void* in, void* out, int kernel, con
   kd.type[0] = kernel;
   kd.arr[0] = karr;
   kd.coef[0] = coef;
-  if (p->plane_precond && kernel == GBOFDFT_KER_ARRAY && karr == p->precond_buf && p->precond_pm && gb_use_ct()) {
+  if (p->plane_precond && kernel == GBOFDFT_KER_ARRAY && karr == p->precond_pm_src && p->precond_pm && gb_use_ct()) {
     // the preconditioner: rows forward, one plane convolution, rows inverse
     const float* pm_arr[GB_MAX_FIELDS] = {p->precond_pm, nullptr, nullptr, nullptr};
     const int64_t fs = p->NG;

@@ -88,9 +88,10 @@ __global__ void __launch_bounds__(kVox) k_conv3d(const float* __restrict__ in, i
 // The same convolution for grids too small to fill the GPU with k_conv3d's
 // (256 voxels x 32 channels) CTAs -- the network's coarsest levels, a few
 // hundred voxels with 64-128 channels: one thread per (output voxel, output
-// channel), consecutive threads on consecutive channels of one voxel (its
-// inputs are shared).  Each output is summed over ci, then taps, in the order
-// of k_conv3d, so both give the same values.
+// channel), consecutive threads on consecutive voxels of one channel (the
+// warp's weight loads are one broadcast, its input loads contiguous).  Each
+// output is summed over ci, then taps, in the order of k_conv3d, so both give
+// the same values.
 constexpr int kVcThreads = 256;
 
 __global__ void __launch_bounds__(kVcThreads) k_conv3d_vc(const float* __restrict__ in, int cin,
@@ -101,8 +102,8 @@ __global__ void __launch_bounds__(kVcThreads) k_conv3d_vc(const float* __restric
   const int64_t N = (int64_t)D * HW;
   const int64_t id = (int64_t)blockIdx.x * kVcThreads + threadIdx.x;
   if (id >= N * cout) return;
-  const int co = (int)(id % cout);
-  const int64_t v = id / cout;
+  const int64_t v = id % N;
+  const int co = (int)(id / N);
   const int z = (int)(v / HW), r = (int)(v % HW);
   const int y = r / W, x = r % W;
   const int oz[3] = {((z + D - 1) % D) * HW, z * HW, ((z + 1) % D) * HW};
@@ -357,7 +358,7 @@ int gbofdft_nn_conv3d(const float* in, int cin, const void* w_bf16, const float*
   const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(w_bf16);
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t tiles = cout <= 16 ? 1 : (cout + 31) / 32;
-  if ((int64_t)nv * tiles < 2 * 152 && N * cout <= (int64_t)INT32_MAX) {
+  if ((int64_t)nv * tiles < 76 && N * cout <= (int64_t)INT32_MAX) {
     // too few k_conv3d CTAs for the GPU: one thread per (voxel, channel)
     const unsigned nb = (unsigned)((N * cout + kVcThreads - 1) / kVcThreads);
     k_conv3d_vc<<<nb, kVcThreads, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);

@@ -11,14 +11,12 @@
 // interval weights) is regrouped by linearity into one forward transform per
 // knot of the accumulated weight field.
 #include <math.h>
-#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
 #include <vector>
 
 #include "gkernels.cuh"
-#include "passes_ct.cuh"
 #include "plan.h"
 
 double kf_of_host(double rho);
@@ -138,109 +136,6 @@ __global__ void k_lwt_acc(GInfo g, BG<T> bg, const cpx<T>* __restrict__ U, int64
     if (first) acc[o] = cpx<T>{ax, ay};
     else acc[o] = cpx<T>{acc[o].x + ax, acc[o].y + ay};
   }
-}
-
-// Axis-0 column pass of a knot's transforms with the kernel multiply fused in
-// (compile-time length N and the tile of gbct::k_ct_cols: TB columns k2 of one
-// i1, the whole i0 line of each in shared memory):
-//   DIR = +1: dst[f] = the axis-0 inverse pass of K_f(q / kf) S / N (f = 0 the
-//             kernel table, f = 1 the derivative table over kf): k_lwt_kmul
-//             and the first pass of the inverse transform in one;
-//   DIR = -1: dst (+)= sum_f K_f(q / kf) / N times the axis-0 forward pass of
-//             U_f: the last pass of the forward transform and k_lwt_acc in one.
-// Same arithmetic, in the same order, as the separate kernels.
-template <typename T>
-struct LwtColsArgs {
-  const cpx<T>* src;   // S (DIR +1) or the U_f (DIR -1), layout ld2
-  int64_t sfs;         // field stride of the U_f (complex elements)
-  cpx<T>* dst;         // DIR +1: the knot's spectra; DIR -1: the accumulator
-  int64_t dfs;         // field stride of dst (DIR +1)
-  int nf, first, ld2, ncols;
-  int64_t stride;      // n1 * ld2: one step along axis 0
-  const cpx<T>* tw;
-  GInfo gi;
-  BG<T> bg;
-  UTable<T> tk, td;
-  T inv_kf, kf, scale;
-};
-
-template <typename T>
-__device__ __forceinline__ T lwt_kcoef(const LwtColsArgs<T>& a, int f, int i0, int i1, int k2) {
-  if (i0 == 0 && i1 == 0 && k2 == 0) return (T)0;
-  T kv = lwt_kval<T>(a.gi, a.bg, f == 0 ? a.tk : a.td, a.inv_kf, i0, i1, k2);
-  if (f == 1) kv /= a.kf;
-  return kv * a.scale;
-}
-
-template <typename T, int N, int DIR>
-__global__ void __launch_bounds__(gbct::Tpl<N>::value * gbct::ColsCfg<T, N>::TB) k_lwt_cols(LwtColsArgs<T> a) {
-  constexpr int TB = gbct::ColsCfg<T, N>::TB, TPL = gbct::Tpl<N>::value, NP = gbct::Pad<T, N>::NP;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cpx<T>* tw = reinterpret_cast<cpx<T>*>(smem_raw);
-  cpx<T>* A = tw + N;
-  cpx<T>* B = A + TB * NP;
-  const int tid = threadIdx.x, l = tid / TPL, lane = tid % TPL;
-  for (int i = tid; i < N; i += blockDim.x) tw[i] = a.tw[i];
-  const int c0 = blockIdx.x * TB;
-  const int nc = min(TB, a.ncols - c0);
-  const int outer = blockIdx.y;
-  const int64_t base = (int64_t)outer * a.ld2 + c0;
-  for (int f = 0; f < a.nf; ++f) {
-    const cpx<T>* src = a.src + (DIR > 0 ? 0 : f * a.sfs) + base;
-    __syncthreads();   // the previous field's results are read
-    for (int idx = tid; idx < N * TB; idx += blockDim.x) {
-      const int c = idx % TB, j = idx / TB;
-      cpx<T> v = {(T)0, (T)0};
-      if (c < nc) {
-        v = src[(int64_t)j * a.stride + c];
-        if (DIR > 0) {
-          const T kv = lwt_kcoef(a, f, j, outer, c0 + c);
-          v = cpx<T>{v.x * kv, v.y * kv};
-        }
-      }
-      A[gbct::sw<T, NP>(c, j)] = v;
-    }
-    __syncthreads();
-    cpx<T>* res = gbct::fft<DIR, T, N>(A, B, tw, l, lane, true);
-    for (int idx = tid; idx < N * TB; idx += blockDim.x) {
-      const int c = idx % TB, j = idx / TB;
-      if (c >= nc) continue;
-      const cpx<T> z = res[gbct::sw<T, NP>(c, j)];
-      const int64_t o = base + (int64_t)j * a.stride + c;
-      if (DIR > 0) {
-        a.dst[f * a.dfs + o] = z;
-      } else {
-        const T kv = lwt_kcoef(a, f, j, outer, c0 + c);
-        const cpx<T> acc = (a.first && f == 0) ? cpx<T>{(T)0, (T)0} : a.dst[o];
-        a.dst[o] = cpx<T>{acc.x + kv * z.x, acc.y + kv * z.y};
-      }
-    }
-  }
-}
-
-// Launch k_lwt_cols for the plan's axis-0 length; 1 when that length has no
-// compile-time specialisation (the caller then runs the separate kernels).
-template <typename T, int DIR>
-int lwt_cols(gbofdft_plan* p, const LwtColsArgs<T>& args, cudaStream_t st) {
-  // GBOFDFT_LWT_FUSED=0: the separate kernel-multiply / accumulation kernels
-  static const bool off = [] {
-    const char* e = getenv("GBOFDFT_LWT_FUSED");
-    return e && e[0] == '0';
-  }();
-  if (off || !gb_use_ct()) return 1;
-  int rc = 1;
-  gbct::ct_dispatch(p->n[0], [&](auto ncst) {
-    constexpr int N = decltype(ncst)::value;
-    constexpr int TB = gbct::ColsCfg<T, N>::TB, NP = gbct::Pad<T, N>::NP;
-    const size_t sm = sizeof(cpx<T>) * (N + 2 * TB * NP);
-    if ((rc = gbct::ct_smem(k_lwt_cols<T, N, DIR>, sm))) return;
-    dim3 grid((p->n2h + TB - 1) / TB, p->n[1]);
-    k_lwt_cols<T, N, DIR><<<grid, gbct::Tpl<N>::value * TB, sm, st>>>(args);
-    gb_count_launch();
-    cudaError_t e = cudaGetLastError();
-    rc = e == cudaSuccess ? 0 : gb_set_error(GBOFDFT_ERR_CUDA, "lwt cols: %s", cudaGetErrorString(e));
-  });
-  return rc;
 }
 
 __device__ __forceinline__ double kf_of(double rho) { return 2.0 * cbrt(3.0 * 9.86960440108935861883 * rho); }
@@ -620,39 +515,10 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   const int nwf = hermite ? 2 : 1;
   int cur = 0;
   const int64_t ofs = (int64_t)(fb / gb_elem(p));   // p[c] -> m[c], in elements
-  auto cols_args = [&](double kf) {
-    LwtColsArgs<T> a;
-    memset(&a, 0, sizeof(a));
-    a.ld2 = p->ld2;
-    a.ncols = p->n2h;
-    a.stride = (int64_t)p->n[1] * p->ld2;
-    a.tw = reinterpret_cast<const cpx<T>*>(p->tw[0]);
-    a.gi = p->gi;
-    a.bg = bg;
-    a.tk = tk;
-    a.td = td;
-    a.inv_kf = (T)(1.0 / kf);
-    a.kf = (T)kf;
-    a.scale = (T)invN;
-    return a;
-  };
-  // weights of knot kk complete: G (+)= K_kk fft(w) (+ D_kk fft(wd)); the
-  // last forward pass carries the kernel multiply and the accumulation
+  // weights of knot kk complete: G (+)= K_kk fft(w) (+ D_kk fft(wd))
   auto accumulate = [&](int kk, const void* w, const void* wd, int first) -> int {
-    const int op = OP_RHO;
-    int r2 = gb_rows_fwd(p, w, L.U, 0, p->ld2, 1, &op, 1.0, 1.0, st);
-    if (!r2 && hermite) r2 = gb_rows_fwd(p, wd, (char*)L.U + sb, 0, p->ld2, 1, &op, 1.0, 1.0, st);
-    if (!r2) r2 = gb_cols(p, L.U, sfs, p->ld2, nwf, 1, -1, 1.0, st);
-    if (r2) return r2;
-    LwtColsArgs<T> ca = cols_args(kfl[kk]);
-    ca.src = reinterpret_cast<const cpx<T>*>(L.U);
-    ca.sfs = sfs;
-    ca.dst = reinterpret_cast<cpx<T>*>(L.G);
-    ca.nf = nwf;
-    ca.first = first;
-    r2 = lwt_cols<T, -1>(p, ca, st);
-    if (r2 != 1) return r2;
-    r2 = gb_cols(p, L.U, sfs, p->ld2, nwf, 0, -1, 1.0, st);
+    int r2 = fwd3d(p, w, L.U, OP_RHO, 1.0, st);
+    if (!r2 && hermite) r2 = fwd3d(p, wd, (char*)L.U + sb, OP_RHO, 1.0, st);
     if (r2) return r2;
     k_lwt_acc<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.U, sfs, nwf, tk, td, kfl[kk], invN,
                                                     (cpx<T>*)L.G, first);
@@ -661,22 +527,11 @@ int lwt_run(gbofdft_plan* p, const void* rho, gbofdft_lwt* d, void* pot, double*
   };
   for (int k = 0; k < nsp; ++k) {
     // p[cur] (and m[cur], the next field): the knot's kernels times the shared
-    // spectrum, inverse-transformed (multiply fused into the first pass)
-    LwtColsArgs<T> ca = cols_args(kfl[k]);
-    ca.src = reinterpret_cast<const cpx<T>*>(L.S);
-    ca.dst = reinterpret_cast<cpx<T>*>(L.T);
-    ca.dfs = sfs;
-    ca.nf = nkf;
-    rc = lwt_cols<T, 1>(p, ca, st);
-    if (rc == 1) {
-      k_lwt_kmul<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs,
-                                                       nkf, tk, td, kfl[k], invN);
-      GB_CHECK_LAUNCH();
-      rc = gb_cols(p, L.T, sfs, p->ld2, nkf, 0, 1, 1.0, st);
-    }
-    if (!rc) rc = gb_cols(p, L.T, sfs, p->ld2, nkf, 1, 1, 1.0, st);
-    if (!rc) rc = gb_rows_inv_store(p, L.T, sfs, p->ld2, nkf, L.p[cur], ofs, 1.0, st);
-    if (rc) return rc;
+    // spectrum, inverse-transformed in one launch sequence
+    k_lwt_kmul<T><<<rl.blocks, rl.threads, 0, st>>>(p->gi, bg, (const cpx<T>*)L.S, p->ld2, (cpx<T>*)L.T, sfs, nkf,
+                                                     tk, td, kfl[k], invN);
+    GB_CHECK_LAUNCH();
+    if ((rc = inv3d(p, L.T, sfs, nkf, L.p[cur], ofs, st))) return rc;
     if (k >= 1) {
       const int prv = cur ^ 1;
       IntervalArgs a;

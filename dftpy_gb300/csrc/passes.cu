@@ -724,7 +724,8 @@ int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
   // the optimiser's workspace keeps it between solves of the same grid: the
   // table depends on the grid and the mean density only (stream order makes
   // the earlier build complete before any later reader on the plan's stream)
-  if (p->precond_buf == out && p->precond_rho0 == rho0) return 0;
+  for (int i = 0; i < 2; ++i)
+    if (p->precond_buf[i] == out && p->precond_rho0[i] == rho0) return 0;
   const int64_t total = p->NG;
   const int nblk = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
   // plans that convolve with it on the plane pipeline keep a plane-major copy
@@ -740,8 +741,11 @@ int gb_build_precond(gbofdft_plan* p, double rho0, void* out, cudaStream_t st) {
     k_precond<double><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<double*>(out), nullptr);
   else k_precond<float><<<nblk, 256, 0, st>>>(p->gi, rho0, reinterpret_cast<float*>(out), pm);
   GB_CHECK_LAUNCH();
-  p->precond_buf = out;
-  p->precond_rho0 = rho0;
+  const int slot = p->precond_next;
+  p->precond_next ^= 1;
+  p->precond_buf[slot] = out;
+  p->precond_rho0[slot] = rho0;
+  if (pm) p->precond_pm_src = out;
   return 0;
 }
 

@@ -38,9 +38,14 @@ struct gbofdft_plan {
   const void* wt_pm_src; // the table that copy belongs to
   float* wgc_pm;         // plane-major copy of the last WGC kernels (4 x NG) built on this plan
   const void* wgc_pm_src; // the kernels that copy belongs to
-  const void* precond_buf;  // the buffer the last TN preconditioner was built into ...
-  double precond_rho0;      // ... and its mean density (a rebuild is skipped when both match)
-  float* precond_pm;        // FP32 plane-pipeline plans: plane-major copy of that preconditioner
+  // the buffers the last two TN preconditioners were built into and their
+  // mean densities (a rebuild is skipped when both match): the FP32 stage
+  // and the refinement's Hessian products keep one each on the same plan
+  const void* precond_buf[2];
+  double precond_rho0[2];
+  int precond_next;         // slot the next build replaces
+  float* precond_pm;        // FP32 plane-pipeline plans: plane-major copy of one preconditioner ...
+  const void* precond_pm_src;  // ... the one built into this buffer
   int plane_precond;        // 1: preconditioner convolutions through the plane pipeline
 };
 

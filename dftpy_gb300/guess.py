@@ -471,10 +471,14 @@ def residual(total, rho):
     from .field import DirectField
     grid = rho.grid
     x = DirectField(grid, data=rho.as_subclass(torch.Tensor).to(torch.float32))
-    v = total(x, calcType={"V"}).potential.as_subclass(torch.Tensor).to(torch.float64)
-    r = x.as_subclass(torch.Tensor).to(torch.float64)
-    mu = (v * r).sum() / r.sum()
-    return float(torch.sqrt(((v - mu) ** 2 * r.clamp(min=0.0)).sum() * grid.dV))
+    v = total(x, calcType={"V"}).potential.as_subclass(torch.Tensor).reshape(-1).to(torch.float64)
+    r = x.as_subclass(torch.Tensor).reshape(-1).clamp(min=0.0).to(torch.float64)
+    # one pass of sums: int r, int V r, int V^2 r; then
+    # int (V - mu)^2 r = int V^2 r - mu int V r
+    vr = v * r
+    s0, s1, s2 = (float(t) for t in torch.stack([r.sum(), vr.sum(), (vr * v).sum()]).tolist())
+    mu = s1 / s0
+    return math.sqrt(max(s2 - mu * s1, 0.0) * grid.dV)
 
 
 def uniform_residual(total, grid):

@@ -302,6 +302,7 @@ struct CtRowsInvWgc {
   float rho0, inv0, ea, eb;
   int two;
   float* pot;
+  double* part;         // non-null: per-CTA partial sums of int A (X0 + u X1 + u^2 X2)
 };
 
 template <int N>
@@ -318,6 +319,7 @@ __global__ void __launch_bounds__(Tpl<N>::value * RowsCfg<float>::RP * 6) k_ct_r
   for (int i = tid; i < N; i += blockDim.x) tw[i] = twg[i];
   cpx<float>* res = ct_rows_inv_lines<float, N, true, 6>(a.r, base, tw, A, B);
   const int gy = a.two ? 3 : 0;
+  float es = 0.0f;   // per-thread energy sum (a handful of points), FP64 above
   for (int idx = tid; idx < 2 * RP * N; idx += blockDim.x) {
     const int rr = idx / N, j = idx % N;
     const int64_t row = base + rr;
@@ -335,6 +337,7 @@ __global__ void __launch_bounds__(Tpl<N>::value * RowsCfg<float>::RP * 6) k_ct_r
     const float u = (rc - a.rho0) * a.inv0;
     const float Aa = powf(rc, a.ea);
     const float sx = X0 + u * X1 + u * u * X2;
+    es += Aa * sx;
     float v;
     if (a.two) {
       const float Bb = powf(rc, a.eb);
@@ -344,6 +347,18 @@ __global__ void __launch_bounds__(Tpl<N>::value * RowsCfg<float>::RP * 6) k_ct_r
       v = 2.0f * (a.ea * Aa / rc * sx + Aa * a.inv0 * (X1 + 2.0f * u * X2));
     }
     a.pot[g] += v;
+  }
+  if (!a.part) return;
+  __shared__ double red[32];
+  const int lane32 = tid & 31, warp = tid >> 5;
+  const double wsum = warp_sum((double)es);
+  if (lane32 == 0) red[warp] = wsum;
+  __syncthreads();
+  if (tid == 0) {
+    KSum t;
+    t.init();
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) t.add(red[w]);
+    a.part[blockIdx.x] = t.value();
   }
 }
 
@@ -742,7 +757,7 @@ int ct_rows_inv(gbofdft_plan* p, const void* spec, int64_t fstride, int ld2, int
 }
 
 inline int ct_rows_inv_wgc(gbofdft_plan* p, const void* spec, int64_t fstride, int two, const float* rho, double rho0,
-                           double ea, double eb, float* pot, cudaStream_t st) {
+                           double ea, double eb, float* pot, double* part, int64_t* nblk_out, cudaStream_t st) {
   int rc = 1;
   ct_dispatch(p->n[2], [&](auto nc) {
     constexpr int N = decltype(nc)::value;
@@ -752,8 +767,9 @@ inline int ct_rows_inv_wgc(gbofdft_plan* p, const void* spec, int64_t fstride, i
     a.r.in = spec; a.r.fstride = fstride; a.r.nrows = p->n[0] * p->n[1]; a.r.ld2 = 0; a.r.nf = two ? 6 : 3;
     a.r.tw = p->tw[2];
     a.rho = rho; a.rho0 = (float)rho0; a.inv0 = (float)(1.0 / rho0); a.ea = (float)ea; a.eb = (float)eb;
-    a.two = two; a.pot = pot;
+    a.two = two; a.pot = pot; a.part = part;
     const int nblk = (a.r.nrows + 2 * RP - 1) / (2 * RP);
+    if (nblk_out) *nblk_out = nblk;
     const size_t sm = sizeof(cpx<float>) * (N + 2 * (size_t)a.r.nf * RP * NP);
     if ((rc = ct_smem(k_ct_rows_inv_wgc<N>, sm))) return;
     k_ct_rows_inv_wgc<N><<<nblk, Tpl<N>::value * RP * a.r.nf, sm, st>>>(a);
@@ -940,8 +956,9 @@ inline int plane_wgc_inv_f32(gbofdft_plan* p, const void* spec, int64_t fstride,
                                           nullptr, nullptr, 0, nullptr, nullptr, st);                          \
   }                                                                                                            \
   int gb_ct_rows_inv_wgc_pm_f32(gbofdft_plan* p, const void* spec, int64_t fstride, int two, const float* rho,   \
-                                double rho0, double ea, double eb, float* pot, cudaStream_t st) {             \
-    return gbct::ct_rows_inv_wgc(p, spec, fstride, two, rho, rho0, ea, eb, pot, st);                          \
+                                double rho0, double ea, double eb, float* pot, double* part, int64_t* nblk,     \
+                                cudaStream_t st) {                                                            \
+    return gbct::ct_rows_inv_wgc(p, spec, fstride, two, rho, rho0, ea, eb, pot, part, nblk, st);              \
   }                                                                                                            \
   int gb_plane_fwd_f32(gbofdft_plan* p, void* spec, int64_t fstride, int nf, cudaStream_t st) {                \
     return gbct::plane_fwd_f32(p, spec, fstride, nf, st);                                                      \

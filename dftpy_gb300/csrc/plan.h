@@ -116,9 +116,10 @@ int gb_plane_wgc_inv_f32(gbofdft_plan*, const void* spec, int64_t fstride, void*
 int gb_ct_rows_inv_store_pm_f32(gbofdft_plan*, const void* spec, int64_t fstride, int nf, void* out, int64_t ostride,
                                 cudaStream_t);
 // the inverse rows of the six (three when a == b) combined WGC spectra with
-// the NL potential added to pot (potential-only FP32 evaluations)
+// the NL potential added to pot (FP32 evaluations); part non-null: per-CTA
+// partial sums of the NL energy integrand, *nblk of them
 int gb_ct_rows_inv_wgc_pm_f32(gbofdft_plan*, const void* spec, int64_t fstride, int two, const float* rho, double rho0,
-                              double ea, double eb, float* pot, cudaStream_t);
+                              double ea, double eb, float* pot, double* part, int64_t* nblk, cudaStream_t);
 int gb_plane_variants_f32(int n0, int n1);
 // the plane-major evaluation (returns 1 when the plan has no plane pipeline
 // or a kernel table has no plane-major copy)

@@ -43,6 +43,13 @@ bool wgc_plane(const gbofdft_plan* p) { return p->prec == GBOFDFT_F32 && p->plan
 constexpr int kBlocks = 1216;
 constexpr int kThreads = 256;
 
+// per-CTA energy partials: the grid-stride passes use kBlocks, the fused
+// inverse row pass of the plane pipeline one per pair of rows at most
+int64_t wgc_part_count(const gbofdft_plan* p) {
+  const int64_t rows = (int64_t)p->n[0] * p->n[1] / 2 + 1;
+  return rows > kBlocks ? rows : kBlocks;
+}
+
 WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
   const size_t fb = r256(gb_elem(p) * (size_t)p->N), sb = r256(2 * gb_elem(p) * (size_t)p->NGld);
   char* b = reinterpret_cast<char*>(work);
@@ -50,7 +57,7 @@ WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
   for (int i = 0; i < 6; ++i) { W.f[i] = b; b += fb; }
   for (int i = 0; i < 6; ++i) { W.s[i] = b; b += sb; }
   W.part = reinterpret_cast<double*>(b);
-  b += r256(sizeof(double) * kBlocks);
+  b += r256(sizeof(double) * (size_t)wgc_part_count(p));
   W.vref = nullptr;
   W.eref = nullptr;
   W.pw[0] = W.pw[1] = nullptr;
@@ -75,7 +82,7 @@ WgcBufs wgc_layout(const gbofdft_plan* p, void* work) {
 // (in f[0..5]), its NL potential and energy
 size_t wgc_bytes(const gbofdft_plan* p) {
   size_t b = 6 * r256(gb_elem(p) * (size_t)p->N) + 6 * r256(2 * gb_elem(p) * (size_t)p->NGld) +
-             r256(sizeof(double) * kBlocks);
+             r256(sizeof(double) * (size_t)wgc_part_count(p));
   if (p->prec == GBOFDFT_F64) b += 3 * r256(sizeof(double) * (size_t)p->N) + 256;
   else if (wgc_plane(p)) b += 6 * r256(2 * gb_elem(p) * (size_t)p->NGld);
   return b;
@@ -318,7 +325,8 @@ __global__ void k_wgc_energy(const double* __restrict__ part, int nb, double dV,
 // (potential-only evaluations): the inverse row pass adds the NL potential
 // to pot directly instead of storing the fields.
 int wgc_xfields_plane(gbofdft_plan* p, const WgcBufs& W, int two, const float* K, const float* rho,
-                      const gbofdft_wgc* d, cudaStream_t st, float* pot = nullptr) {
+                      const gbofdft_wgc* d, cudaStream_t st, float* pot = nullptr, double* part = nullptr,
+                      int64_t* nblk = nullptr) {
   const int nfield = two ? 6 : 3;
   const int64_t fs = (int64_t)((char*)W.s[1] - (char*)W.s[0]) / (int64_t)sizeof(float2);
   const int64_t os = (int64_t)((char*)W.o[1] - (char*)W.o[0]) / (int64_t)sizeof(float2);
@@ -334,7 +342,7 @@ int wgc_xfields_plane(gbofdft_plan* p, const WgcBufs& W, int two, const float* K
   if (!rc) rc = gb_plane_fwd_f32(p, W.s[0], fs, nfield, st);
   if (!rc) rc = gb_plane_wgc_inv_f32(p, W.s[0], fs, W.o[0], os, two ? 2 : 1, K, 1.0 / (double)p->N, st);
   if (!rc && pot && rho) {
-    rc = gb_ct_rows_inv_wgc_pm_f32(p, W.o[0], os, two, rho, d->rho0, d->alpha, d->beta, pot, st);
+    rc = gb_ct_rows_inv_wgc_pm_f32(p, W.o[0], os, two, rho, d->rho0, d->alpha, d->beta, pot, part, nblk, st);
     if (rc == 1) return gb_set_error(GBOFDFT_ERR_STATE, "wgc: plane size without specialisation");
     return rc;
   }
@@ -383,10 +391,19 @@ int wgc_run(gbofdft_plan* p, const void* rho, const gbofdft_wgc* d, void* pot, d
   const T* r = reinterpret_cast<const T*>(rho);
   int rc;
   if (wgc_plane(p) && p->wgc_pm && p->wgc_pm_src == d->kernels) {
-    if (!calc_e && calc_v && !store_ref)
-      // potential only: the inverse rows add the potential themselves
-      return wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st,
-                               reinterpret_cast<float*>(pot));
+    if (calc_v && !store_ref) {
+      // the inverse rows add the potential themselves (and sum the energy
+      // integrand per CTA) instead of storing the six fields
+      int64_t nblk = 0;
+      rc = wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st,
+                             reinterpret_cast<float*>(pot), calc_e ? W.part : nullptr, &nblk);
+      if (rc || !calc_e) return rc;
+      if (nblk > wgc_part_count(p)) return gb_set_error(GBOFDFT_ERR_STATE, "wgc: partials buffer too small");
+      k_wgc_energy<<<1, 256, 0, st>>>(W.part, (int)nblk, p->dV, energies, nullptr, nullptr);
+      GB_CHECK_LAUNCH();
+      gb_count_launch();
+      return 0;
+    }
     rc = wgc_xfields_plane(p, W, two, p->wgc_pm, reinterpret_cast<const float*>(rho), d, st);
   } else {
     k_wgc_prep<T><<<kBlocks, kThreads, 0, st>>>(p->N, r, (T)d->rho0, (T)d->alpha, (T)d->beta, two, (T*)W.f[0],

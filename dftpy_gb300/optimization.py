@@ -47,6 +47,9 @@ DEFAULTS = {
     "fp32_eps": -1.0e-3,
     "refine_maxls": 10,
     "refine": "split",
+    # refinements that end in a line-search failure while the energy still
+    # moved by more than econv are started again from their last density
+    "refine_restarts": 1,
     "refine_pred_stop": None,
     # relative energy resolution of the evaluations, for the line-search
     # acceptance on the derivative (mixed precision only): the PZ81 LDA is
@@ -220,18 +223,32 @@ class Optimization:
             n_in = float(rho.as_subclass(torch.Tensor).to(torch.float64).sum())
             n_out = float(r64.as_subclass(torch.Tensor).sum())
             r64 = r64 * (n_in / n_out)
-            if o["refine"] == "split":
-                ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.01 * o["econv"]
-                r, out = self._run(r64, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
-                                   hess_rho=r32, pred_stop=ps, eres=o["refine_eres"], ncheck=o["refine_ncheck"],
-                                   cg_rtol=o["refine_cg_rtol"], pred_next=True, precond=o["mixed_precond"],
-                                   c2=o["refine_c2"], delta=o["refine_delta"])
-            elif o["refine"] == "fp64":
-                r, out = self._run(r64, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
-                                   eres=o["refine_eres"])
-            else:
+            if o["refine"] not in ("split", "fp64"):
                 raise ValueError("refine must be 'split' or 'fp64', got %r" % (o["refine"],))
+
+            def refine(r_start, r_hess):
+                if o["refine"] == "split":
+                    ps = o["refine_pred_stop"] if o["refine_pred_stop"] is not None else 0.01 * o["econv"]
+                    return self._run(r_start, o["econv"], o["fp32_eps"], o["maxiter"], maxls=o["refine_maxls"],
+                                     hess_rho=r_hess, pred_stop=ps, eres=o["refine_eres"],
+                                     ncheck=o["refine_ncheck"], cg_rtol=o["refine_cg_rtol"], pred_next=True,
+                                     precond=o["mixed_precond"], c2=o["refine_c2"], delta=o["refine_delta"])
+                return self._run(r_start, o["econv"], eps, o["maxiter"], maxls=o["refine_maxls"],
+                                 eres=o["refine_eres"])
+
+            r, out = refine(r64, r32)
             self.stats["stages"].append(dict(precision="fp64", **out))
+            # a refinement whose line search failed while it was still lowering
+            # the energy by more than econv starts again from where it stopped
+            # (once by default): functionals whose form moves with the density
+            # -- the LMGP k_F range only widens -- can make a line search fail
+            # far from the minimum, and a fresh start sees the settled form
+            for _ in range(int(o["refine_restarts"])):
+                h = out["history"]
+                if not (out["converged"] == 1 and len(h) >= 2 and abs(h[-1] - h[0]) > o["econv"]):
+                    break
+                r, out = refine(r, r.to(torch.float32))
+                self.stats["stages"].append(dict(precision="fp64", restart=True, **out))
             # a refinement whose line search stops on FP64 rounding (no energy
             # change above econv along the last direction) sits at the FP64
             # minimum: report it converged

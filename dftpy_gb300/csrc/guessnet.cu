@@ -87,40 +87,50 @@ __global__ void __launch_bounds__(kVox) k_conv3d(const float* __restrict__ in, i
 
 // The same convolution for grids too small to fill the GPU with k_conv3d's
 // (256 voxels x 32 channels) CTAs -- the network's coarsest levels, a few
-// hundred voxels with 64-128 channels: one thread per (output voxel, output
-// channel), consecutive threads on consecutive voxels of one channel (the
-// warp's weight loads are one broadcast, its input loads contiguous).  Each
-// output is summed over ci, then taps, in the order of k_conv3d, so both give
-// the same values.
-constexpr int kVcThreads = 256;
+// hundred voxels with 64-128 channels.  One CTA per (output channel, 64
+// voxels); its 256 threads are 64 voxels x 4 groups of input channels (the
+// warp's weight loads are one broadcast, its input loads contiguous), and the
+// four groups' sums are added in a fixed order (deterministic).
+constexpr int kKsVox = 64, kKsGroups = 4;
 
-__global__ void __launch_bounds__(kVcThreads) k_conv3d_vc(const float* __restrict__ in, int cin,
-                                                           const __nv_bfloat16* __restrict__ w,
-                                                           const float* __restrict__ bias, float* __restrict__ out,
-                                                           int cout, int D, int H, int W, int transposed) {
+__global__ void __launch_bounds__(kKsVox * kKsGroups) k_conv3d_ks(const float* __restrict__ in, int cin,
+                                                                  const __nv_bfloat16* __restrict__ w,
+                                                                  const float* __restrict__ bias,
+                                                                  float* __restrict__ out, int cout, int D, int H,
+                                                                  int W, int transposed) {
+  __shared__ float red[kKsGroups][kKsVox];
   const int HW = H * W;
   const int64_t N = (int64_t)D * HW;
-  const int64_t id = (int64_t)blockIdx.x * kVcThreads + threadIdx.x;
-  if (id >= N * cout) return;
-  const int64_t v = id % N;
-  const int co = (int)(id / N);
-  const int z = (int)(v / HW), r = (int)(v % HW);
-  const int y = r / W, x = r % W;
-  const int oz[3] = {((z + D - 1) % D) * HW, z * HW, ((z + 1) % D) * HW};
-  const int oy[3] = {((y + H - 1) % H) * W, y * W, ((y + 1) % H) * W};
-  const int ox[3] = {(x + W - 1) % W, x, (x + 1) % W};
-  float acc = bias ? bias[co] : 0.0f;
-  for (int ci = 0; ci < cin; ++ci) {
-    const float* base = in + (int64_t)ci * N;
-    const int64_t w0 = transposed ? ((int64_t)ci * cout + co) * 27 : ((int64_t)co * cin + ci) * 27;
+  const int lane = threadIdx.x % kKsVox, grp = threadIdx.x / kKsVox;
+  const int64_t v = (int64_t)blockIdx.x * kKsVox + lane;
+  const int co = blockIdx.y;
+  float acc = 0.0f;
+  if (v < N) {
+    const int z = (int)(v / HW), r = (int)(v % HW);
+    const int y = r / W, x = r % W;
+    const int oz[3] = {((z + D - 1) % D) * HW, z * HW, ((z + 1) % D) * HW};
+    const int oy[3] = {((y + H - 1) % H) * W, y * W, ((y + 1) % H) * W};
+    const int ox[3] = {(x + W - 1) % W, x, (x + 1) % W};
+    const int c0 = (int)((int64_t)cin * grp / kKsGroups), c1 = (int)((int64_t)cin * (grp + 1) / kKsGroups);
+    for (int ci = c0; ci < c1; ++ci) {
+      const float* base = in + (int64_t)ci * N;
+      const int64_t w0 = transposed ? ((int64_t)ci * cout + co) * 27 : ((int64_t)co * cin + ci) * 27;
 #pragma unroll
-    for (int t = 0; t < 27; ++t) {
-      const float xv = __ldg(base + oz[t / 9] + oy[(t / 3) % 3] + ox[t % 3]);
-      const float wv = __bfloat162float(w[w0 + (transposed ? 26 - t : t)]);
-      acc += wv * xv;
+      for (int t = 0; t < 27; ++t) {
+        const float xv = __ldg(base + oz[t / 9] + oy[(t / 3) % 3] + ox[t % 3]);
+        const float wv = __bfloat162float(w[w0 + (transposed ? 26 - t : t)]);
+        acc += wv * xv;
+      }
     }
   }
-  out[(int64_t)co * N + v] = acc;
+  red[grp][lane] = acc;
+  __syncthreads();
+  if (grp == 0 && v < N) {
+    float s = bias ? bias[co] : 0.0f;
+#pragma unroll
+    for (int g = 0; g < kKsGroups; ++g) s += red[g][lane];
+    out[(int64_t)co * N + v] = s;
+  }
 }
 
 // weight gradient of one (co, ci) pair over all voxels: gw[co][ci][tap] =
@@ -358,10 +368,10 @@ int gbofdft_nn_conv3d(const float* in, int cin, const void* w_bf16, const float*
   const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(w_bf16);
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t tiles = cout <= 16 ? 1 : (cout + 31) / 32;
-  if ((int64_t)nv * tiles < 76 && N * cout <= (int64_t)INT32_MAX) {
-    // too few k_conv3d CTAs for the GPU: one thread per (voxel, channel)
-    const unsigned nb = (unsigned)((N * cout + kVcThreads - 1) / kVcThreads);
-    k_conv3d_vc<<<nb, kVcThreads, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);
+  if ((int64_t)nv * tiles < 76 && cout <= 65535) {
+    // too few k_conv3d CTAs for the GPU: one CTA per (channel, 64 voxels)
+    const dim3 grid((unsigned)((N + kKsVox - 1) / kKsVox), (unsigned)cout);
+    k_conv3d_ks<<<grid, kKsVox * kKsGroups, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);
   } else if (cout <= 4) {
     k_conv3d<4><<<dim3(nv, 1), kVox, 0, st>>>(in, cin, wb, bias, out, cout, D, H, W, transposed);
   } else if (cout <= 16) {

@@ -27,9 +27,10 @@ def _bf16_round(a):
 @pytest.mark.parametrize("shape,cin,cout", [((4, 6, 8), 3, 37), ((8, 8, 8), 16, 32), ((2, 4, 2), 5, 1),
                                              ((16, 32, 160), 3, 37)])
 def test_conv_kernels(gn, shape, cin, cout):
-    """The CUDA-core convolution against the oracle: small grids run one thread
-    per (voxel, channel) (``k_conv3d_vc``), the 81920-voxel grid the voxel-tile
-    kernel (``k_conv3d``); both sum in the same order."""
+    """The CUDA-core convolution against the oracle: small grids run one CTA
+    per (channel, 64 voxels) with the input channels split over four thread
+    groups (``k_conv3d_ks``), the 81920-voxel grid the voxel-tile kernel
+    (``k_conv3d``)."""
     import torch
     rng = np.random.default_rng(2)
     layer = gn.Conv(cin, cout, rng)

@@ -49,7 +49,9 @@ DEFAULTS = {
     "refine": "split",
     # refinements that end in a line-search failure while the energy still
     # moved by more than econv are started again from their last density
-    "refine_restarts": 1,
+    # this many times (the 4000-atom LMGP solve ends the same either way: its
+    # restart stops after one step at the same energy)
+    "refine_restarts": 0,
     "refine_pred_stop": None,
     # relative energy resolution of the evaluations, for the line-search
     # acceptance on the derivative (mixed precision only): the PZ81 LDA is
@@ -238,11 +240,9 @@ class Optimization:
 
             r, out = refine(r64, r32)
             self.stats["stages"].append(dict(precision="fp64", **out))
-            # a refinement whose line search failed while it was still lowering
-            # the energy by more than econv starts again from where it stopped
-            # (once by default): functionals whose form moves with the density
-            # -- the LMGP k_F range only widens -- can make a line search fail
-            # far from the minimum, and a fresh start sees the settled form
+            # refine_restarts: a refinement whose line search failed while it
+            # was still lowering the energy by more than econv starts again
+            # from where it stopped
             for _ in range(int(o["refine_restarts"])):
                 h = out["history"]
                 if not (out["converged"] == 1 and len(h) >= 2 and abs(h[-1] - h[0]) > o["econv"]):

@@ -13,7 +13,7 @@ each structure's starting density comes from the guess network
 1.5 M parameters, run on 4x pooled features; trained on the solver's own
 converged densities of 2000 other snapshots, seeds 1000-2999; inference on the
 tensor cores inside the step, with the fallback check against the uniform
-density's residual), then FP32 truncated Newton and the FP64 refinement, 16
+density's residual), then FP32 truncated Newton and the FP64 refinement, 6
 structures in flight on their own streams.  The evaluators' set-up (pseudopotentials, Ewald, kernel
 tables, plans) is done before the timed steps, as the reference's timing
 excludes it.  ``value`` is the wall time of one step.  Beside it: the plain
@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--impl", default="gbofdft", choices=["gbofdft", "reference"])
     p.add_argument("--workload", default="alloy64", choices=["alloy64", "al256"])
     p.add_argument("--n", type=int, default=N_ALLOY, help="alloy snapshots in the batch (seeds 0..n-1)")
-    p.add_argument("--workers", type=int, default=16, help="structures in flight on the GPU")
+    p.add_argument("--workers", type=int, default=6, help="structures in flight on the GPU")
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
     p.add_argument("--no-plain", action="store_true", help="skip timing the FP64 plain path")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

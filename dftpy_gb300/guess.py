@@ -6,7 +6,8 @@ No reference counterpart: the reference starts from a uniform density or
 superposed atomic densities (``density/density.py:151-319``); those remain
 the network's inputs and its baseline.  The network predicts the correction
 to sqrt(rho_atom) (in units of sqrt(rho0), rho0 the mean density); the
-truncated-Newton optimiser always finishes from the guess and judges it.
+truncated-Newton optimiser always finishes from the guess, so the guess
+changes how many evaluations a solve takes, not where it ends.
 
 Architecture (all convolutions 3x3x3 and periodic, SiLU activations):
 ``levels`` resolutions, two convolutions per level on the way down (2x
@@ -14,7 +15,12 @@ average pooling between levels), 2x nearest upsampling, one convolution,
 an additive skip from the encoder and a second convolution per level on the
 way up, and a 1-channel head.  The network is fully convolutional at the
 grid spacing of the workloads (0.24 Bohr), so a net trained on small cells
-applies to any cell whose grid extents are divisible by 2^(levels-1).
+applies to any cell whose grid extents are divisible by its stride,
+2^(levels-1) times ``res``: with ``res`` 2 or 4 it runs on the 2x or 4x
+average-pooled features and its output is brought back by periodic
+trilinear 2x steps.  The alloy network (``data/guessnet.npz``) has 32-128
+channels on 4x pooled features; the Al network for Wang-Teter
+(``data/guessnet_al_wt.npz``) 16-64 channels at full resolution.
 Weights are BF16 for the arithmetic with FP32 master copies; every kernel
 (forward, input and weight gradients, pooling, activations, loss, Adam) is
 the project's own (``gbofdft_nn_*``).

@@ -28,10 +28,28 @@ __device__ double vline_eval(const gbofdft_vtable& t, double q) {
     const double dx = q / t.dp;
     return t.q4[0] + dx * (t.q4[1] + dx * (t.q4[2] + dx * (t.q4[3] + dx * t.q4[4]))) / 24.0;
   }
-  int lo = 0, hi = t.m - 1;  // x[lo] <= q < x[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(t.x + mid) <= q) lo = mid; else hi = mid;
+  // the interval x[lo] <= q < x[lo + 1]: first the index a uniform grid
+  // would give (the tables' usual case: two loads), else a bisection; both
+  // find the same interval
+  int lo;
+  {
+    int g = -1;
+    if (t.m >= 2) {
+      const double x0 = __ldg(t.x), xl = __ldg(t.x + t.m - 1);
+      const double f = xl > x0 ? (q - x0) / (xl - x0) * (double)(t.m - 1) : 0.0;
+      g = f < 0.0 ? 0 : (f > (double)(t.m - 2) ? t.m - 2 : (int)f);
+      if (!(__ldg(t.x + g) <= q && q < __ldg(t.x + g + 1))) g = -1;
+    }
+    if (g >= 0) {
+      lo = g;
+    } else {
+      lo = 0;
+      int hi = t.m - 1;  // x[lo] <= q < x[hi]
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(t.x + mid) <= q) lo = mid; else hi = mid;
+      }
+    }
   }
   const double u = q - __ldg(t.x + lo);
   const double* cc = t.c + 4 * (size_t)lo;

@@ -68,7 +68,7 @@ class TnOptions(ctypes.Structure):
                 ("xtol", ctypes.c_double), ("ncheck", ctypes.c_int), ("eps", ctypes.c_double),
                 ("pred_stop", ctypes.c_double), ("eres", ctypes.c_double), ("cg_rtol", ctypes.c_double),
                 ("pred_next", ctypes.c_int), ("precond", ctypes.c_int), ("time_evals", ctypes.c_int),
-                ("delta", ctypes.c_void_p), ("delta_rtol", ctypes.c_double)]
+                ("delta", ctypes.c_void_p), ("delta_rtol", ctypes.c_double), ("res0_max", ctypes.c_double)]
 
 
 class TnResult(ctypes.Structure):

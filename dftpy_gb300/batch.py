@@ -89,15 +89,30 @@ def _solve_one(job, options, stream, guess=None):
     per_atom = o.pop("econv_per_atom", None)
     if "econv" not in o:
         o["econv"] = per_atom * _natoms(total)
+    extra = {}
     with torch.cuda.stream(stream):
+        start = rho0
         if guess is not None:
-            rho0 = guess.guess(total, rho0.grid)
+            # the guess's residual check is left to the optimiser's first
+            # evaluation (no evaluation of its own); a rejected guess starts
+            # the solve again from the job's density
+            start = guess.guess(total, rho0.grid, defer_check=True)
+            lim = getattr(start, "start_residual_max", None)
+            if lim:
+                o["start_residual_max"] = float(lim)
         opt = Optimization(EnergyEvaluator=total, optimization_method="TN", optimization_options=o)
-        rho = opt.optimize_rho(guess_rho=rho0)
+        rho = opt.optimize_rho(guess_rho=start)
+        if opt.converged == 3:
+            rejected = opt.stats
+            o["start_residual_max"] = 0.0
+            opt = Optimization(EnergyEvaluator=total, optimization_method="TN", optimization_options=o)
+            rho = opt.optimize_rho(guess_rho=rho0)
+            opt.stats["stages"] = rejected["stages"] + opt.stats["stages"]
+            extra["guess_rejected"] = True
         energy = float(opt.energy)
         stream.synchronize()
     return BatchResult(rho=rho, energy=energy, converged=int(opt.converged), stats=opt.stats,
-                       wall_s=time.perf_counter() - t0, name=name)
+                       wall_s=time.perf_counter() - t0, name=name, extra=extra)
 
 
 def optimize_batch(jobs, workers=None, options=None, kedf="WGC", guess=None, **kedf_options):

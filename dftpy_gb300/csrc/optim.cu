@@ -572,6 +572,28 @@ static int tn_run(TnState& s, void* rho_io, const gbofdft_tn_options& o, gbofdft
   };
   double mu, energy, resN;
   if ((rc = mu_residual(mu, energy, resN))) return rc;
+  if (o.res0_max > 0.0) {
+    // the caller's check of its starting density: a residual above res0_max
+    // returns at once (rho_io untouched), converged = 3
+    if ((rc = ts_sync(s))) return rc;
+    const double r0 = sqrt(s.host[S_C] * dV);
+    if (!(r0 <= o.res0_max)) {
+      res->energy = energy;
+      res->mu = mu;
+      res->converged = 3;
+      res->n_iter = 0;
+      res->n_eval_ev = s.n_ev;
+      res->n_eval_v = s.n_v;
+      res->n_eval_hess = s.n_hv;
+      res->n_history = 0;
+      res->n_sync = s.n_sync;
+      res->t_sync = s.t_sync;
+      res->t_total = now_s() - s.t_start;
+      res->n_eval_delta = s.n_delta;
+      for (int k = 0; k < GBOFDFT_NE; ++k) res->energies[k] = s.host[S_EN + k];
+      return 0;
+    }
+  }
   const int hist_cap = res->history_cap;
   int nh = 0;
   double ehist_last[64];
@@ -813,6 +835,7 @@ int gbofdft_tn_options_default(gbofdft_tn_options* o) {
   o->time_evals = 0;
   o->delta = nullptr;
   o->delta_rtol = 1e-3;
+  o->res0_max = 0.0;
   return GBOFDFT_OK;
 }
 

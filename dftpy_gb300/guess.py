@@ -498,9 +498,16 @@ def uniform_residual(total, grid):
     rho0 = nel / grid.volume
     fusable = getattr(total, "fusable", None)
     if fusable is not None and fusable():
-        v = total.PSEUDO.vreal_of(torch.float64)
-        dv = v - v.mean()
-        return float(torch.sqrt((dv * dv).sum() * (rho0 * grid.dV)))
+        # a set-up quantity of the structure, like v_loc itself: kept with it
+        ps = total.PSEUDO
+        cache = ps.__dict__.setdefault("_uniform_residual", {})
+        key = (id(grid), id(ps.vreal_of(torch.float64)))
+        if key not in cache:
+            v = ps.vreal_of(torch.float64)
+            dv = v - v.mean()
+            cache.clear()
+            cache[key] = float(torch.sqrt((dv * dv).sum() * (rho0 * grid.dV)))
+        return cache[key]
     uni = DirectField(grid, data=torch.full(tuple(int(n) for n in grid.nrR), rho0, dtype=torch.float64,
                                             device="cuda"))
     return residual(total, uni)
@@ -518,7 +525,14 @@ class LearnedGuess:
     ``last_choice`` records the pick.  The default ratio 2 catches a broken
     guess, not a merely different one: this residual does not rank good
     starts (the 4000-atom LMGP cell's network density has 1.17x the uniform
-    density's residual yet needs far fewer evaluations from it)."""
+    density's residual yet needs far fewer evaluations from it).
+
+    ``guess(..., defer_check=True)`` leaves the residual comparison to the
+    optimiser: the density carries ``start_residual_max`` (fallback_ratio
+    times the uniform density's residual), which the TN compares with the
+    residual of its own first evaluation (``optimization`` option
+    ``start_residual_max``); ``batch.optimize_batch`` does this and starts
+    again from the uniform density when the TN rejects the guess."""
 
     def __init__(self, net, mix=None, fallback=True, fallback_ratio=2.0):
         self.net = net
@@ -539,7 +553,7 @@ class LearnedGuess:
         self.guess(total, grid)
         torch.cuda.synchronize()
 
-    def guess(self, total, grid=None, dtype=torch.float64):
+    def guess(self, total, grid=None, dtype=torch.float64, defer_check=False):
         from .field import DirectField
         grid = grid or total.PSEUDO.grid
         x, phib, rho0 = features(total, grid)
@@ -554,8 +568,12 @@ class LearnedGuess:
         out = DirectField(grid, data=rho.to(dtype))
         choice = "network"
         if self.fallback:
-            if not bool(torch.isfinite(rho).all()) or \
-                    not residual(total, out) < self.fallback_ratio * uniform_residual(total, grid):
+            if not bool(torch.isfinite(rho).all()):
+                out = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
+                choice = "uniform"
+            elif defer_check:
+                out.start_residual_max = self.fallback_ratio * uniform_residual(total, grid)
+            elif not residual(total, out) < self.fallback_ratio * uniform_residual(total, grid):
                 out = DirectField(grid, data=torch.full_like(rho, rho0_u).to(dtype))
                 choice = "uniform"
         self.last_choice = choice

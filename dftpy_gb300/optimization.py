@@ -52,6 +52,11 @@ DEFAULTS = {
     # this many times (the 4000-atom LMGP solve ends the same either way: its
     # restart stops after one step at the same energy)
     "refine_restarts": 0,
+    # > 0: the TN returns at once with converged = 3 (density unchanged) when
+    # the residual norm at the start is above it -- a caller's check of a
+    # starting density without an evaluation of its own (no reference
+    # counterpart)
+    "start_residual_max": 0.0,
     "refine_pred_stop": None,
     # relative energy resolution of the evaluations, for the line-search
     # acceptance on the derivative (mixed precision only): the PZ81 LDA is
@@ -127,7 +132,7 @@ class Optimization:
                                       "functionals (KEDF, XC, HARTREE, PSEUDO)")
 
     def _run(self, rho, econv, eps, maxiter, maxls=None, hess_rho=None, pred_stop=0.0, eres=0.0, ncheck=None,
-             cg_rtol=0.1, pred_next=False, precond=False, c2=None, delta=False):
+             cg_rtol=0.1, pred_next=False, precond=False, c2=None, delta=False, res0_max=0.0):
         o = self.optimization_options
         grid = rho.grid
         plan = grid.plan(rho.dtype)
@@ -138,6 +143,7 @@ class Optimization:
         opts.maxfun = int(o["maxfun"])
         opts.maxiter = int(maxiter)
         opts.maxls = int(o["maxls"] if maxls is None else maxls)
+        opts.res0_max = float(res0_max or 0.0)
         opts.c1, opts.c2, opts.xtol = float(o["c1"]), float(o["c2"] if c2 is None else c2), float(o["xtol"])
         opts.ncheck = int(o["ncheck"] if ncheck is None else ncheck)
         opts.eps = float(eps)
@@ -206,7 +212,7 @@ class Optimization:
             dt = torch.float64 if prec == "fp64" else torch.float32
             eps = o["eps"] if o["eps"] is not None else (1e-9 if dt == torch.float64 else o["fp32_eps"])
             r, out = self._run(rho.to(dt) if rho.dtype != dt else rho, o["econv"], eps, o["maxiter"],
-                               precond=bool(o["precond"]))
+                               precond=bool(o["precond"]), res0_max=o["start_residual_max"])
             self.stats["stages"].append(dict(precision=prec, **out))
         elif prec == "mixed":
             # FP32 until its energy changes by less than fp32_econv (default:
@@ -216,8 +222,12 @@ class Optimization:
             e32 = o["fp32_econv"] if o["fp32_econv"] is not None else max(o["econv"], 3.67e-7 * nat)
             r32, out32 = self._run(rho.to(torch.float32), e32, o["fp32_eps"], o["maxiter"],
                                    pred_stop=0.1 * e32, eres=o["fp32_eres"], ncheck=o["stage_ncheck"],
-                                   cg_rtol=o["fp32_cg_rtol"], precond=o["mixed_precond"], c2=o["fp32_c2"])
+                                   cg_rtol=o["fp32_cg_rtol"], precond=o["mixed_precond"], c2=o["fp32_c2"],
+                                   res0_max=o["start_residual_max"])
             self.stats["stages"].append(dict(precision="fp32", **out32))
+            if out32["converged"] == 3:
+                # the start was rejected (start_residual_max): no refinement
+                return self._finish(t_start, rho, out32)
             eps = o["eps"] if o["eps"] is not None else 1e-9
             # the FP32 stage conserves the electron number only to single
             # precision: restore the guess's integral before refining in FP64
@@ -258,6 +268,11 @@ class Optimization:
                 out = dict(out, converged=0)
         else:
             raise ValueError("precision must be 'fp64', 'fp32' or 'mixed', got %r" % (prec,))
+        if out["converged"] == 3:
+            return self._finish(t_start, rho, out)
+        return self._finish(t_start, r, out)
+
+    def _finish(self, t_start, r, out):
         self.stats["t_wall"] = time.perf_counter() - t_start
         self.stats["t_glue"] = self.stats["t_wall"] - sum(st["t_total"] for st in self.stats["stages"])
         self.converged = out["converged"]

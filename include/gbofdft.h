@@ -434,12 +434,19 @@ typedef struct gbofdft_tn_options {
                            full evaluation (NULL: every one in full FP64) */
   double delta_rtol;    /* rebase (full FP64 evaluation) when
                            ||rho - rho_ref|| > delta_rtol ||rho_ref|| */
+  double res0_max;      /* > 0: check the start -- when the residual norm
+                           sqrt(int ((V - mu) phi)^2) at the initial density
+                           exceeds it (or is not finite), return at once with
+                           converged = 3 and the density unchanged, so the
+                           caller can start again from another one; 0: off
+                           (no reference counterpart) */
 } gbofdft_tn_options;
 
 typedef struct gbofdft_tn_result {
   double energy;          /* total energy at the final density (Ha) */
   double mu;              /* chemical potential (Ha) */
-  int converged;          /* 0 converged, 1 line search failed, 2 maxiter */
+  int converged;          /* 0 converged, 1 line search failed, 2 maxiter,
+                             3 start rejected by res0_max */
   int n_iter;
   int n_eval_ev;          /* energy+potential evaluations */
   int n_eval_v;           /* potential-only evaluations */

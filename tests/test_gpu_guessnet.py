@@ -342,3 +342,32 @@ def test_half_resolution_network_gradients(gn):
             return float((full(enc2, dec2, head2) * c).sum())
         fd = (loss(e) - loss(-e)) / (2 * e)
         assert abs(g_gpu - fd) <= 2e-3 * max(1.0, abs(fd)), (lvl, which, idx, g_gpu, fd)
+
+
+def test_batch_leaves_the_guess_check_to_the_optimiser(gn):
+    """In ``optimize_batch`` the guess's residual check is the TN's own first
+    evaluation: a start whose residual is above ``start_residual_max``
+    returns at once (converged 3, density unchanged) and the batch starts
+    again from the uniform density.  A broken network (head scaled 50x) is
+    rejected and its solve ends where the uniform start's does; the
+    option alone rejects any start below its residual."""
+    import torch
+    from dftpy_gb300 import batch as B
+    from dftpy_gb300 import systems
+    from dftpy_gb300.optimization import Optimization
+    st = systems.fcc_supercell((2, 2, 2), sigma=0.15, seed=6, nr=(64, 64, 64), mg_fraction=0.2, name="defer")
+    total, rho_u = B.build_evaluator(st, kedf="WGC")
+    o = {"econv": 1e-8 * st.nat, "maxfun": 50, "maxiter": 100, "precision": "mixed",
+         "start_residual_max": 1e-12}
+    opt = Optimization(EnergyEvaluator=total, optimization_method="TN", optimization_options=o)
+    r = opt.optimize_rho(guess_rho=rho_u)
+    assert opt.converged == 3
+    assert torch.equal(r.as_subclass(torch.Tensor), rho_u.as_subclass(torch.Tensor))
+    bad_net = gn.GuessNet(channels=(16, 32, 48, 64), seed=11)
+    bad_net.head.w.mul_(50.0)
+    bad_net.head.sync_bf16()
+    opts = {"precision": "mixed", "econv_per_atom": 1e-8}
+    ref = B.optimize_batch([(total, rho_u)], workers=1, options=opts)[0]
+    res = B.optimize_batch([(total, rho_u)], workers=1, options=opts, guess=gn.LearnedGuess(bad_net))[0]
+    assert res.extra.get("guess_rejected") and res.converged == 0
+    assert abs(res.energy - ref.energy) * 27.211386 / st.nat <= 1e-8
